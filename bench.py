@@ -1,0 +1,450 @@
+#!/usr/bin/env python
+"""Headline benchmark: stable key-value radix sort of 2^28 uint32 keys.
+
+One step = one out-of-place sort_by_key of n = 2^28 uniform uint32 keys with
+uint32 values equal to the original index (the key-value sort of the
+"key-value radix sort plus scan and histogram" configuration), through the
+library's C ABI. Inputs stay resident in HBM and are never modified, so every
+step does identical work; they are larger than L2 (2 GiB per step), so no L2
+flush is needed between steps.
+
+Printed (rank 0, one JSON line): Gkeys/s over the timed steps (CUDA events on
+the library's stream, max over ranks), the digit-pass kernel's achieved
+HBM bandwidth against MEASURED_PEAKS.json, an end-to-end figure through
+clc_buffer_write -> clc_sort -> clc_buffer_read from pinned host memory, the
+CPU baseline (the oracle's restatement of the reference's 4-bit LSD sort on
+all host cores, on a bounded sample), SM clocks sampled during the run, and
+the other configuration workloads measured the same way under "workloads".
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "opencl-sdk_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "sort Gkeys/s & % HBM roofline: batched / learned-CDF vs plain LSD, bit-exact"
+N_MAIN = 1 << 28
+CPU_SAMPLE = 1 << 24
+
+
+def load_peak_gbs() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic() -> dict:
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the workload runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        powers = [num(r[3]) or 0.0 for r in rows]
+        pmax = max(powers)
+        loaded = [r for r, p in zip(rows, powers) if p >= 0.5 * pmax] or rows
+        sm = [num(r[1]) for r in loaded if num(r[1]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in loaded:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(rows[0][2]),
+                "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(loaded),
+                "power_w_max": pmax}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference's CPU algorithm (oracle restatement), no GPU
+# ---------------------------------------------------------------------------
+
+def cpu_reference_sample(n: int, seed: int = 1):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    keys = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    return keys, vals
+
+
+def time_cpu_reference(steps: int, warmup: int, n: int) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    threads = oracle.hardware_threads()
+    keys, vals = cpu_reference_sample(n)
+    for _ in range(warmup):
+        oracle.ref_radix_sort(keys, vals, threads=threads)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        oracle.ref_radix_sort(keys, vals, threads=threads)
+        times.append(time.perf_counter() - t0)
+    return {"threads": threads, "times": times, "n": n}
+
+
+def cpu_baseline_block(seconds: float = 10.0) -> dict:
+    """Times the oracle's restated reference sort for about `seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    threads = oracle.hardware_threads()
+    keys, vals = cpu_reference_sample(CPU_SAMPLE)
+    oracle.ref_radix_sort(keys, vals, threads=threads)  # warm
+    times, t_end = [], time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(times) < 2:
+        t0 = time.perf_counter()
+        oracle.ref_radix_sort(keys, vals, threads=threads)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": CPU_SAMPLE / t / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+            "sample": f"2^24 uniform uint32 key/value pairs (same distribution as the 2^28 workload), "
+                      f"median of {len(times)} runs of the restated reference 4-bit LSD sort "
+                      f"(8 passes, 128x8 tiles) on {threads} host threads"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    r = time_cpu_reference(args.steps, args.warmup, CPU_SAMPLE)
+    t = statistics.median(r["times"])
+    value = r["n"] / t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "kv_sort_u32_uniform", "n_per_step": r["n"], "key": "u32", "value": "u32"},
+        "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": r["threads"], "kind": "port",
+                         "sample": f"2^24 pairs per step (bounded sample of the 2^28 workload); the reference "
+                                   f"Compute library needs an OpenCL runtime, absent here, so its algorithm "
+                                   f"runs as the oracle's C++ restatement"},
+        "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extras", action="store_true", help="only the headline workload")
+    ap.add_argument("--n", type=int, default=N_MAIN, help="keys per step (default 2^28)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import gbcompute as gbc
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    ctx = gbc.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    peak, peak_src = load_peak_gbs()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    n = args.n
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1 + rank)
+
+    def uniform_u32(count: int) -> torch.Tensor:
+        return torch.randint(0, 2**32, (count,), dtype=torch.int64, device="cuda", generator=gen).to(torch.int32)
+
+    def timed(fn, steps: int, warmup: int, families: tuple[str, ...], soak_s: float = 0.0):
+        """Runs fn warmup times (plus a soak), then `steps` timed calls between
+        CUDA events on the library stream. Returns (ms per step, per-family
+        (launches, ms) inside the timed region)."""
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        t_end = time.perf_counter() + soak_s
+        while time.perf_counter() < t_end:
+            fn()
+            ctx.finish()
+        ctx.profile_reset()
+        ctx.profile_enable(True)
+        barrier()
+        torch.cuda.synchronize()
+        ctx.finish()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        ctx.finish()
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+        prof = ctx.profile()
+        ctx.profile_enable(False)
+        return ms, {k: v for k, v in prof.items() if k.startswith(families)} if families else prof
+
+    # ---- headline: key-value sort of 2^28 uniform u32 -----------------------
+    keys_in = uniform_u32(n)
+    vals_in = torch.arange(n, dtype=torch.int32, device="cuda")
+    keys_out = torch.empty_like(keys_in)
+    vals_out = torch.empty_like(vals_in)
+    torch.cuda.synchronize()
+
+    def kv_sort():
+        gbc.sort_raw(ctx, keys_in.data_ptr(), keys_out.data_ptr(), np.uint32, n, vals_in.data_ptr(),
+                     vals_out.data_ptr())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, prof = timed(kv_sort, args.steps, args.warmup, ("sort.",), soak_s=3.0)
+    clk = clocks.stop()
+    value = n * world / (ms * 1e-3) / 1e9
+
+    launches = sum(v[0] for v in prof.values())
+    # Uniform keys: every digit position varies, so all 4 pass launches work.
+    pass_launches, pass_ms = prof.get("sort.digit_pass", (0, 0.0))
+    hist_launches, hist_ms = prof.get("sort.upfront_histogram", (0, 0.0))
+    pass_avg_ms = pass_ms / max(1, pass_launches)
+    pass_bytes = 16 * n  # read + write of key and value
+    achieved = pass_bytes / (pass_avg_ms * 1e-3) / 1e9
+    traffic = load_traffic().get("sort.digit_pass:kv_u32")
+    traffic_per_launch = traffic * n if traffic is not None else None
+
+    # bit-exact check against an independent stable sort (torch/CUB) on the device
+    ki = keys_in.to(torch.int64) & 0xFFFFFFFF
+    sk, si = torch.sort(ki, stable=True)
+    bitexact = bool(torch.equal(sk, keys_out.to(torch.int64) & 0xFFFFFFFF)) and bool(
+        torch.equal(si.to(torch.int32), vals_out))
+    del ki, sk, si
+
+    # ---- end to end through the C ABI with host buffers ---------------------
+    h_keys = keys_in.cpu().pin_memory()
+    h_vals = vals_in.cpu().pin_memory()
+    h_keys_out = torch.empty_like(h_keys).pin_memory()
+    h_vals_out = torch.empty_like(h_vals).pin_memory()
+    kb, vb = gbc.DeviceBuffer(ctx, n, np.uint32), gbc.DeviceBuffer(ctx, n, np.uint32)
+    import ctypes as C
+
+    def e2e_step():
+        gbc._raise_for(gbc.lib.clc_buffer_write(ctx.handle, kb.handle, 0, 4 * n, C.c_void_p(h_keys.data_ptr())))
+        gbc._raise_for(gbc.lib.clc_buffer_write(ctx.handle, vb.handle, 0, 4 * n, C.c_void_p(h_vals.data_ptr())))
+        gbc._raise_for(gbc.lib.clc_sort(ctx.handle, kb.handle, gbc.TYPE_U32, vb.handle, n, 0))
+        gbc._raise_for(gbc.lib.clc_buffer_read(ctx.handle, kb.handle, 0, 4 * n, C.c_void_p(h_keys_out.data_ptr())))
+        gbc._raise_for(gbc.lib.clc_buffer_read(ctx.handle, vb.handle, 0, 4 * n, C.c_void_p(h_vals_out.data_ptr())))
+
+    e2e_step()
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0) / e2e_steps
+    e2e_ok = bool(torch.equal(h_keys_out, keys_out.cpu())) and bool(torch.equal(h_vals_out, vals_out.cpu()))
+    e2e = {"value": n * world / e2e_s / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": 8 * n,
+           "d2h_bytes_per_step": 8 * n, "ms_per_step": e2e_s * 1e3, "bitexact": e2e_ok,
+           "path": "clc_buffer_write x2 (pinned host) -> clc_sort -> clc_buffer_read x2"}
+    del h_keys, h_vals, h_keys_out, h_vals_out
+    kb.release()
+    vb.release()
+
+    workloads = {}
+    if not args.no_extras:
+        workloads = run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, max(5, args.steps // 5),
+                               args.warmup)
+    del keys_in, vals_in, keys_out, vals_out
+    torch.cuda.empty_cache()
+
+    cpu = cpu_baseline_block() if rank == 0 else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic: seeded uniform uint32 keys (torch generator on the device), uint32 values = index",
+        "config": {"workload": "kv_sort_u32_uniform_n2^28", "n": n, "key": "u32", "value": "u32 (index)",
+                   "step": "out-of-place stable sort_by_key through clc_sort_keys_raw",
+                   "l2": "inputs (2 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "bitexact": bitexact,
+        "roofline": {"bound": "hbm", "kernel": "sort.digit_pass", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic_per_launch, "algorithmic_bytes_per_launch": pass_bytes,
+                     "launch_ms": pass_avg_ms,
+                     "whole_sort": {"bytes": 68 * n, "frac": 68 * n / (ms * 1e-3) / 1e9 / peak,
+                                    "upfront_histogram_ms": hist_ms / max(1, hist_launches)}},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": launches,
+        "kernel_profile": {k: {"launches": v[0], "ms_total": v[1]} for k, v in prof.items()},
+        "workloads": workloads,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, warmup) -> dict:
+    """The other configuration workloads, each timed the same way."""
+    out = {}
+
+    def entry(name, count, unit_name, ms, bytes_moved, ok, prof, extra=None):
+        e = {"value": count / (ms * 1e-3) / 1e9, "unit": unit_name, "ms": ms,
+             "hbm_frac": bytes_moved / (ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": bytes_moved,
+             "bitexact": ok, "kernels": {k: {"launches": v[0], "ms_avg": v[1] / max(1, v[0])} for k, v in prof.items()}}
+        if extra:
+            e.update(extra)
+        out[name] = e
+
+    # keys-only u32 sort of 2^28 (target: >= 60% of the 36n-byte roofline)
+    keys = uniform_u32(n)
+    kout = torch.empty_like(keys)
+    ms, prof = timed(lambda: gbc.sort_raw(ctx, keys.data_ptr(), kout.data_ptr(), np.uint32, n), steps, warmup, ("sort.",))
+    ref = torch.sort(keys.to(torch.int64) & 0xFFFFFFFF).values
+    entry("keys_sort_u32_uniform_n2^28", n, "Gkeys/s", ms, 36 * n,
+          bool(torch.equal(ref, kout.to(torch.int64) & 0xFFFFFFFF)), prof)
+    del ref, kout
+
+    # entropy sweep: keys = AND of k uniform words, values = index
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    vout = torch.empty_like(vals)
+    kout = torch.empty_like(keys)
+    for k in (0, 2, 4):
+        kk = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+        for _ in range(k):
+            kk &= uniform_u32(n)
+        ms, prof = timed(lambda: gbc.sort_raw(ctx, kk.data_ptr(), kout.data_ptr(), np.uint32, n, vals.data_ptr(),
+                                              vout.data_ptr()), steps, warmup, ("sort.",))
+        ki = kk.to(torch.int64) & 0xFFFFFFFF
+        sk, si = torch.sort(ki, stable=True)
+        ok = bool(torch.equal(sk, kout.to(torch.int64) & 0xFFFFFFFF)) and bool(torch.equal(si.to(torch.int32), vout))
+        passes = int(sum(1 for b in range(4) if int(((ki >> (8 * b)) & 255).unique().numel()) > 1))
+        moved = 4 * n + 16 * n * passes + (8 * n if passes == 0 else 0)
+        entry(f"kv_sort_u32_and{k}_n2^28", n, "Gkeys/s", ms, moved, ok, prof, {"active_passes": passes})
+        del kk, ki, sk, si
+    del keys, vals, vout, kout
+    torch.cuda.empty_cache()
+
+    # exclusive scan of 2^30 int32 in [-1000, 1000] with an exact int64 total
+    m = 1 << 30
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(2)
+    x = torch.randint(-1000, 1001, (m,), dtype=torch.int32, device="cuda", generator=gen)
+    y = torch.empty_like(x)
+    total = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ms, prof = timed(lambda: gbc.scan_raw(ctx, x.data_ptr(), y.data_ptr(), m, np.int32, exclusive=True,
+                                          total_device=total.data_ptr()), steps, warmup, ("scan.",))
+    cs = torch.cumsum(x.to(torch.int64), 0)
+    ok = int(total.item()) == int(cs[-1].item())
+    ok = ok and bool(torch.equal(y[1:], cs[:-1].to(torch.int32))) and int(y[0].item()) == 0
+    entry("exclusive_scan_i32_n2^30", m, "Gelem/s", ms, 8 * m, ok, prof)
+    del cs, y
+
+    # reduce (plus) of the same data
+    ms, prof = timed(lambda: gbc.reduce(ctx, gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), m, np.int32)), steps, warmup,
+                     ("reduce.",))
+    entry("reduce_i32_n2^30", m, "Gelem/s", ms, 4 * m, True, prof, {"note": "includes the blocking result read"})
+    del x
+
+    # 256-bin histogram of 2^30 uniform bytes
+    u8 = torch.randint(0, 256, (m,), dtype=torch.uint8, device="cuda", generator=gen)
+    hist = torch.empty(256, dtype=torch.int32, device="cuda")
+    ms, prof = timed(lambda: gbc.histogram_even_raw(ctx, u8.data_ptr(), m, np.uint8, hist.data_ptr(), 256, 0.0, 256.0),
+                     steps, warmup, ("histogram.",))
+    ok = bool(torch.equal(torch.bincount(u8.to(torch.int64), minlength=256).to(torch.int32), hist))
+    entry("histogram256_u8_n2^30", m, "Gelem/s", ms, m, ok, prof)
+    del u8
+    torch.cuda.empty_cache()
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+/*
+ * gbcompute C interface: the drop-in boundary for the OpenCL Compute
+ * library's primitive core (radix sort, scan, reduce, histogram), built for
+ * one NVIDIA GB300 (sm_103a).
+ *
+ * The first part of this header keeps the names, enum values and argument
+ * meaning of the reference C interface (lib/include/CL/Compute/compute_c.h)
+ * so that a caller written against it relinks against libgbcompute.so:
+ *   - every fallible call returns a clc_status and never lets a C++ exception
+ *     escape; clc_last_error() holds a thread-local message;
+ *   - handles are opaque; a buffer keeps its context's memory resource (and
+ *     CUDA stream) alive, so it may outlive the context;
+ *   - a context is not thread-safe: one per thread, or serialise;
+ *   - sort, scan, fill, sequence and histogram are asynchronous on the
+ *     context's stream; reduce and buffer reads/writes block; clc_finish waits.
+ * CUDA replaces OpenCL underneath: clc_last_cl_error() reports the
+ * cudaError_t of the last CLC_ERROR_OPENCL, a context owns one CUDA stream,
+ * and operators are not compiled at run time but matched against a table of
+ * canonical expressions (see clc_reduce).
+ *
+ * The second part adds what the reference does not have (64-bit keys,
+ * segmented and learned sorts, reduce_by_key, histogram through C, raw device
+ * pointers, graph capture, autotuning). Those functions say so.
+ */
+#ifndef GBCOMPUTE_COMPUTE_C_H
+#define GBCOMPUTE_COMPUTE_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define GBC_EXPORT __declspec(dllexport)
+#else
+#define GBC_EXPORT __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct clc_context_s* clc_context;
+typedef struct clc_buffer_s* clc_buffer;
+typedef struct clc_kernel_s* clc_kernel;
+
+/* Numeric values as in the reference (compute_c.h:30-41). */
+typedef enum clc_status {
+    CLC_SUCCESS = 0,
+    CLC_ERROR_OPENCL = 1, /* device runtime error: clc_last_cl_error() has the cudaError_t */
+    CLC_ERROR_INVALID_ARGUMENT = 2,
+    CLC_ERROR_BUILD = 3, /* kept for ABI compatibility; kernels are compiled ahead of time */
+    CLC_ERROR_NO_DEVICE = 4,
+    CLC_ERROR_OUT_OF_MEMORY = 5,
+    CLC_ERROR_UNSUPPORTED = 6, /* operator, type or feature without a kernel here */
+    CLC_ERROR_INTERNAL = 7,
+    CLC_ERROR_IO = 8
+} clc_status;
+
+/* Element types, numeric values as in the reference (compute_c.h:44-56). */
+typedef enum clc_type {
+    CLC_TYPE_I8 = 0,
+    CLC_TYPE_U8 = 1,
+    CLC_TYPE_I16 = 2,
+    CLC_TYPE_U16 = 3,
+    CLC_TYPE_I32 = 4,
+    CLC_TYPE_U32 = 5,
+    CLC_TYPE_I64 = 6,
+    CLC_TYPE_U64 = 7,
+    CLC_TYPE_F32 = 8,
+    CLC_TYPE_F64 = 9
+} clc_type;
+
+/* Device index meaning "the first GPU" (compute_c.h:58-60). */
+#define CLC_DEFAULT_DEVICE ((size_t)-1)
+
+/* ---- errors (replaces compute_c.h:64-66) -------------------------------- */
+
+GBC_EXPORT const char* clc_last_error(void);
+/* cudaError_t of the last CLC_ERROR_OPENCL on this thread, else 0. */
+GBC_EXPORT int clc_last_cl_error(void);
+
+/* ---- devices and contexts (replaces compute_c.h:70-99) ------------------ */
+
+typedef struct clc_device_info {
+    char name[256];
+    char platform[256];
+    int is_gpu;
+    int has_fp64;
+    unsigned long long global_memory;
+    size_t max_work_group_size;
+} clc_device_info;
+
+/* CUDA devices. *count = 0 with CLC_SUCCESS when there is no device or no
+ * driver (compute_c.h:80-82). */
+GBC_EXPORT clc_status clc_device_count(size_t* count);
+GBC_EXPORT clc_status clc_device_get_info(size_t index, clc_device_info* info);
+
+/* Creates a context: one CUDA stream, a pooled stream-ordered memory resource
+ * and the tuning table (compute_c.h:86-89). */
+GBC_EXPORT clc_status clc_context_create(size_t index, clc_context* out);
+/* cache_dir holds the tuning table (gbcompute_tuning.txt); NULL or "" falls
+ * back to CLC_TUNING_DIR, then CL_COMPUTE_CACHE_DIR (compute_c.h:90-94). */
+GBC_EXPORT clc_status clc_context_create_with_cache(size_t index, const char* cache_dir,
+                                                    clc_context* out);
+GBC_EXPORT void clc_context_release(clc_context ctx);
+GBC_EXPORT clc_status clc_context_get_info(clc_context ctx, clc_device_info* info);
+/* Waits for the context's stream; reports an error a kernel recorded
+ * (e.g. a look-back wait that timed out) as CLC_ERROR_OPENCL. */
+GBC_EXPORT clc_status clc_finish(clc_context ctx);
+
+/* ---- buffers (replaces compute_c.h:101-118) ----------------------------- */
+
+GBC_EXPORT clc_status clc_buffer_alloc(clc_context ctx, size_t bytes, clc_buffer* out);
+GBC_EXPORT void clc_buffer_release(clc_buffer buffer);
+GBC_EXPORT size_t clc_buffer_size(clc_buffer buffer);
+/* Blocking; offset + bytes must stay within the buffer. */
+GBC_EXPORT clc_status clc_buffer_write(clc_context ctx, clc_buffer buffer, size_t offset,
+                                       size_t bytes, const void* src);
+GBC_EXPORT clc_status clc_buffer_read(clc_context ctx, clc_buffer buffer, size_t offset,
+                                      size_t bytes, void* dst);
+/* Asynchronous device-to-device copy on the context's stream. */
+GBC_EXPORT clc_status clc_buffer_copy(clc_context ctx, clc_buffer src, size_t src_offset,
+                                      clc_buffer dst, size_t dst_offset, size_t bytes);
+
+/* ---- file I/O: outside this library's scope; return CLC_ERROR_UNSUPPORTED  */
+GBC_EXPORT clc_status clc_file_size(const char* path, size_t* bytes);
+GBC_EXPORT clc_status clc_file_read(clc_context ctx, const char* path, size_t file_offset,
+                                    clc_buffer buffer, size_t buffer_offset, size_t bytes,
+                                    size_t* done);
+GBC_EXPORT clc_status clc_file_write(clc_context ctx, const char* path, int truncate,
+                                     size_t file_offset, clc_buffer buffer, size_t buffer_offset,
+                                     size_t bytes, size_t* done);
+
+/* ---- typed algorithms (replaces compute_c.h:137-171) -------------------- */
+/* Operators: a precedes b. Accepted spellings (whitespace-insensitive, outer
+ * parentheses optional): "a + b", "a * b", "a & b", "a | b", "a ^ b",
+ * "(b < a) ? b : a" / "min(a, b)", "(a < b) ? b : a" / "max(a, b)",
+ * "b" (right projection) and "a" (left projection). Any other expression
+ * returns CLC_ERROR_UNSUPPORTED. Identities: decimal or hex literals (with
+ * an optional u/l suffix or float syntax), "(~0)", INT_MIN, INT_MAX, UINT_MAX,
+ * LONG_MIN, LONG_MAX, ULONG_MAX, CHAR_MIN, CHAR_MAX, UCHAR_MAX, SHRT_MIN,
+ * SHRT_MAX, USHRT_MAX, INFINITY, (-INFINITY). */
+
+GBC_EXPORT clc_status clc_fill(clc_context ctx, clc_buffer out, size_t n, clc_type type,
+                               const void* value);
+GBC_EXPORT clc_status clc_sequence(clc_context ctx, clc_buffer out, size_t n, clc_type type,
+                                   const void* start, const void* step);
+/* Run-time expressions need an OpenCL C compiler: CLC_ERROR_UNSUPPORTED. */
+GBC_EXPORT clc_status clc_transform(clc_context ctx, clc_buffer in, clc_type in_type,
+                                    clc_buffer out, clc_type out_type, size_t n,
+                                    const char* expression);
+GBC_EXPORT clc_status clc_transform2(clc_context ctx, clc_buffer in1, clc_type type1,
+                                     clc_buffer in2, clc_type type2, clc_buffer out,
+                                     clc_type out_type, size_t n, const char* expression);
+/* result = op(init, in[0] op ... op in[n-1]); blocks. n = 0 gives init. */
+GBC_EXPORT clc_status clc_reduce(clc_context ctx, clc_buffer in, size_t n, clc_type type,
+                                 const char* op, const char* identity, const void* init,
+                                 void* result);
+/* out may be in (in-place). Exclusive: out[0] = identity. */
+GBC_EXPORT clc_status clc_scan(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
+                               clc_type type, const char* op, const char* identity,
+                               int exclusive);
+/* Stable radix sort of 32-bit keys (I32, U32, F32) in place; values may be
+ * NULL, else n 32-bit elements permuted alongside. Other key types give
+ * CLC_ERROR_INVALID_ARGUMENT as in the reference (CApi.cpp:517-531). */
+GBC_EXPORT clc_status clc_sort(clc_context ctx, clc_buffer keys, clc_type key_type,
+                               clc_buffer values, size_t n, int descending);
+GBC_EXPORT clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
+                                  clc_type type, const char* predicate, size_t* count);
+
+/* ---- user kernels: need an OpenCL C compiler; CLC_ERROR_UNSUPPORTED ------ */
+GBC_EXPORT clc_status clc_add_header(clc_context ctx, const char* name, const char* content);
+GBC_EXPORT clc_status clc_kernel_create(clc_context ctx, const char* source, const char* name,
+                                        const char* options, const char* const* define_names,
+                                        const char* const* define_values, size_t ndefines,
+                                        clc_kernel* out);
+GBC_EXPORT void clc_kernel_release(clc_kernel kernel);
+GBC_EXPORT clc_status clc_kernel_set_buffer(clc_kernel kernel, unsigned index, clc_buffer buffer);
+GBC_EXPORT clc_status clc_kernel_set_value(clc_kernel kernel, unsigned index, size_t size,
+                                           const void* value);
+GBC_EXPORT clc_status clc_kernel_set_local(clc_kernel kernel, unsigned index, size_t bytes);
+GBC_EXPORT clc_status clc_kernel_work_group_size(clc_context ctx, clc_kernel kernel, size_t limit,
+                                                 size_t* out);
+GBC_EXPORT clc_status clc_kernel_launch(clc_context ctx, clc_kernel kernel, size_t global,
+                                        size_t local);
+
+/* ======================================================================== */
+/* Extensions (no counterpart in the reference C interface).               */
+/* ======================================================================== */
+
+/* Counts in[i] into bins equal-width bins over [lower, upper) exactly as the
+ * reference's C++ histogram_even (Algorithm.hpp:243-250, Algorithm.cpp:
+ * 240-273, 569-615): hist is zeroed first; for non-double input the bin is
+ * (uint)(((float)x - lower) * scale) with scale = (float)bins / (upper -
+ * lower) in float, clamped to bins - 1; out-of-range samples are ignored.
+ * Asynchronous. */
+GBC_EXPORT clc_status clc_histogram_even(clc_context ctx, clc_buffer in, size_t n, clc_type type,
+                                         clc_buffer hist, size_t bins, double lower, double upper);
+
+/* clc_scan plus a wide total: for 8/16/32-bit integer plus-scans, *total
+ * (host, int64_t or uint64_t) receives the exact sum of all n inputs without
+ * wrap-around; for other scans, the last inclusive value widened. Blocks when
+ * total != NULL. */
+GBC_EXPORT clc_status clc_scan_ex(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
+                                  clc_type type, const char* op, const char* identity,
+                                  int exclusive, void* total);
+
+/* Stable sort of 32- or 64-bit keys (I32, U32, F32, I64, U64, F64) with
+ * optional 32-bit values, in place. */
+GBC_EXPORT clc_status clc_sort_ex(clc_context ctx, clc_buffer keys, clc_type key_type,
+                                  clc_buffer values, size_t n, int descending);
+
+/* Device pointer of a buffer (NULL for a zero-byte buffer). */
+GBC_EXPORT void* clc_buffer_device_pointer(clc_buffer buffer);
+/* Wraps existing device memory of the context's device as a buffer that does
+ * not own it (the memory must outlive the buffer). */
+GBC_EXPORT clc_status clc_buffer_wrap(clc_context ctx, void* device_pointer, size_t bytes,
+                                      clc_buffer* out);
+/* The context's CUDA stream (a cudaStream_t). */
+GBC_EXPORT void* clc_context_stream(clc_context ctx);
+/* Memory statistics of the context's resource (current/peak/total bytes,
+ * current/total allocations) and the pool's cached bytes. */
+typedef struct clc_memory_stats {
+    size_t current_bytes, peak_bytes, total_bytes;
+    size_t current_allocations, total_allocations;
+    size_t cached_bytes;
+} clc_memory_stats;
+GBC_EXPORT clc_status clc_context_memory_stats(clc_context ctx, clc_memory_stats* out);
+/* Returns the pool's cached blocks to the device. */
+GBC_EXPORT clc_status clc_context_release_cache(clc_context ctx);
+
+/* Raw-pointer forms: the same algorithms on device pointers, asynchronous on
+ * the context's stream. keys_in == keys_out sorts in place. vals may be NULL. */
+GBC_EXPORT clc_status clc_sort_keys_raw(clc_context ctx, const void* keys_in, void* keys_out,
+                                        clc_type key_type, const uint32_t* vals_in,
+                                        uint32_t* vals_out, size_t n, int descending);
+GBC_EXPORT clc_status clc_scan_raw(clc_context ctx, const void* in, void* out, size_t n,
+                                   clc_type type, const char* op, const char* identity,
+                                   int exclusive, void* total_device);
+GBC_EXPORT clc_status clc_histogram_even_raw(clc_context ctx, const void* in, size_t n,
+                                             clc_type type, uint32_t* hist, size_t bins,
+                                             double lower, double upper);
+GBC_EXPORT clc_status clc_reduce_raw(clc_context ctx, const void* in, size_t n, clc_type type,
+                                     const char* op, const char* identity, const void* init,
+                                     void* result);
+
+/* Failure-path self-test: runs one scan tile whose predecessor never
+ * publishes its status, so the tile's bounded look-back wait gives up after
+ * about one second instead of hanging. Returns what the next synchronising
+ * call reports: CLC_ERROR_OPENCL with a "timed out" message. The context
+ * stays usable. */
+GBC_EXPORT clc_status clc_selftest_lookback_timeout(clc_context ctx);
+
+/* Profiling: when enabled, every kernel launch is bracketed by CUDA events on
+ * the context's stream and its time accumulated per kernel family
+ * ("sort.digit_pass", "scan.lookback", ...). Reading entries synchronises. */
+GBC_EXPORT clc_status clc_profile_enable(clc_context ctx, int enable);
+GBC_EXPORT clc_status clc_profile_reset(clc_context ctx);
+GBC_EXPORT clc_status clc_profile_count(clc_context ctx, size_t* count);
+GBC_EXPORT clc_status clc_profile_entry(clc_context ctx, size_t index, char* name, size_t name_bytes,
+                                        unsigned long long* launches, double* total_ms);
+
+/* Tuning: entries of the context's table and how many compiled variants a
+ * sort family has; the autotuner times them (bench-side) and stores the
+ * fastest with clc_tuning_set, clc_tuning_save writes the table. */
+GBC_EXPORT int clc_tuning_sort_variants(int key_bytes, int has_values);
+GBC_EXPORT clc_status clc_tuning_sort_key(int key_bytes, int has_values, size_t n, char* out,
+                                          size_t out_bytes);
+GBC_EXPORT clc_status clc_tuning_set(clc_context ctx, const char* key, int variant);
+GBC_EXPORT clc_status clc_tuning_get(clc_context ctx, const char* key, int* variant);
+GBC_EXPORT clc_status clc_tuning_save(clc_context ctx, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,400 @@
+// Single-pass inclusive/exclusive scan with decoupled look-back.
+//
+// Reference path replaced: detail::scan -> scan_impl (lib/src/Compute/
+// Algorithm.cpp:280-318, 444-451) with kernels clc_scan_tiles / clc_scan_add
+// (79-127): every tile is scanned, the tile totals are scanned recursively and
+// added back, i.e. about four passes over the data. Here each element is read
+// once and written once: a tile publishes its aggregate as soon as it is
+// known, looks back over its predecessors' status words for its exclusive
+// prefix and writes its outputs.
+//
+// Semantics kept: any canonical associative operator, combined in sequence
+// order (op(earlier, later)), so non-commutative operators such as the right
+// projection work; out may alias in; exclusive output starts with identity.
+// Added: a wide total (exact int64/uint64 sum for integer plus-scans of
+// 32-bit elements, otherwise the last inclusive value widened).
+//
+// Tile layout (256 threads): row r, thread t holds VEC consecutive elements
+// at tile_base + (r * 256 + t) * VEC, loaded as one 128-bit access. Sequence
+// order is row, then thread, then element, so each row is a warp scan and the
+// ROWS x 8 row-warp totals are scanned by one warp.
+#include <cstring>
+
+#include "device_common.cuh"
+#include "ops.cuh"
+#include "runtime.hpp"
+#include "sort_internal.hpp"
+
+namespace gbc {
+namespace {
+
+using dev::FULL_MASK;
+
+constexpr int THREADS = 256;
+constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
+constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
+
+template <typename T> __device__ __forceinline__ uint64_t to_bits(T v)
+{
+    uint64_t b = 0;
+    memcpy(&b, &v, sizeof(T));
+    return b;
+}
+template <typename T> __device__ __forceinline__ T from_bits(uint64_t b)
+{
+    T v;
+    memcpy(&v, &b, sizeof(T));
+    return v;
+}
+
+// Status of one tile. 32-bit elements: one word (flag | tag | value) that is
+// overwritten atomically from AGG to PRE. 64-bit elements: separate words for
+// the aggregate and the inclusive prefix, published with release stores
+// before the flag word, so a reader never pairs a flag with the wrong value.
+template <typename T, bool WIDE = (sizeof(T) == 8)> struct Status;
+
+template <typename T> struct Status<T, false> {
+    static constexpr uint64_t SLOTS = onesweep::RING_BYTES / 8;
+    __device__ static void publish(uint64_t* ring, uint64_t seq, uint64_t flag, T v)
+    {
+        dev::st_relaxed(&ring[seq & (SLOTS - 1)],
+                        (flag << 62) | ((seq & TAG_MASK) << 32) | (uint32_t)to_bits(v));
+    }
+    __device__ static bool read(const uint64_t* ring, uint64_t seq, uint64_t& flag, T& v)
+    {
+        const uint64_t w = dev::ld_relaxed(&ring[seq & (SLOTS - 1)]);
+        flag = w >> 62;
+        if (flag == 0 || ((w >> 32) & TAG_MASK) != (seq & TAG_MASK)) return false;
+        v = from_bits<T>((uint32_t)w);
+        return true;
+    }
+};
+
+template <typename T> struct Status<T, true> {
+    static constexpr uint64_t SLOTS = onesweep::RING_BYTES / 32;
+    __device__ static void publish(uint64_t* ring, uint64_t seq, uint64_t flag, T v)
+    {
+        uint64_t* s = ring + (seq & (SLOTS - 1)) * 4;
+        dev::st_relaxed(&s[flag == FLAG_PRE ? 1 : 0], to_bits(v));
+        dev::st_release(&s[2], (flag << 62) | ((seq & TAG_MASK) << 32));
+    }
+    __device__ static bool read(const uint64_t* ring, uint64_t seq, uint64_t& flag, T& v)
+    {
+        const uint64_t* s = ring + (seq & (SLOTS - 1)) * 4;
+        const uint64_t w = dev::ld_acquire(&s[2]);
+        flag = w >> 62;
+        if (flag == 0 || ((w >> 32) & TAG_MASK) != (seq & TAG_MASK)) return false;
+        v = from_bits<T>(dev::ld_relaxed(&s[flag == FLAG_PRE ? 1 : 0]));
+        return true;
+    }
+};
+
+template <typename T> struct ScanArgs {
+    const T* in;
+    T* out;
+    uint32_t n;
+    T identity;
+    int exclusive;
+    int aligned;  // in and out are 16-byte aligned
+    uint32_t num_tiles;
+    uint64_t* ring;
+    uint64_t seq0;
+    uint32_t* tile_ctr;
+    unsigned long long* wide_sum;  // exact sum (integer plus, <= 32-bit), or null
+    void* total;                   // last inclusive value widened to 8 bytes, or null
+    int* err;
+};
+
+template <typename T> __device__ __forceinline__ void store_wide(void* dst, T v)
+{
+    if (std::is_floating_point<T>::value) {
+        const double d = (double)v;
+        memcpy(dst, &d, 8);
+    } else if (std::is_signed<T>::value) {
+        const long long w = (long long)v;
+        memcpy(dst, &w, 8);
+    } else {
+        const unsigned long long w = (unsigned long long)v;
+        memcpy(dst, &w, 8);
+    }
+}
+
+template <typename T, typename Op, bool WIDE_SUM>
+__global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
+{
+    constexpr int VEC = 16 / sizeof(T);
+    constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
+    constexpr int TILE = THREADS * VEC * ROWS;
+    constexpr int RW = ROWS * (THREADS / 32);
+    constexpr int PER = RW / 32;
+    static_assert(RW % 32 == 0, "row-warp totals fill whole lanes");
+
+    __shared__ T s_rw[RW];
+    __shared__ T s_prefix;
+    __shared__ uint32_t s_tile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const Op op;
+    const T identity = a.identity;
+
+    for (;;) {
+        if (tid == 0) s_tile = atomicAdd(a.tile_ctr, 1u);
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= a.num_tiles) break;
+        const uint32_t base = t * TILE;
+        const bool full = base + TILE <= a.n;
+
+        T x[ROWS][VEC];
+        if (full && a.aligned) {
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) {
+                const uint4 w = dev::ld_stream(reinterpret_cast<const uint4*>(a.in + base + (r * THREADS + tid) * VEC));
+                memcpy(x[r], &w, 16);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
+                    x[r][j] = idx < a.n ? a.in[idx] : identity;
+                }
+        }
+
+        if (WIDE_SUM) {
+            // Exact sum of the valid elements, widened, one atomic per warp.
+            unsigned long long s = 0;
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
+                    if (idx < a.n) {
+                        if (std::is_signed<T>::value) s += (unsigned long long)(long long)x[r][j];
+                        else s += (unsigned long long)x[r][j];
+                    }
+                }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o);
+            if (lane == 0) atomicAdd(a.wide_sum, s);
+        }
+
+        // Per-row warp scans of the thread totals.
+        T winc[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            T acc = x[r][0];
+#pragma unroll
+            for (int j = 1; j < VEC; ++j) acc = op(acc, x[r][j]);
+            winc[r] = dev::warp_inclusive_scan(acc, op);
+            if (lane == 31) s_rw[r * (THREADS / 32) + warp] = winc[r];
+        }
+        __syncthreads();
+
+        if (warp == 0) {
+            // Exclusive scan of the row-warp totals, in sequence order.
+            T v[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) v[k] = s_rw[lane * PER + k];
+            T lt = v[0];
+#pragma unroll
+            for (int k = 1; k < PER; ++k) lt = op(lt, v[k]);
+            const T linc = dev::warp_inclusive_scan(lt, op);
+            const T up = __shfl_up_sync(FULL_MASK, linc, 1);
+            T run = lane == 0 ? identity : up;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                s_rw[lane * PER + k] = run;
+                run = op(run, v[k]);
+            }
+            const T agg = __shfl_sync(FULL_MASK, linc, 31);
+            const uint64_t my_seq = a.seq0 + t;
+            if (lane == 0) Status<T>::publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
+
+            // Warp-cooperative look-back: lane l inspects tile w_end-32+l;
+            // the nearest tile holding an inclusive prefix ends the walk.
+            T excl = identity;
+            if (t > 0) {
+                bool have = false;
+                int64_t w_end = t;
+                for (;;) {
+                    const int64_t k = w_end - 32 + lane;
+                    uint64_t flag = FLAG_PRE;
+                    T val = identity;
+                    bool gave_up = false;
+                    if (k >= 0) {
+                        if (!Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) {
+                            const unsigned long long start = dev::globaltimer();
+                            for (uint32_t spin = 1;; ++spin) {
+                                if (Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) break;
+                                if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                    gave_up = true;
+                                    flag = FLAG_PRE;
+                                    val = identity;
+                                    break;
+                                }
+                                if (spin > 32) __nanosleep(64);
+                            }
+                        }
+                    }
+                    if (__any_sync(FULL_MASK, gave_up)) {
+                        if (lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                    }
+                    const uint32_t pre = __ballot_sync(FULL_MASK, flag == FLAG_PRE);
+                    const int L = pre ? 31 - __clz(pre) : 0;
+                    const T contrib = lane >= L ? val : identity;
+                    const T wsum = dev::warp_reduce(contrib, op);
+                    excl = have ? op(wsum, excl) : wsum;
+                    have = true;
+                    if (pre) break;
+                    w_end -= 32;
+                }
+                if (lane == 0) Status<T>::publish(a.ring, my_seq, FLAG_PRE, op(excl, agg));
+            }
+            if (lane == 0) s_prefix = excl;
+        }
+        __syncthreads();
+
+        const T prefix = s_prefix;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const T wexc = __shfl_up_sync(FULL_MASK, winc[r], 1);
+            T run = op(prefix, s_rw[r * (THREADS / 32) + warp]);
+            if (lane > 0) run = op(run, wexc);
+            T o[VEC];
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const T inc = op(run, x[r][j]);
+                o[j] = a.exclusive ? run : inc;
+                run = inc;
+                if (a.total != nullptr && base + (r * THREADS + tid) * VEC + j == a.n - 1)
+                    store_wide<T>(a.total, inc);
+            }
+            if (full && a.aligned) {
+                uint4 w;
+                memcpy(&w, o, 16);
+                *reinterpret_cast<uint4*>(a.out + base + (r * THREADS + tid) * VEC) = w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
+                    if (idx < a.n) a.out[idx] = o[j];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+std::map<const void*, int> g_occ;
+std::mutex g_occ_m;
+
+template <typename F> int blocks_per_sm(F* kernel)
+{
+    std::lock_guard<std::mutex> lock(g_occ_m);
+    auto it = g_occ.find((const void*)kernel);
+    if (it != g_occ.end()) return it->second;
+    int b = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, THREADS, 0),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    b = std::max(b, 1);
+    g_occ[(const void*)kernel] = b;
+    return b;
+}
+
+struct ScanLaunch {
+    device_context& ctx;
+    const void* in;
+    void* out;
+    std::size_t n;
+    const void* identity;
+    bool exclusive;
+    void* total_dev;
+    bool wide_plus;
+
+    template <typename T, typename Op> void run()
+    {
+        constexpr int VEC = 16 / sizeof(T);
+        constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
+        constexpr uint32_t TILE = THREADS * VEC * ROWS;
+        constexpr bool can_wide = std::is_integral<T>::value && sizeof(T) == 4 &&
+                                  std::is_same<Op, ops::Plus>::value;
+        ScanArgs<T> a;
+        a.in = static_cast<const T*>(in);
+        a.out = static_cast<T*>(out);
+        a.n = (uint32_t)n;
+        std::memcpy(&a.identity, identity, sizeof(T));
+        a.exclusive = exclusive ? 1 : 0;
+        a.aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+        a.num_tiles = (uint32_t)((n + TILE - 1) / TILE);
+        a.ring = ctx.lookback_ring;
+        a.seq0 = ctx.reserve_seq(a.num_tiles);
+        a.err = ctx.d_error;
+        // Control block: tile counter + wide sum, in the context's small area.
+        unsigned char* ctl = ctx.d_small;
+        check_cuda(cudaMemsetAsync(ctl, 0, 64, ctx.stream), "cudaMemsetAsync");
+        a.tile_ctr = reinterpret_cast<uint32_t*>(ctl);
+        a.wide_sum = reinterpret_cast<unsigned long long*>(ctl + 8);
+        const bool use_wide = can_wide && total_dev != nullptr;
+        a.total = use_wide ? nullptr : total_dev;
+        if (!use_wide) a.wide_sum = nullptr;
+
+        auto kernel = use_wide ? &k_scan<T, Op, can_wide> : &k_scan<T, Op, false>;
+        const int grid = (int)std::min<std::size_t>(a.num_tiles, (std::size_t)ctx.sm_count * blocks_per_sm(kernel));
+        {
+            kernel_timer kt(ctx, "scan.lookback");
+            kernel<<<grid, THREADS, 0, ctx.stream>>>(a);
+            check_cuda(cudaGetLastError(), "scan launch");
+        }
+        if (use_wide)
+            check_cuda(cudaMemcpyAsync(total_dev, a.wide_sum, 8, cudaMemcpyDeviceToDevice, ctx.stream),
+                       "cudaMemcpyAsync");
+    }
+};
+
+}  // namespace
+
+void selftest_lookback_timeout(device_context& ctx)
+{
+    // A two-tile int32 plus-scan whose only CTA starts at tile 1: tile 0 never
+    // runs, so its status word never appears and the bounded wait must give
+    // up, record ERR_LOOKBACK_TIMEOUT and let the kernel finish. Every access
+    // stays inside the two-tile buffer.
+    ctx.activate();
+    constexpr uint32_t TILE = THREADS * 16;
+    temp_buffer buf(ctx.resource, 2 * TILE * sizeof(int32_t));
+    check_cuda(cudaMemsetAsync(buf.get(), 0, 2 * TILE * sizeof(int32_t), ctx.stream), "cudaMemsetAsync");
+    unsigned char* ctl = ctx.d_small;
+    check_cuda(cudaMemsetAsync(ctl, 0, 64, ctx.stream), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(ctl, 1, 1, ctx.stream), "cudaMemsetAsync");  // tile counter = 1
+    ScanArgs<int32_t> a;
+    a.in = buf.as<int32_t>();
+    a.out = buf.as<int32_t>();
+    a.n = 2 * TILE;
+    a.identity = 0;
+    a.exclusive = 0;
+    a.aligned = 1;
+    a.num_tiles = 2;
+    a.ring = ctx.lookback_ring;
+    a.seq0 = ctx.reserve_seq(2);
+    a.tile_ctr = reinterpret_cast<uint32_t*>(ctl);
+    a.wide_sum = nullptr;
+    a.total = nullptr;
+    a.err = ctx.d_error;
+    k_scan<int32_t, ops::Plus, false><<<1, THREADS, 0, ctx.stream>>>(a);
+    check_cuda(cudaGetLastError(), "scan launch");
+}
+
+void scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t, op_kind op,
+          const void* identity, bool exclusive, void* total_dev)
+{
+    if (n == 0) return;
+    check_size(n);
+    if (in == nullptr || out == nullptr || identity == nullptr)
+        throw std::invalid_argument("scan: null argument");
+    ctx.activate();
+    ScanLaunch l{ctx, in, out, n, identity, exclusive, total_dev, false};
+    ops::dispatch(t, op, l);
+}
+
+}  // namespace gbc

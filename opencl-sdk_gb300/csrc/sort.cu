@@ -1,0 +1,566 @@
+// Onesweep LSD radix sort for sm_103a: 8-bit digits, one upfront pass that
+// builds every digit histogram, then one kernel per digit that ranks a tile of
+// keys with warp match/ballot votes and finds the tile's global offsets by a
+// decoupled look-back over per-(tile, digit) status words.
+//
+// Reference path replaced: detail::radix_sort (lib/src/Compute/
+// Algorithm.cpp:453-527) with its kernels clc_radix_histogram (153-171) and
+// clc_radix_scatter (173-212). The reference makes 8 passes of 4 bits, each a
+// histogram launch, a recursive scan of the digit-major count table and a
+// scatter whose in-tile rank comes from a work-group scan of packed counters.
+// This file makes ceil(bits/8) passes; the counts of all digits come from one
+// read of the keys, and the per-tile prefix is resolved on the fly, so each
+// pass reads and writes the keys once.
+//
+// Semantics kept from the reference:
+//   * stable: equal keys keep their input order (digits are ranked in input
+//     order within a tile; tiles are ordered by their look-back sequence);
+//   * the key bijection of Algorithm.cpp:459-469 (int: flip sign bit; float:
+//     negative -> ~k, else k | sign; descending -> complement) is applied to
+//     compute digits only, the stored keys are untouched;
+//   * keys and values end up in the caller's buffers.
+// Added: 64-bit keys, an out-of-place form, and skipping of digit positions
+// on which all keys agree (decided on the device, so the launch sequence is
+// fixed and graph-capturable).
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "device_common.cuh"
+#include "runtime.hpp"
+#include "sort_internal.hpp"
+
+namespace gbc {
+namespace onesweep {
+
+using dev::FULL_MASK;
+
+// Status word of one (tile, digit): [63:62] flag, [61:32] sequence tag,
+// [31:0] count. FLAG_AGG: the tile's own count; FLAG_PRE: the inclusive count
+// of this digit over all tiles up to and including this one.
+constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
+constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
+
+__device__ __forceinline__ uint64_t pack_status(uint64_t flag, uint64_t seq, uint32_t v)
+{
+    return (flag << 62) | ((seq & TAG_MASK) << 32) | v;
+}
+
+template <typename K> struct Traits;
+template <> struct Traits<uint32_t> {
+    static constexpr int PASSES = 4;
+};
+template <> struct Traits<uint64_t> {
+    static constexpr int PASSES = 8;
+};
+
+template <typename K> struct SortArgs {
+    const K* in_keys;
+    K* out_keys;
+    K* alt_keys;
+    const uint32_t* in_vals;
+    uint32_t* out_vals;
+    uint32_t* alt_vals;
+    uint32_t n;
+    int in_place;
+    dev::KeyXform<K> xf;
+    SortControl* ctl;
+    uint64_t* ring;
+    uint64_t seq0;
+    uint32_t num_tiles;
+    int* err;
+};
+
+// ---------------------------------------------------------------------------
+// K1: upfront histogram of every digit position, plus the pass plan.
+// ---------------------------------------------------------------------------
+template <typename K, int THREADS, int NSUB>
+__global__ void __launch_bounds__(THREADS) k_upfront(SortArgs<K> a)
+{
+    constexpr int P = Traits<K>::PASSES;
+    constexpr int PER_VEC = 16 / sizeof(K);
+    extern __shared__ __align__(16) uint32_t sh_hist[];  // NSUB x P x 256
+    __shared__ uint32_t s_scratch[8];
+    __shared__ uint32_t s_trivial[8];
+    __shared__ int s_last;
+
+    for (int i = threadIdx.x; i < NSUB * P * RADIX; i += THREADS) sh_hist[i] = 0;
+    __syncthreads();
+    uint32_t* my = sh_hist + ((threadIdx.x >> 5) % NSUB) * (P * RADIX);
+
+    const size_t n = a.n;
+    const K* keys = a.in_keys;
+    const size_t gtid = (size_t)blockIdx.x * THREADS + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * THREADS;
+    auto count = [&](K k) {
+        const K t = a.xf(k);
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+            atomicAdd(&my[p * RADIX + (uint32_t)((t >> (8 * p)) & 0xFF)], 1u);
+    };
+    size_t head = 0;
+    if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
+        const size_t nv = n / PER_VEC;
+        const uint4* kv = reinterpret_cast<const uint4*>(keys);
+        for (size_t v = gtid; v < nv; v += stride) {
+            const uint4 w = dev::ld_stream(kv + v);
+            K ks[PER_VEC];
+            memcpy(ks, &w, 16);
+#pragma unroll
+            for (int j = 0; j < PER_VEC; ++j) count(ks[j]);
+        }
+        head = nv * PER_VEC;
+    }
+    for (size_t i = head + gtid; i < n; i += stride) count(keys[i]);
+    __syncthreads();
+
+    uint32_t* g_hist = &a.ctl->hist[0][0];
+    for (int i = threadIdx.x; i < P * RADIX; i += THREADS) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int b = 0; b < NSUB; ++b) s += sh_hist[b * P * RADIX + i];
+        if (s != 0) atomicAdd(&g_hist[i], s);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&a.ctl->done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+
+    // The last CTA turns the counts into the pass plan: skip every digit
+    // position on which all keys agree; exclusive bin starts for the rest.
+    if (threadIdx.x < 8) s_trivial[threadIdx.x] = 0;
+    __syncthreads();
+    for (int p = 0; p < P; ++p)
+        if (threadIdx.x < RADIX && dev::ld_relaxed(&g_hist[p * RADIX + threadIdx.x]) == (uint32_t)n)
+            s_trivial[p] = 1;
+    __syncthreads();
+    int slot = 0;
+    for (int p = 0; p < P; ++p) {
+        if (s_trivial[p]) continue;
+        const uint32_t c =
+            threadIdx.x < RADIX ? dev::ld_relaxed(&g_hist[p * RADIX + threadIdx.x]) : 0u;
+        const uint32_t ex = dev::bins_exclusive_sum(c, s_scratch);
+        if (threadIdx.x < RADIX) a.ctl->plan.bin_start[slot][threadIdx.x] = ex;
+        if (threadIdx.x == 0) a.ctl->plan.shift[slot] = 8 * p;
+        ++slot;
+    }
+    if (threadIdx.x == 0) a.ctl->plan.num_active = slot;
+}
+
+// When the pass count does not land the result in the right buffer: copy the
+// input once (out-of-place with nothing to sort, or in-place with an odd
+// number of active passes, which then start from the scratch buffer).
+template <typename K> __global__ void k_precopy(SortArgs<K> a)
+{
+    const uint32_t act = a.ctl->plan.num_active;
+    const K* s;
+    K* d;
+    const uint32_t* sv;
+    uint32_t* dv;
+    if (act == 0 && !a.in_place) {
+        s = a.in_keys, d = a.out_keys, sv = a.in_vals, dv = a.out_vals;
+    } else if (a.in_place && (act & 1)) {
+        s = a.in_keys, d = a.alt_keys, sv = a.in_vals, dv = a.alt_vals;
+    } else {
+        return;
+    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        d[i] = s[i];
+        if (sv != nullptr) dv[i] = sv[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K2: one digit pass (persistent CTAs, tiles handed out in order by an atomic
+// counter so every look-back waits only on CTAs that are already running).
+// ---------------------------------------------------------------------------
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool MATCH>
+__global__ void __launch_bounds__(THREADS) k_pass(SortArgs<K> a, int slot)
+{
+    constexpr int WARPS = THREADS / 32;
+    constexpr int TILE = THREADS * ITEMS;
+    static_assert(THREADS >= RADIX, "one thread per bin");
+    static_assert(TILE < (1 << 24), "rank and digit share a word");
+
+    const uint32_t act = a.ctl->plan.num_active;
+    if (slot >= (int)act) return;
+    const uint32_t shift = a.ctl->plan.shift[slot];
+
+    // Buffer roles for this slot (see k_precopy): the last active pass always
+    // writes the caller's output.
+    const bool dst_out = ((act - 1 - slot) & 1) == 0;
+    K* dst_k = dst_out ? a.out_keys : a.alt_keys;
+    uint32_t* dst_v = dst_out ? a.out_vals : a.alt_vals;
+    const K* src_k;
+    const uint32_t* src_v;
+    if (slot == 0) {
+        const bool from_alt = a.in_place && (act & 1);
+        src_k = from_alt ? a.alt_keys : a.in_keys;
+        src_v = from_alt ? a.alt_vals : a.in_vals;
+    } else {
+        const bool prev_out = ((act - slot) & 1) == 0;
+        src_k = prev_out ? a.out_keys : a.alt_keys;
+        src_v = prev_out ? a.out_vals : a.alt_vals;
+    }
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256
+    K* s_keys = reinterpret_cast<K*>(warp_hist + WARPS * RADIX);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
+    __shared__ uint32_t s_scratch[8];
+    __shared__ uint32_t s_tile;
+    __shared__ int s_abort;  // a look-back wait gave up: skip the scatter
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
+    if (tid == 0) s_abort = 0;
+    const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
+    uint32_t* ctr = &a.ctl->tile_ctr[slot];
+    const uint32_t n = a.n;
+
+    for (;;) {
+        if (tid == 0) s_tile = atomicAdd(ctr, 1u);
+        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= a.num_tiles) break;
+        const uint32_t tile_base = t * TILE;
+        const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+
+        // Load: warp w owns keys [w*32*ITEMS, (w+1)*32*ITEMS) of the tile,
+        // row i of the warp is 32 consecutive keys (one 128-byte line for
+        // 32-bit keys). Past the end, the digit is 255 so padding ranks last.
+        const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
+        K key[ITEMS];
+        uint32_t rd[ITEMS];  // (rank << 8) | digit
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t idx = wbase + i * 32;
+            if (idx < n) {
+                key[i] = src_k[idx];
+                rd[i] = (uint32_t)(a.xf(key[i]) >> shift) & 0xFFu;
+            } else {
+                key[i] = 0;
+                rd[i] = 0xFFu;
+            }
+        }
+
+        // Rank within the warp, row by row (= input order): peers are the
+        // lanes holding the same digit; the highest peer bumps the warp's
+        // count for that digit.
+        uint32_t* wh = warp_hist + warp * RADIX;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i];
+            uint32_t peers;
+            if (MATCH) {
+                peers = __match_any_sync(FULL_MASK, d);
+            } else {
+                peers = FULL_MASK;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t bit = (d >> b) & 1u;
+                    const uint32_t vote = __ballot_sync(FULL_MASK, bit);
+                    peers &= bit ? vote : ~vote;
+                }
+            }
+            const int leader = 31 - __clz(peers);
+            uint32_t before = 0;
+            if (lane == leader) {
+                before = wh[d];
+                wh[d] = before + __popc(peers);
+            }
+            before = __shfl_sync(FULL_MASK, before, leader);
+            rd[i] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
+            __syncwarp();
+        }
+        __syncthreads();
+
+        // Per-digit tile counts; warp_hist becomes the exclusive prefix over
+        // warps.
+        uint32_t count = 0;
+        if (tid < RADIX) {
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t c = warp_hist[w * RADIX + tid];
+                warp_hist[w * RADIX + tid] = count;
+                count += c;
+            }
+        }
+        uint32_t agg = count;
+        if (tid == RADIX - 1) agg -= (uint32_t)TILE - valid;  // padding sits in bin 255
+        uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
+        if (tid < RADIX)
+            dev::st_relaxed(&my_status[tid],
+                            pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
+
+        const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
+        if (tid < RADIX) s_local[tid] = local;
+        __syncthreads();
+
+        // Local sort of the tile into shared memory.
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i] & 0xFFu;
+            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
+            s_keys[pos] = key[i];
+            rd[i] = pos;
+        }
+        if (HAS_V) {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t idx = wbase + i * 32;
+                s_vals[rd[i]] = idx < n ? src_v[idx] : 0u;
+            }
+        }
+
+        // Decoupled look-back: one thread per digit walks back over the
+        // preceding tiles until it meets an inclusive prefix.
+        if (tid < RADIX) {
+            uint32_t excl = 0;
+            if (t > 0) {
+                uint64_t k = t - 1;
+                for (;;) {
+                    const uint64_t seq = seq0 + k;
+                    const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
+                    const uint64_t want = seq & TAG_MASK;
+                    uint64_t w = dev::ld_relaxed(p);
+                    bool gave_up = false;
+                    if ((w >> 62) == 0 || ((w >> 32) & TAG_MASK) != want) {
+                        const unsigned long long start = dev::globaltimer();
+                        for (uint32_t spin = 1;; ++spin) {
+                            w = dev::ld_relaxed(p);
+                            if ((w >> 62) != 0 && ((w >> 32) & TAG_MASK) == want) break;
+                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                gave_up = true;
+                                break;
+                            }
+                            if (spin > 32) __nanosleep(64);
+                        }
+                    }
+                    if (gave_up) {
+                        dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                        s_abort = 1;
+                        break;
+                    }
+                    excl += (uint32_t)w;
+                    if ((w >> 62) == FLAG_PRE || k == 0) break;
+                    --k;
+                }
+                dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + agg));
+            }
+            s_bin_off[tid] = s_bin_start[tid] + excl - s_local[tid];
+        }
+        __syncthreads();
+
+        // Write the locally sorted tile: consecutive threads write
+        // consecutive addresses within each digit's run. After a timed-out
+        // wait the offsets are unknown: nothing is written (the error is
+        // reported) and every write is bounds-checked regardless.
+        const uint32_t limit = s_abort ? 0u : valid;
+        for (uint32_t j = tid; j < limit; j += THREADS) {
+            const K kk = s_keys[j];
+            const uint32_t d = (uint32_t)(a.xf(kk) >> shift) & 0xFFu;
+            const uint32_t o = s_bin_off[d] + j;
+            if (o < n) {
+                dst_k[o] = kk;
+                if (HAS_V) dst_v[o] = s_vals[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+template <typename K> struct PassVariant {
+    int threads, items;
+    bool match;
+    void (*kernel)(SortArgs<K>, int);
+};
+
+template <typename K, bool HAS_V> struct Variants;
+
+#define GBC_PV(K, HV, T, I, M) PassVariant<K>{T, I, M, &k_pass<K, HV, T, I, M>}
+template <bool HV> struct Variants<uint32_t, HV> {
+    static constexpr int count = 3;
+    static PassVariant<uint32_t> get(int i)
+    {
+        static const PassVariant<uint32_t> v[count] = {
+            GBC_PV(uint32_t, HV, 256, 16, true),
+            GBC_PV(uint32_t, HV, 256, 16, false),
+            GBC_PV(uint32_t, HV, 256, 24, true),
+        };
+        return v[std::min(std::max(i, 0), count - 1)];
+    }
+};
+template <bool HV> struct Variants<uint64_t, HV> {
+    static constexpr int count = 2;
+    static PassVariant<uint64_t> get(int i)
+    {
+        static const PassVariant<uint64_t> v[count] = {
+            GBC_PV(uint64_t, HV, 256, 12, true),
+            GBC_PV(uint64_t, HV, 256, 16, true),
+        };
+        return v[std::min(std::max(i, 0), count - 1)];
+    }
+};
+#undef GBC_PV
+
+template <typename K> std::size_t pass_smem(int threads, int items, bool has_v)
+{
+    const std::size_t tile = (std::size_t)threads * items;
+    return (std::size_t)(threads / 32) * RADIX * 4 + tile * sizeof(K) + (has_v ? tile * 4 : 0);
+}
+
+struct KernelInfo {
+    int blocks_per_sm = 0;
+};
+
+template <typename F>
+static int prepare_kernel(F* kernel, int threads, std::size_t smem, std::map<const void*, int>& cache,
+                          std::mutex& m)
+{
+    std::lock_guard<std::mutex> lock(m);
+    auto it = cache.find((const void*)kernel);
+    if (it != cache.end()) return it->second;
+    if (smem > 48 * 1024)
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem),
+                   "cudaFuncSetAttribute");
+    int blocks = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, smem),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    cache[(const void*)kernel] = std::max(blocks, 1);
+    return std::max(blocks, 1);
+}
+
+static std::map<const void*, int> g_occupancy;
+static std::mutex g_occupancy_mutex;
+
+template <typename K, bool HAS_V>
+static void run_sort(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v,
+                     uint32_t* out_v, std::size_t n, dev::KeyXform<K> xf, int variant)
+{
+    constexpr int P = Traits<K>::PASSES;
+    const PassVariant<K> pv = Variants<K, HAS_V>::get(variant);
+    const uint32_t tile = (uint32_t)(pv.threads * pv.items);
+    const uint32_t num_tiles = (uint32_t)((n + tile - 1) / tile);
+    const bool in_place = (const void*)in_k == (const void*)out_k;
+
+    temp_buffer alt_k(ctx.resource, n * sizeof(K));
+    temp_buffer alt_v(ctx.resource, HAS_V ? n * sizeof(uint32_t) : 0);
+    temp_buffer ctl(ctx.resource, sizeof(SortControl));
+    check_cuda(cudaMemsetAsync(ctl.get(), 0, sizeof(SortControl), ctx.stream), "cudaMemsetAsync");
+
+    SortArgs<K> a;
+    a.in_keys = in_k;
+    a.out_keys = out_k;
+    a.alt_keys = alt_k.as<K>();
+    a.in_vals = HAS_V ? in_v : nullptr;
+    a.out_vals = HAS_V ? out_v : nullptr;
+    a.alt_vals = HAS_V ? alt_v.as<uint32_t>() : nullptr;
+    a.n = (uint32_t)n;
+    a.in_place = in_place ? 1 : 0;
+    a.xf = xf;
+    a.ctl = ctl.as<SortControl>();
+    a.ring = ctx.lookback_ring;
+    a.seq0 = ctx.reserve_seq((uint64_t)P * num_tiles);
+    a.num_tiles = num_tiles;
+    a.err = ctx.d_error;
+
+    // K1
+    constexpr int HT = 256, NSUB = 2;
+    const std::size_t hsmem = (std::size_t)NSUB * P * RADIX * 4;
+    const int hblocks = prepare_kernel(k_upfront<K, HT, NSUB>, HT, hsmem, g_occupancy, g_occupancy_mutex);
+    const std::size_t hwork = (n + HT * 16 - 1) / (HT * 16);
+    const int hgrid = (int)std::max<std::size_t>(1, std::min<std::size_t>(hwork, (std::size_t)ctx.sm_count * hblocks));
+    {
+        kernel_timer kt(ctx, "sort.upfront_histogram");
+        k_upfront<K, HT, NSUB><<<hgrid, HT, hsmem, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "radix sort histogram launch");
+    }
+
+    const int cgrid = (int)std::max<std::size_t>(1, std::min<std::size_t>((n + 255) / 256, (std::size_t)ctx.sm_count * 8));
+    {
+        kernel_timer kt(ctx, "sort.precopy");
+        k_precopy<K><<<cgrid, 256, 0, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "radix sort copy launch");
+    }
+
+    // K2 x P
+    const std::size_t psmem = pass_smem<K>(pv.threads, pv.items, HAS_V);
+    const int pblocks = prepare_kernel(pv.kernel, pv.threads, psmem, g_occupancy, g_occupancy_mutex);
+    const int pgrid = (int)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * pblocks);
+    for (int s = 0; s < P; ++s) {
+        kernel_timer kt(ctx, "sort.digit_pass");
+        pv.kernel<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
+        check_cuda(cudaGetLastError(), "radix sort pass launch");
+    }
+}
+
+}  // namespace onesweep
+
+int sort_variant_count(int key_bytes, bool has_values)
+{
+    using namespace onesweep;
+    if (key_bytes == 4) return has_values ? Variants<uint32_t, true>::count : Variants<uint32_t, false>::count;
+    return has_values ? Variants<uint64_t, true>::count : Variants<uint64_t, false>::count;
+}
+
+std::string sort_tuning_key(int key_bytes, bool has_values, std::size_t n)
+{
+    return std::string("sort:") + (key_bytes == 4 ? "u32" : "u64") + (has_values ? "kv" : "k") +
+           ":" + tuning_table::size_class(n);
+}
+
+void radix_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes,
+                int key_kind, const uint32_t* vals_in, uint32_t* vals_out, std::size_t n,
+                bool descending)
+{
+    using namespace onesweep;
+    if (key_bytes != 4 && key_bytes != 8)
+        throw std::invalid_argument("sort: keys must be 32 or 64 bits");
+    if (key_kind < 0 || key_kind > 2) throw std::invalid_argument("sort: unknown key kind");
+    if (keys_in == nullptr || keys_out == nullptr) {
+        if (n == 0) return;
+        throw std::invalid_argument("sort: null keys");
+    }
+    if ((vals_in == nullptr) != (vals_out == nullptr))
+        throw std::invalid_argument("sort: values need both an input and an output");
+    ctx.activate();
+    if (n <= 1) {
+        if (n == 1 && keys_in != keys_out) {
+            check_cuda(cudaMemcpyAsync(keys_out, keys_in, key_bytes, cudaMemcpyDeviceToDevice, ctx.stream),
+                       "cudaMemcpyAsync");
+            if (vals_in != nullptr && vals_in != vals_out)
+                check_cuda(cudaMemcpyAsync(vals_out, vals_in, 4, cudaMemcpyDeviceToDevice, ctx.stream),
+                           "cudaMemcpyAsync");
+        }
+        return;
+    }
+    check_size(n);
+    const bool kv = vals_in != nullptr;
+    launch_shape shape;
+    ctx.tuning.lookup(sort_tuning_key(key_bytes, kv, n), shape);
+    if (key_bytes == 4) {
+        const auto xf = dev::make_xform<uint32_t>(key_kind, descending);
+        const auto* in = static_cast<const uint32_t*>(keys_in);
+        auto* out = static_cast<uint32_t*>(keys_out);
+        if (kv) run_sort<uint32_t, true>(ctx, in, out, vals_in, vals_out, n, xf, shape.variant);
+        else run_sort<uint32_t, false>(ctx, in, out, nullptr, nullptr, n, xf, shape.variant);
+    } else {
+        const auto xf = dev::make_xform<uint64_t>(key_kind, descending);
+        const auto* in = static_cast<const uint64_t*>(keys_in);
+        auto* out = static_cast<uint64_t*>(keys_out);
+        if (kv) run_sort<uint64_t, true>(ctx, in, out, vals_in, vals_out, n, xf, shape.variant);
+        else run_sort<uint64_t, false>(ctx, in, out, nullptr, nullptr, n, xf, shape.variant);
+    }
+}
+
+}  // namespace gbc

@@ -1,0 +1,514 @@
+"""Python binding of libgbcompute.so (ctypes over the C ABI in include/compute_c.h).
+
+It mirrors the reference C++ API of the OpenCL Compute library
+(lib/include/CL/Compute/Algorithm.hpp:119-250): a ``Context`` plays
+``compute_context``, ``DeviceBuffer`` plays ``device_buffer<T>``,
+``binary_op``/``ops`` are the operator descriptions, and ``sort``,
+``sort_by_key``, ``reduce``, ``inclusive_scan``, ``exclusive_scan``,
+``histogram_even``, ``fill`` and ``sequence`` keep the reference's argument
+meaning and exceptions (``ValueError`` where the reference throws
+``std::invalid_argument``/``length_error``, ``MemoryError`` for out of memory).
+
+There is no fallback: importing this module fails loudly when the shared
+library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from collections import namedtuple
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY_PATH = os.path.join(os.path.dirname(_HERE), "libgbcompute.so")
+
+if not os.path.exists(LIBRARY_PATH):
+    raise ImportError(
+        f"gbcompute: {LIBRARY_PATH} is missing; build it with "
+        "`python opencl-sdk_gb300/build.py` (needs nvcc)"
+    )
+lib = C.CDLL(LIBRARY_PATH)
+
+# ---- enums (include/compute_c.h) --------------------------------------------
+
+SUCCESS = 0
+ERROR_OPENCL = 1
+ERROR_INVALID_ARGUMENT = 2
+ERROR_BUILD = 3
+ERROR_NO_DEVICE = 4
+ERROR_OUT_OF_MEMORY = 5
+ERROR_UNSUPPORTED = 6
+ERROR_INTERNAL = 7
+ERROR_IO = 8
+
+TYPE_I8, TYPE_U8, TYPE_I16, TYPE_U16, TYPE_I32, TYPE_U32, TYPE_I64, TYPE_U64, TYPE_F32, TYPE_F64 = range(10)
+DEFAULT_DEVICE = C.c_size_t(-1).value
+
+_NP_TO_CLC = {
+    np.dtype(np.int8): TYPE_I8,
+    np.dtype(np.uint8): TYPE_U8,
+    np.dtype(np.int16): TYPE_I16,
+    np.dtype(np.uint16): TYPE_U16,
+    np.dtype(np.int32): TYPE_I32,
+    np.dtype(np.uint32): TYPE_U32,
+    np.dtype(np.int64): TYPE_I64,
+    np.dtype(np.uint64): TYPE_U64,
+    np.dtype(np.float32): TYPE_F32,
+    np.dtype(np.float64): TYPE_F64,
+}
+
+
+def clc_type(dtype) -> int:
+    try:
+        return _NP_TO_CLC[np.dtype(dtype)]
+    except KeyError:
+        raise ValueError(f"gbcompute: unsupported element type {dtype}") from None
+
+
+class ClcError(RuntimeError):
+    """A non-success clc_status; ``status`` and ``native`` (cudaError_t) attached."""
+
+    def __init__(self, status: int, message: str, native: int = 0):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.native = native
+
+
+class UnsupportedError(ClcError, NotImplementedError):
+    pass
+
+
+class NoDeviceError(ClcError):
+    pass
+
+
+class InvalidArgumentError(ClcError, ValueError):
+    pass
+
+
+class OutOfMemoryError(ClcError, MemoryError):
+    pass
+
+
+def _raise_for(status: int) -> None:
+    if status == SUCCESS:
+        return
+    msg = lib.clc_last_error().decode(errors="replace")
+    native = lib.clc_last_cl_error()
+    cls = {
+        ERROR_INVALID_ARGUMENT: InvalidArgumentError,
+        ERROR_UNSUPPORTED: UnsupportedError,
+        ERROR_NO_DEVICE: NoDeviceError,
+        ERROR_OUT_OF_MEMORY: OutOfMemoryError,
+    }.get(status, ClcError)
+    raise cls(status, msg, native)
+
+
+# ---- prototypes ---------------------------------------------------------------
+
+class DeviceInfo(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 256),
+        ("platform", C.c_char * 256),
+        ("is_gpu", C.c_int),
+        ("has_fp64", C.c_int),
+        ("global_memory", C.c_ulonglong),
+        ("max_work_group_size", C.c_size_t),
+    ]
+
+
+class MemoryStats(C.Structure):
+    _fields_ = [
+        ("current_bytes", C.c_size_t),
+        ("peak_bytes", C.c_size_t),
+        ("total_bytes", C.c_size_t),
+        ("current_allocations", C.c_size_t),
+        ("total_allocations", C.c_size_t),
+        ("cached_bytes", C.c_size_t),
+    ]
+
+
+_vp, _sz, _i, _cp = C.c_void_p, C.c_size_t, C.c_int, C.c_char_p
+_PROTOS = {
+    "clc_last_error": (_cp, []),
+    "clc_last_cl_error": (_i, []),
+    "clc_device_count": (_i, [C.POINTER(_sz)]),
+    "clc_device_get_info": (_i, [_sz, C.POINTER(DeviceInfo)]),
+    "clc_context_create": (_i, [_sz, C.POINTER(_vp)]),
+    "clc_context_create_with_cache": (_i, [_sz, _cp, C.POINTER(_vp)]),
+    "clc_context_release": (None, [_vp]),
+    "clc_context_get_info": (_i, [_vp, C.POINTER(DeviceInfo)]),
+    "clc_finish": (_i, [_vp]),
+    "clc_buffer_alloc": (_i, [_vp, _sz, C.POINTER(_vp)]),
+    "clc_buffer_release": (None, [_vp]),
+    "clc_buffer_size": (_sz, [_vp]),
+    "clc_buffer_write": (_i, [_vp, _vp, _sz, _sz, _vp]),
+    "clc_buffer_read": (_i, [_vp, _vp, _sz, _sz, _vp]),
+    "clc_buffer_copy": (_i, [_vp, _vp, _sz, _vp, _sz, _sz]),
+    "clc_file_size": (_i, [_cp, C.POINTER(_sz)]),
+    "clc_file_read": (_i, [_vp, _cp, _sz, _vp, _sz, _sz, C.POINTER(_sz)]),
+    "clc_file_write": (_i, [_vp, _cp, _i, _sz, _vp, _sz, _sz, C.POINTER(_sz)]),
+    "clc_fill": (_i, [_vp, _vp, _sz, _i, _vp]),
+    "clc_sequence": (_i, [_vp, _vp, _sz, _i, _vp, _vp]),
+    "clc_transform": (_i, [_vp, _vp, _i, _vp, _i, _sz, _cp]),
+    "clc_transform2": (_i, [_vp, _vp, _i, _vp, _i, _vp, _i, _sz, _cp]),
+    "clc_reduce": (_i, [_vp, _vp, _sz, _i, _cp, _cp, _vp, _vp]),
+    "clc_scan": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i]),
+    "clc_sort": (_i, [_vp, _vp, _i, _vp, _sz, _i]),
+    "clc_copy_if": (_i, [_vp, _vp, _vp, _sz, _i, _cp, C.POINTER(_sz)]),
+    "clc_add_header": (_i, [_vp, _cp, _cp]),
+    "clc_kernel_create": (_i, [_vp, _cp, _cp, _cp, _vp, _vp, _sz, C.POINTER(_vp)]),
+    "clc_kernel_release": (None, [_vp]),
+    "clc_kernel_set_buffer": (_i, [_vp, C.c_uint, _vp]),
+    "clc_kernel_set_value": (_i, [_vp, C.c_uint, _sz, _vp]),
+    "clc_kernel_set_local": (_i, [_vp, C.c_uint, _sz]),
+    "clc_kernel_work_group_size": (_i, [_vp, _vp, _sz, C.POINTER(_sz)]),
+    "clc_kernel_launch": (_i, [_vp, _vp, _sz, _sz]),
+    "clc_histogram_even": (_i, [_vp, _vp, _sz, _i, _vp, _sz, C.c_double, C.c_double]),
+    "clc_scan_ex": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp]),
+    "clc_sort_ex": (_i, [_vp, _vp, _i, _vp, _sz, _i]),
+    "clc_buffer_device_pointer": (_vp, [_vp]),
+    "clc_buffer_wrap": (_i, [_vp, _vp, _sz, C.POINTER(_vp)]),
+    "clc_context_stream": (_vp, [_vp]),
+    "clc_context_memory_stats": (_i, [_vp, C.POINTER(MemoryStats)]),
+    "clc_context_release_cache": (_i, [_vp]),
+    "clc_sort_keys_raw": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _i]),
+    "clc_scan_raw": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp]),
+    "clc_histogram_even_raw": (_i, [_vp, _vp, _sz, _i, _vp, _sz, C.c_double, C.c_double]),
+    "clc_reduce_raw": (_i, [_vp, _vp, _sz, _i, _cp, _cp, _vp, _vp]),
+    "clc_selftest_lookback_timeout": (_i, [_vp]),
+    "clc_profile_enable": (_i, [_vp, _i]),
+    "clc_profile_reset": (_i, [_vp]),
+    "clc_profile_count": (_i, [_vp, C.POINTER(_sz)]),
+    "clc_profile_entry": (_i, [_vp, _sz, _cp, _sz, C.POINTER(C.c_ulonglong), C.POINTER(C.c_double)]),
+    "clc_tuning_sort_variants": (_i, [_i, _i]),
+    "clc_tuning_sort_key": (_i, [_i, _i, _sz, _cp, _sz]),
+    "clc_tuning_set": (_i, [_vp, _cp, _i]),
+    "clc_tuning_get": (_i, [_vp, _cp, C.POINTER(_i)]),
+    "clc_tuning_save": (_i, [_vp, _cp]),
+}
+for _name, (_res, _args) in _PROTOS.items():
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+EXPORTED_SYMBOLS = tuple(_PROTOS)
+
+
+# ---- devices and contexts ---------------------------------------------------
+
+def device_count() -> int:
+    n = C.c_size_t(0)
+    _raise_for(lib.clc_device_count(C.byref(n)))
+    return n.value
+
+
+def device_info(index: int) -> DeviceInfo:
+    info = DeviceInfo()
+    _raise_for(lib.clc_device_get_info(index, C.byref(info)))
+    return info
+
+
+class Context:
+    """One device, one CUDA stream, a pooled stream-ordered memory resource and
+    the tuning table (the reference's compute_context)."""
+
+    def __init__(self, device: int = DEFAULT_DEVICE, cache_dir: str | None = None):
+        h = C.c_void_p()
+        if cache_dir is None:
+            _raise_for(lib.clc_context_create(device, C.byref(h)))
+        else:
+            _raise_for(lib.clc_context_create_with_cache(device, cache_dir.encode(), C.byref(h)))
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            lib.clc_context_release(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> DeviceInfo:
+        info = DeviceInfo()
+        _raise_for(lib.clc_context_get_info(self.handle, C.byref(info)))
+        return info
+
+    def finish(self) -> None:
+        _raise_for(lib.clc_finish(self.handle))
+
+    @property
+    def stream(self) -> int:
+        return lib.clc_context_stream(self.handle) or 0
+
+    def memory_stats(self) -> MemoryStats:
+        s = MemoryStats()
+        _raise_for(lib.clc_context_memory_stats(self.handle, C.byref(s)))
+        return s
+
+    def release_cache(self) -> None:
+        _raise_for(lib.clc_context_release_cache(self.handle))
+
+    # profiler
+    def profile_enable(self, on: bool = True) -> None:
+        _raise_for(lib.clc_profile_enable(self.handle, int(on)))
+
+    def profile_reset(self) -> None:
+        _raise_for(lib.clc_profile_reset(self.handle))
+
+    def profile(self) -> dict:
+        """{kernel family: (launches, total milliseconds)}; synchronises."""
+        n = C.c_size_t(0)
+        _raise_for(lib.clc_profile_count(self.handle, C.byref(n)))
+        out = {}
+        name = C.create_string_buffer(128)
+        launches, ms = C.c_ulonglong(0), C.c_double(0)
+        for i in range(n.value):
+            _raise_for(lib.clc_profile_entry(self.handle, i, name, 128, C.byref(launches), C.byref(ms)))
+            out[name.value.decode()] = (launches.value, ms.value)
+        return out
+
+    # tuning table
+    def tuning_set(self, key: str, variant: int) -> None:
+        _raise_for(lib.clc_tuning_set(self.handle, key.encode(), variant))
+
+    def tuning_get(self, key: str) -> int:
+        v = C.c_int(-1)
+        _raise_for(lib.clc_tuning_get(self.handle, key.encode(), C.byref(v)))
+        return v.value
+
+    def tuning_save(self, path: str | None = None) -> None:
+        _raise_for(lib.clc_tuning_save(self.handle, path.encode() if path else None))
+
+
+class DeviceBuffer:
+    """Typed device allocation (device_buffer<T>): ``size`` elements of ``dtype``."""
+
+    def __init__(self, ctx: Context, size: int, dtype, _handle=None):
+        self.ctx = ctx
+        self.dtype = np.dtype(dtype)
+        self.size = int(size)
+        if _handle is None:
+            h = C.c_void_p()
+            _raise_for(lib.clc_buffer_alloc(ctx.handle, self.size * self.dtype.itemsize, C.byref(h)))
+            self.handle = h
+        else:
+            self.handle = _handle
+
+    @classmethod
+    def from_host(cls, ctx: Context, host) -> "DeviceBuffer":
+        host = np.ascontiguousarray(host)
+        b = cls(ctx, host.size, host.dtype)
+        b.write(host)
+        return b
+
+    @classmethod
+    def wrap(cls, ctx: Context, device_pointer: int, size: int, dtype) -> "DeviceBuffer":
+        """A non-owning view of existing device memory (e.g. a torch tensor)."""
+        dtype = np.dtype(dtype)
+        h = C.c_void_p()
+        _raise_for(lib.clc_buffer_wrap(ctx.handle, C.c_void_p(device_pointer), size * dtype.itemsize, C.byref(h)))
+        return cls(ctx, size, dtype, _handle=h)
+
+    @property
+    def nbytes(self) -> int:
+        return self.size * self.dtype.itemsize
+
+    @property
+    def device_pointer(self) -> int:
+        return lib.clc_buffer_device_pointer(self.handle) or 0
+
+    def write(self, host, offset: int = 0) -> None:
+        host = np.ascontiguousarray(host, dtype=self.dtype)
+        _raise_for(lib.clc_buffer_write(self.ctx.handle, self.handle, offset * self.dtype.itemsize,
+                                        host.nbytes, host.ctypes.data_as(C.c_void_p)))
+
+    def to_host(self, count: int | None = None) -> np.ndarray:
+        count = self.size if count is None else count
+        out = np.empty(count, dtype=self.dtype)
+        _raise_for(lib.clc_buffer_read(self.ctx.handle, self.handle, 0, out.nbytes,
+                                       out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def release(self) -> None:
+        if self.handle:
+            lib.clc_buffer_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+# ---- operators (Algorithm.hpp:25-66) ------------------------------------------
+
+binary_op = namedtuple("binary_op", ["expression", "identity"])
+
+_LIMITS = {
+    np.dtype(np.int8): ("CHAR_MIN", "CHAR_MAX"),
+    np.dtype(np.uint8): ("0", "UCHAR_MAX"),
+    np.dtype(np.int16): ("SHRT_MIN", "SHRT_MAX"),
+    np.dtype(np.uint16): ("0", "USHRT_MAX"),
+    np.dtype(np.int32): ("INT_MIN", "INT_MAX"),
+    np.dtype(np.uint32): ("0", "UINT_MAX"),
+    np.dtype(np.int64): ("LONG_MIN", "LONG_MAX"),
+    np.dtype(np.uint64): ("0", "ULONG_MAX"),
+    np.dtype(np.float32): ("(-INFINITY)", "INFINITY"),
+    np.dtype(np.float64): ("(-INFINITY)", "INFINITY"),
+}
+
+
+class ops:
+    @staticmethod
+    def plus():
+        return binary_op("(a + b)", "0")
+
+    @staticmethod
+    def multiplies():
+        return binary_op("(a * b)", "1")
+
+    @staticmethod
+    def bit_and():
+        return binary_op("(a & b)", "(~0)")
+
+    @staticmethod
+    def bit_or():
+        return binary_op("(a | b)", "0")
+
+    @staticmethod
+    def bit_xor():
+        return binary_op("(a ^ b)", "0")
+
+    @staticmethod
+    def minimum(dtype):
+        return binary_op("((b < a) ? b : a)", _LIMITS[np.dtype(dtype)][1])
+
+    @staticmethod
+    def maximum(dtype):
+        return binary_op("((a < b) ? b : a)", _LIMITS[np.dtype(dtype)][0])
+
+
+# ---- algorithms ----------------------------------------------------------------
+
+def _scalar(dtype, value):
+    return np.array([value], dtype=dtype)
+
+
+def fill(ctx: Context, out: DeviceBuffer, value) -> None:
+    v = _scalar(out.dtype, value)
+    _raise_for(lib.clc_fill(ctx.handle, out.handle, out.size, clc_type(out.dtype), v.ctypes.data_as(C.c_void_p)))
+
+
+def sequence(ctx: Context, out: DeviceBuffer, start=0, step=1) -> None:
+    s, d = _scalar(out.dtype, start), _scalar(out.dtype, step)
+    _raise_for(lib.clc_sequence(ctx.handle, out.handle, out.size, clc_type(out.dtype),
+                                s.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p)))
+
+
+def reduce(ctx: Context, inp: DeviceBuffer, op: binary_op | None = None, init=0):
+    op = op or ops.plus()
+    i = _scalar(inp.dtype, init)
+    r = np.zeros(1, dtype=inp.dtype)
+    _raise_for(lib.clc_reduce(ctx.handle, inp.handle, inp.size, clc_type(inp.dtype), op.expression.encode(),
+                              op.identity.encode(), i.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p)))
+    return r[0]
+
+
+def _scan(ctx, inp, out, op, exclusive, want_total):
+    if out.size < inp.size:
+        raise ValueError(("exclusive" if exclusive else "inclusive") + "_scan: output too small")
+    op = op or ops.plus()
+    if not want_total:
+        _raise_for(lib.clc_scan(ctx.handle, inp.handle, out.handle, inp.size, clc_type(inp.dtype),
+                                op.expression.encode(), op.identity.encode(), int(exclusive)))
+        return None
+    total = np.zeros(1, dtype=np.float64 if inp.dtype.kind == "f" else
+                     (np.int64 if inp.dtype.kind == "i" else np.uint64))
+    _raise_for(lib.clc_scan_ex(ctx.handle, inp.handle, out.handle, inp.size, clc_type(inp.dtype),
+                               op.expression.encode(), op.identity.encode(), int(exclusive),
+                               total.ctypes.data_as(C.c_void_p)))
+    return total[0]
+
+
+def inclusive_scan(ctx, inp, out, op=None, total=False):
+    return _scan(ctx, inp, out, op, False, total)
+
+
+def exclusive_scan(ctx, inp, out, op=None, total=False):
+    return _scan(ctx, inp, out, op, True, total)
+
+
+def sort(ctx: Context, keys: DeviceBuffer, descending: bool = False) -> None:
+    """Stable radix sort of 32-bit keys in place (cl::compute::sort)."""
+    if keys.dtype.itemsize != 4:
+        raise TypeError("sort: keys must be 32-bit")
+    _raise_for(lib.clc_sort(ctx.handle, keys.handle, clc_type(keys.dtype), None, keys.size, int(descending)))
+
+
+def sort_by_key(ctx: Context, keys: DeviceBuffer, values: DeviceBuffer, descending: bool = False) -> None:
+    """Sorts keys and permutes 32-bit values alongside (cl::compute::sort_by_key)."""
+    if keys.dtype.itemsize != 4 or values.dtype.itemsize != 4:
+        raise TypeError("sort_by_key: keys and values must be 32-bit")
+    if values.size < keys.size:
+        raise ValueError("sort_by_key: too few values")
+    _raise_for(lib.clc_sort(ctx.handle, keys.handle, clc_type(keys.dtype), values.handle, keys.size,
+                            int(descending)))
+
+
+def sort_ex(ctx: Context, keys: DeviceBuffer, values: DeviceBuffer | None = None, descending: bool = False) -> None:
+    """Extension: 32- or 64-bit keys with optional 32-bit values."""
+    if values is not None and values.size < keys.size:
+        raise ValueError("sort_ex: too few values")
+    _raise_for(lib.clc_sort_ex(ctx.handle, keys.handle, clc_type(keys.dtype),
+                               values.handle if values is not None else None, keys.size, int(descending)))
+
+
+def sort_raw(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int, vals_in: int = 0, vals_out: int = 0,
+             descending: bool = False) -> None:
+    """Extension: sort on raw device pointers (asynchronous)."""
+    _raise_for(lib.clc_sort_keys_raw(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype),
+                                     C.c_void_p(vals_in or None), C.c_void_p(vals_out or None), n, int(descending)))
+
+
+def scan_raw(ctx: Context, inp: int, out: int, n: int, dtype, op: binary_op | None = None, exclusive: bool = False,
+             total_device: int = 0) -> None:
+    op = op or ops.plus()
+    _raise_for(lib.clc_scan_raw(ctx.handle, C.c_void_p(inp), C.c_void_p(out), n, clc_type(dtype),
+                                op.expression.encode(), op.identity.encode(), int(exclusive),
+                                C.c_void_p(total_device or None)))
+
+
+def histogram_even(ctx: Context, inp: DeviceBuffer, hist: DeviceBuffer, lower: float, upper: float) -> None:
+    """Counts into hist.size equal-width bins over [lower, upper) (cl::compute::histogram_even)."""
+    if hist.dtype != np.dtype(np.uint32):
+        raise TypeError("histogram_even: histogram must be uint32")
+    _raise_for(lib.clc_histogram_even(ctx.handle, inp.handle, inp.size, clc_type(inp.dtype), hist.handle,
+                                      hist.size, float(lower), float(upper)))
+
+
+def histogram_even_raw(ctx: Context, inp: int, n: int, dtype, hist: int, bins: int, lower: float,
+                       upper: float) -> None:
+    _raise_for(lib.clc_histogram_even_raw(ctx.handle, C.c_void_p(inp), n, clc_type(dtype), C.c_void_p(hist), bins,
+                                          float(lower), float(upper)))
+
+
+def tuning_sort_variants(key_bytes: int, has_values: bool) -> int:
+    return lib.clc_tuning_sort_variants(key_bytes, int(has_values))
+
+
+def tuning_sort_key(key_bytes: int, has_values: bool, n: int) -> str:
+    buf = C.create_string_buffer(128)
+    _raise_for(lib.clc_tuning_sort_key(key_bytes, int(has_values), n, buf, 128))
+    return buf.value.decode()

@@ -1,0 +1,158 @@
+"""CPU ORACLE loader — test infrastructure only.
+
+ctypes access to oracle/_build/liboracle.so (built from oracle.cpp by
+oracle/Makefile). Used by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg as the checker; never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+T_I8, T_U8, T_I16, T_U16, T_I32, T_U32, T_I64, T_U64, T_F32, T_F64 = range(10)
+OP_PLUS, OP_MUL, OP_AND, OP_OR, OP_XOR, OP_MIN, OP_MAX, OP_RIGHT = range(8)
+
+_TYPES = {
+    np.dtype(np.int8): T_I8, np.dtype(np.uint8): T_U8, np.dtype(np.int16): T_I16,
+    np.dtype(np.uint16): T_U16, np.dtype(np.int32): T_I32, np.dtype(np.uint32): T_U32,
+    np.dtype(np.int64): T_I64, np.dtype(np.uint64): T_U64, np.dtype(np.float32): T_F32,
+    np.dtype(np.float64): T_F64,
+}
+
+# Operator expressions (as the C ABI spells them) -> oracle op codes.
+OPS = {
+    "(a + b)": OP_PLUS, "(a * b)": OP_MUL, "(a & b)": OP_AND, "(a | b)": OP_OR,
+    "(a ^ b)": OP_XOR, "((b < a) ? b : a)": OP_MIN, "((a < b) ? b : a)": OP_MAX, "b": OP_RIGHT,
+}
+
+
+def build() -> str:
+    src = os.path.join(HERE, "oracle.cpp")
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, sz, i = C.c_void_p, C.c_size_t, C.c_int
+        L.orc_random_uints.argtypes = [vp, sz, C.c_uint32, C.c_uint]
+        L.orc_random_floats.argtypes = [vp, sz, C.c_float, C.c_float, C.c_uint]
+        L.orc_std_sort.argtypes = [vp, vp, sz, i, i, i]
+        L.orc_std_scan.argtypes = [vp, vp, sz, i, i, vp, i]
+        L.orc_std_reduce.argtypes = [vp, sz, i, i, vp, vp, vp]
+        L.orc_sum_i32.argtypes = [vp, sz]
+        L.orc_sum_i32.restype = C.c_longlong
+        L.orc_histogram_even.argtypes = [vp, sz, i, vp, sz, C.c_double, C.c_double, i]
+        L.orc_ref_radix_sort.argtypes = [vp, vp, sz, i, i, i, i]
+        L.orc_ref_scan.argtypes = [vp, vp, sz, i, i, vp, i, i]
+        L.orc_ref_reduce.argtypes = [vp, sz, i, i, vp, vp, vp, i]
+        L.orc_hardware_threads.restype = i
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def key_kind(dtype) -> int:
+    k = np.dtype(dtype).kind
+    return {"u": 0, "i": 1, "f": 2}[k]
+
+
+# ---- generators ---------------------------------------------------------------
+
+def random_uints(n: int, maximum: int, seed: int) -> np.ndarray:
+    """std::mt19937(seed) + uniform_int_distribution<uint32>(0, maximum)."""
+    out = np.empty(n, dtype=np.uint32)
+    lib().orc_random_uints(_p(out), n, maximum, seed)
+    return out
+
+
+def random_floats(n: int, lo: float, hi: float, seed: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float32)
+    lib().orc_random_floats(_p(out), n, lo, hi, seed)
+    return out
+
+
+# ---- ground truth ---------------------------------------------------------------
+
+def std_sort(keys: np.ndarray, values: np.ndarray | None = None, descending: bool = False):
+    k = np.ascontiguousarray(keys).copy()
+    v = None if values is None else np.ascontiguousarray(values, dtype=np.uint32).copy()
+    lib().orc_std_sort(_p(k), None if v is None else _p(v), k.size, k.dtype.itemsize, key_kind(k.dtype),
+                       int(descending))
+    return k, v
+
+
+def ref_radix_sort(keys: np.ndarray, values: np.ndarray | None = None, descending: bool = False,
+                   threads: int = 0):
+    k = np.ascontiguousarray(keys).copy()
+    v = None if values is None else np.ascontiguousarray(values, dtype=np.uint32).copy()
+    lib().orc_ref_radix_sort(_p(k), None if v is None else _p(v), k.size, k.dtype.itemsize, key_kind(k.dtype),
+                             int(descending), threads)
+    return k, v
+
+
+def _ident(dtype, identity) -> np.ndarray:
+    return np.array([identity], dtype=dtype)
+
+
+def std_scan(x: np.ndarray, op: int = OP_PLUS, identity=0, exclusive: bool = False) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    out = np.empty_like(x)
+    lib().orc_std_scan(_p(x), _p(out), x.size, _TYPES[x.dtype], op, _p(_ident(x.dtype, identity)), int(exclusive))
+    return out
+
+
+def ref_scan(x: np.ndarray, op: int = OP_PLUS, identity=0, exclusive: bool = False, threads: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    out = np.empty_like(x)
+    lib().orc_ref_scan(_p(x), _p(out), x.size, _TYPES[x.dtype], op, _p(_ident(x.dtype, identity)), int(exclusive),
+                       threads)
+    return out
+
+
+def std_reduce(x: np.ndarray, op: int = OP_PLUS, identity=0, init=0):
+    x = np.ascontiguousarray(x)
+    r = np.zeros(1, dtype=x.dtype)
+    lib().orc_std_reduce(_p(x), x.size, _TYPES[x.dtype], op, _p(_ident(x.dtype, identity)),
+                         _p(_ident(x.dtype, init)), _p(r))
+    return r[0]
+
+
+def ref_reduce(x: np.ndarray, op: int = OP_PLUS, identity=0, init=0, threads: int = 0):
+    x = np.ascontiguousarray(x)
+    r = np.zeros(1, dtype=x.dtype)
+    lib().orc_ref_reduce(_p(x), x.size, _TYPES[x.dtype], op, _p(_ident(x.dtype, identity)),
+                         _p(_ident(x.dtype, init)), _p(r), threads)
+    return r[0]
+
+
+def sum_i32(x: np.ndarray) -> int:
+    x = np.ascontiguousarray(x, dtype=np.int32)
+    return int(lib().orc_sum_i32(_p(x), x.size))
+
+
+def histogram_even(x: np.ndarray, bins: int, lower: float, upper: float, threads: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    h = np.zeros(bins, dtype=np.uint32)
+    lib().orc_histogram_even(_p(x), x.size, _TYPES[x.dtype], _p(h), bins, lower, upper, threads)
+    return h
+
+
+def hardware_threads() -> int:
+    return lib().orc_hardware_threads()

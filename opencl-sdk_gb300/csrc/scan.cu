@@ -259,7 +259,10 @@ __global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
             const T wexc = __shfl_up_sync(FULL_MASK, winc[r], 1);
-            T run = op(prefix, s_rw[r * (THREADS / 32) + warp]);
+            // The first row-warp's exclusive value is the identity; combining
+            // it on the right would break operators whose identity only works
+            // from the left (the right projection), so it is skipped.
+            T run = (r == 0 && warp == 0) ? prefix : op(prefix, s_rw[r * (THREADS / 32) + warp]);
             if (lane > 0) run = op(run, wexc);
             T o[VEC];
 #pragma unroll

@@ -1,0 +1,87 @@
+"""Profiling harness: runs one named workload a fixed number of times so that
+an ncu capture has a short, deterministic launch sequence.
+
+  python opencl-sdk_gb300/profile_cases.py CASE [--n N] [--iters K]
+
+Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
+(u64 keys + u32 values), scan-i32 (exclusive, int64 total), reduce-i32,
+hist-u8 (256 bins). Inputs are seeded uniform data generated on the device;
+every call goes through the C ABI on the library's stream.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case")
+    ap.add_argument("--n", type=int, default=1 << 25)
+    ap.add_argument("--iters", type=int, default=3)
+    args = ap.parse_args()
+
+    import numpy as np
+    import torch
+
+    import gbcompute as gbc
+
+    ctx = gbc.Context(0)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    n = args.n
+
+    def u32(count):
+        return torch.randint(0, 2**32, (count,), dtype=torch.int64, device="cuda", generator=g).to(torch.int32)
+
+    if args.case in ("sort-kv", "sort-keys"):
+        k, ko = u32(n), torch.empty(n, dtype=torch.int32, device="cuda")
+        v, vo = torch.arange(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")
+        kv = args.case == "sort-kv"
+
+        def step():
+            gbc.sort_raw(ctx, k.data_ptr(), ko.data_ptr(), np.uint32, n, v.data_ptr() if kv else 0,
+                         vo.data_ptr() if kv else 0)
+    elif args.case == "sort-kv64":
+        k = torch.randint(-2**63, 2**63 - 1, (n,), dtype=torch.int64, device="cuda", generator=g)
+        ko = torch.empty_like(k)
+        v, vo = torch.arange(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")
+
+        def step():
+            gbc.sort_raw(ctx, k.data_ptr(), ko.data_ptr(), np.uint64, n, v.data_ptr(), vo.data_ptr())
+    elif args.case == "scan-i32":
+        x = torch.randint(-1000, 1001, (n,), dtype=torch.int32, device="cuda", generator=g)
+        y = torch.empty_like(x)
+        t = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+        def step():
+            gbc.scan_raw(ctx, x.data_ptr(), y.data_ptr(), n, np.int32, exclusive=True, total_device=t.data_ptr())
+    elif args.case == "reduce-i32":
+        x = torch.randint(-1000, 1001, (n,), dtype=torch.int32, device="cuda", generator=g)
+        xb = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), n, np.int32)
+
+        def step():
+            gbc.reduce(ctx, xb)
+    elif args.case == "hist-u8":
+        x = torch.randint(0, 256, (n,), dtype=torch.uint8, device="cuda", generator=g)
+        h = torch.empty(256, dtype=torch.int32, device="cuda")
+
+        def step():
+            gbc.histogram_even_raw(ctx, x.data_ptr(), n, np.uint8, h.data_ptr(), 256, 0.0, 256.0)
+    else:
+        raise SystemExit(f"unknown case {args.case}")
+
+    torch.cuda.synchronize()
+    for _ in range(args.iters):
+        step()
+    ctx.finish()
+    print(f"{args.case}: {args.iters} iterations of n={n} done")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

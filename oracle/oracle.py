@@ -33,8 +33,8 @@ OPS = {
 
 
 def build() -> str:
-    src = os.path.join(HERE, "oracle.cpp")
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    newest = max(os.path.getmtime(os.path.join(HERE, f)) for f in ("oracle.cpp", "Makefile"))
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
 

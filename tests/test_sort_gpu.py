@@ -48,6 +48,7 @@ def test_signed_keys(ctx, gbc):
 def test_float_keys_descending_bit_exact(ctx, gbc, orc):
     f = orc.random_floats(3000, -1e6, 1e6, 5)
     f[0], f[1], f[2] = np.float32(-0.0), np.float32(np.inf), np.float32(-np.inf)
+    assert digest(f) == GOLDEN["floats_desc"]["keys_in"]  # same generator output on every host
     fb = gbc.DeviceBuffer.from_host(ctx, f)
     gbc.sort(ctx, fb, True)
     got = fb.to_host()

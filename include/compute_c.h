@@ -243,6 +243,31 @@ GBC_EXPORT clc_status clc_reduce_raw(clc_context ctx, const void* in, size_t n, 
                                      const char* op, const char* identity, const void* init,
                                      void* result);
 
+/* Allocation-free int32 plus-scan. No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory when they need a scan: code
+ * whose device memory belongs to another allocator (a framework's caching
+ * allocator, a fixed arena on a shared GPU) and code that cannot afford the
+ * device-wide synchronisation of cudaFree. The call allocates nothing and
+ * needs no clc_context: its scratch (one look-back status word per tile of
+ * 4,096 elements, and a tile counter) is a fixed 512 KiB array inside the
+ * library, so n is limited to 2^28 elements; larger n returns
+ * CLC_ERROR_INVALID_ARGUMENT without launching anything.
+ *
+ * in and out are device pointers of the current device (out may equal in);
+ * exclusive != 0 gives an exclusive scan (out[0] = 0). The scan is enqueued on
+ * `stream` (a cudaStream_t; NULL is the legacy default stream) and the call
+ * returns without waiting. Sums wrap modulo 2^32, as clc_scan's do.
+ *
+ * The first call on a device looks up the device address of the scratch
+ * array (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. Every call shares the one array and clears the
+ * part it uses before its kernel runs, so calls whose work may overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller. */
+GBC_EXPORT clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size_t n, int exclusive,
+                                           void* stream);
+
 /* Failure-path self-test: runs one scan tile whose predecessor never
  * publishes its status, so the tile's bounded look-back wait gives up after
  * about one second instead of hanging. Returns what the next synchronising

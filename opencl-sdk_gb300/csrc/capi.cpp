@@ -59,6 +59,23 @@ clc_status fail(clc_status s, const std::string& msg, int native = 0)
     return s;
 }
 
+}  // namespace
+
+namespace gbc {
+// Sets the thread's last error for entry points defined outside this file.
+int set_last_error(int status, const char* msg, int native)
+{
+    if (status == CLC_SUCCESS) {
+        last_error.clear();
+        last_native_error = 0;
+        return status;
+    }
+    return fail(static_cast<clc_status>(status), msg, native);
+}
+}  // namespace gbc
+
+namespace {
+
 template <typename F> clc_status guarded(F&& body)
 {
     try {

@@ -229,4 +229,8 @@ void histogram_even(device_context& ctx, const void* in, std::size_t n, elem t,
 //! path of the bounded look-back wait); the next finish() reports it.
 void selftest_lookback_timeout(device_context& ctx);
 
+//! Records a clc_status and message as the calling thread's last error (for
+//! C entry points defined outside capi.cpp); returns the status.
+int set_last_error(int status, const char* msg, int native);
+
 }  // namespace gbc

@@ -19,7 +19,10 @@
 // order is row, then thread, then element, so each row is a warp scan and the
 // ROWS x 8 row-warp totals are scanned by one warp.
 #include <cstring>
+#include <map>
+#include <mutex>
 
+#include "../../include/compute_c.h"
 #include "device_common.cuh"
 #include "ops.cuh"
 #include "runtime.hpp"
@@ -400,4 +403,111 @@ void scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t,
     ops::dispatch(t, op, l);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free int32 scan (clc_scan_i32_noalloc).
+//
+// Some callers cannot allocate device memory when they need a scan: an
+// embedder whose device memory belongs to another allocator (a framework's
+// caching allocator, or a fixed arena on a GPU shared with other jobs) must
+// not call cudaMalloc behind that allocator's back, and cudaFree synchronises
+// the whole device, which a latency-bound caller cannot afford. This entry
+// point therefore keeps its scratch -- the look-back status word of every
+// tile and the tile counter -- in a fixed array compiled into the library, and
+// it needs no clc_context (creating one allocates). The caller passes the
+// input, the output and the stream.
+//
+// The array holds 65,536 tiles of 4,096 elements: at most 2^28 elements per
+// call (512 KiB of status words, held by every GPU that loads the library
+// until the process exits). Every call shares it and it keeps the last call's
+// contents, so each call first clears the words it will read; calls whose
+// work overlaps on the GPU (different streams, or different host threads)
+// race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace noalloc {
+
+constexpr uint32_t TILE = THREADS * 16;  // the int32 tile of k_scan
+constexpr uint32_t MAX_TILES = 1u << 16;
+constexpr std::size_t MAX_ELEMENTS = (std::size_t)TILE * MAX_TILES;  // 2^28
+
+// [0, MAX_TILES): status word of each tile; [MAX_TILES]: the tile counter.
+static __device__ __align__(256) uint64_t scan_scratch[MAX_TILES + 32];
+
+struct device_setup {
+    uint64_t* scratch = nullptr;  // device address of scan_scratch on this device
+    int grid_cap = 0;             // SMs x resident CTAs of the scan kernel
+};
+std::mutex g_mutex;
+std::map<int, device_setup> g_setup;
+
+// Once per device, with that device current: the host-side name of
+// scan_scratch is only a stand-in, so its device address is looked up here
+// and handed to the kernel.
+device_setup setup_current_device(int dev)
+{
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = g_setup.find(dev);
+    if (it != g_setup.end()) return it->second;
+    device_setup s;
+    void* p = nullptr;
+    check_cuda(cudaGetSymbolAddress(&p, scan_scratch), "cudaGetSymbolAddress");
+    s.scratch = static_cast<uint64_t*>(p);
+    int sms = 0, blocks = 0;
+    check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, &k_scan<int32_t, ops::Plus, false>, THREADS, 0),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    s.grid_cap = sms * std::max(blocks, 1);
+    g_setup[dev] = s;
+    return s;
+}
+
+}  // namespace noalloc
+
 }  // namespace gbc
+
+extern "C" clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size_t n, int exclusive, void* stream)
+{
+    using namespace gbc;
+    try {
+        if (n == 0) return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
+        if (n > noalloc::MAX_ELEMENTS)
+            return (clc_status)set_last_error(
+                CLC_ERROR_INVALID_ARGUMENT,
+                ("clc_scan_i32_noalloc: n = " + std::to_string(n) +
+                 " exceeds the 268435456 (2^28) elements its built-in scratch covers")
+                    .c_str(),
+                0);
+        if (in == nullptr || out == nullptr)
+            return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT, "clc_scan_i32_noalloc: null pointer", 0);
+        int dev = 0;
+        check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+        const noalloc::device_setup s = noalloc::setup_current_device(dev);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const uint32_t num_tiles = (uint32_t)((n + noalloc::TILE - 1) / noalloc::TILE);
+        // Clear what this call reads before it is written: the tile counter
+        // and the status words of its tiles (an earlier call left its own).
+        check_cuda(cudaMemsetAsync(s.scratch, 0, (std::size_t)num_tiles * sizeof(uint64_t), st), "cudaMemsetAsync");
+        check_cuda(cudaMemsetAsync(s.scratch + noalloc::MAX_TILES, 0, sizeof(uint64_t), st), "cudaMemsetAsync");
+        ScanArgs<int32_t> a;
+        a.in = in;
+        a.out = out;
+        a.n = (uint32_t)n;
+        a.identity = 0;
+        a.exclusive = exclusive ? 1 : 0;
+        a.aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+        a.num_tiles = num_tiles;
+        a.ring = s.scratch;  // tile t uses word t (sequence numbers start at 0)
+        a.seq0 = 0;
+        a.tile_ctr = reinterpret_cast<uint32_t*>(s.scratch + noalloc::MAX_TILES);
+        a.wide_sum = nullptr;
+        a.total = nullptr;
+        a.err = nullptr;  // a wait that runs out ends the kernel; there is no context to report to
+        const int grid = (int)std::min<uint32_t>(num_tiles, (uint32_t)s.grid_cap);
+        k_scan<int32_t, ops::Plus, false><<<grid, THREADS, 0, st>>>(a);
+        check_cuda(cudaGetLastError(), "clc_scan_i32_noalloc launch");
+        return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
+    } catch (const device_error& e) {
+        return (clc_status)set_last_error(CLC_ERROR_OPENCL, e.what(), e.code);
+    } catch (const std::exception& e) {
+        return (clc_status)set_last_error(CLC_ERROR_INTERNAL, e.what(), 0);
+    }
+}

@@ -87,7 +87,7 @@ void launch(device_context& ctx, const void* in, uint32_t n, uint32_t* hist, uin
     else m = 2, smem = 0;
     void (*kernel)(const T*, uint32_t, uint32_t*, uint32_t, ACC, ACC) =
         m == 0 ? &k_histogram<T, ACC, 0> : m == 1 ? &k_histogram<T, ACC, 1> : &k_histogram<T, ACC, 2>;
-    if (smem > 48 * 1024)
+    if (smem > 0)  // static shared memory adds to this against the 48 KiB default
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                    "cudaFuncSetAttribute");
     int per_sm = 0;

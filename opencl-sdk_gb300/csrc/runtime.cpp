@@ -60,10 +60,24 @@ stream_holder::~stream_holder()
     }
 }
 
+bool cuda_async_resource::capturing() const
+{
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s_->stream, &st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
 void* cuda_async_resource::do_allocate(std::size_t bytes)
 {
     void* p = nullptr;
     cudaSetDevice(s_->device);
+    if (capturing())
+        throw unsupported_error(
+            "gbcompute: a temporary is not in the pool while the stream is being captured; run the same "
+            "call once before capturing it");
     check_cuda(cudaMallocAsync(&p, std::max<std::size_t>(bytes, 1), s_->stream), "cudaMallocAsync");
     return p;
 }
@@ -71,7 +85,24 @@ void* cuda_async_resource::do_allocate(std::size_t bytes)
 void cuda_async_resource::do_deallocate(void* p, std::size_t) noexcept
 {
     cudaSetDevice(s_->device);
+    if (capturing()) {
+        std::lock_guard<std::mutex> lock(m_);
+        try {
+            deferred_.push_back(p);
+            return;
+        } catch (...) {
+            // no host memory for the list: fall through
+        }
+    }
     cudaFreeAsync(p, s_->stream);
+}
+
+void cuda_async_resource::flush_deferred()
+{
+    std::lock_guard<std::mutex> lock(m_);
+    cudaSetDevice(s_->device);
+    for (void* p : deferred_) cudaFreeAsync(p, s_->stream);
+    deferred_.clear();
 }
 
 pool_resource::options default_pool_options(std::size_t global_memory)
@@ -109,7 +140,7 @@ device_context::device_context(int dev, cudaStream_t external_stream,
         holder->owned = true;
     }
     stream = holder->stream;
-    auto upstream = std::make_shared<cuda_async_resource>(holder);
+    upstream = std::make_shared<cuda_async_resource>(holder);
     pool = std::make_shared<pool_resource>(upstream, opts);
     stats = std::make_shared<statistics_adaptor>(pool);
     resource = stats;
@@ -142,10 +173,27 @@ device_context::device_context(int dev, cudaStream_t external_stream,
     }
 }
 
+cudaStream_t device_context::aux_stream()
+{
+    if (aux == nullptr) {
+        activate();
+        check_cuda(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&join_event, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    return aux;
+}
+
 device_context::~device_context()
 {
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
+    if (aux != nullptr) {
+        cudaStreamSynchronize(aux);
+        cudaStreamDestroy(aux);
+        cudaEventDestroy(fork_event);
+        cudaEventDestroy(join_event);
+    }
     cudaFree(d_error);
     cudaFree(lookback_ring);
     cudaFree(d_small);
@@ -154,10 +202,25 @@ device_context::~device_context()
 
 void device_context::activate() const { check_cuda(cudaSetDevice(device), "cudaSetDevice"); }
 
+bool device_context::capturing() const
+{
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
 uint64_t device_context::reserve_seq(uint64_t count)
 {
     constexpr uint64_t WRAP = uint64_t(1) << 30;
-    if ((ring_seq % WRAP) + count >= WRAP) {
+    if (capturing()) {
+        // A graph replays the sequence numbers it was captured with, so the
+        // words of the previous replay would carry matching tags: a captured
+        // call clears the ring first (one 16 MiB memset node).
+        check_cuda(cudaMemsetAsync(lookback_ring, 0, onesweep::RING_BYTES, stream), "cudaMemsetAsync");
+    } else if ((ring_seq % WRAP) + count >= WRAP) {
         check_cuda(cudaMemsetAsync(lookback_ring, 0, onesweep::RING_BYTES, stream), "cudaMemsetAsync");
         ring_seq = (ring_seq / WRAP + 1) * WRAP;
     }
@@ -209,6 +272,11 @@ cudaEvent_t profiler::get_event()
 int profiler::start(cudaStream_t s, const char* name)
 {
     if (!enabled_) return -1;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
+        (void)cudaGetLastError();
+        return -1;  // events recorded inside a capture cannot be timed
+    }
     std::lock_guard<std::mutex> lock(m_);
     pending p{name, get_event(), get_event()};
     check_cuda(cudaEventRecord(p.a, s), "cudaEventRecord");

@@ -63,13 +63,22 @@ struct stream_holder {
 class cuda_async_resource final : public memory_resource {
 public:
     explicit cuda_async_resource(std::shared_ptr<stream_holder> s) : s_(std::move(s)) {}
+    //! Frees what was handed back while the stream was being captured.
+    void flush_deferred();
 
 protected:
+    // While the stream is being captured into a CUDA graph, an allocation
+    // would become a graph node whose memory the pool must not keep: it is
+    // refused (warm the pool by running the call once first), and frees are
+    // deferred until the capture ends.
     void* do_allocate(std::size_t bytes) override;
     void do_deallocate(void* p, std::size_t bytes) noexcept override;
 
 private:
+    bool capturing() const;
     std::shared_ptr<stream_holder> s_;
+    std::mutex m_;
+    std::vector<void*> deferred_;
 };
 
 // ---- tuning table (replaces the JIT program cache) ------------------------
@@ -169,6 +178,12 @@ struct device_context {
     unsigned char* d_small = nullptr;   // 64 KiB of per-call control blocks
     void* pinned = nullptr;         // 64 KiB of pinned host staging
 
+    // A second stream for independent work inside one call (forked from and
+    // joined back to `stream` with the two events), created on first use.
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork_event = nullptr, join_event = nullptr;
+    cudaStream_t aux_stream();
+
     device_context(int device, cudaStream_t external_stream,
                    const pool_resource::options& opts, const std::string& tuning_dir);
     ~device_context();
@@ -180,6 +195,9 @@ struct device_context {
     //! bits wide: before they would wrap, the ring is cleared (stream-ordered)
     //! so that no stale word can carry a matching tag.
     uint64_t reserve_seq(uint64_t count);
+    //! True while the context's stream is being captured into a CUDA graph.
+    bool capturing() const;
+    std::shared_ptr<cuda_async_resource> upstream;
     //! Synchronises the stream and reports a kernel-recorded error, if any.
     void finish();
     //! Reads and clears the device error word (synchronises the stream).

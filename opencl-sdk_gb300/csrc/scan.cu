@@ -122,172 +122,253 @@ template <typename T> __device__ __forceinline__ void store_wide(void* dst, T v)
     }
 }
 
-template <typename T, typename Op, bool WIDE_SUM>
-__global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
-{
-    constexpr int VEC = 16 / sizeof(T);
-    constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
-    constexpr int TILE = THREADS * VEC * ROWS;
-    constexpr int RW = ROWS * (THREADS / 32);
-    constexpr int PER = RW / 32;
+template <typename T> struct ScanShape {
+    static constexpr int VEC = 16 / sizeof(T);
+    static constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
+    static constexpr int TILE = THREADS * VEC * ROWS;
+    static constexpr int RW = ROWS * (THREADS / 32);
+    static constexpr int PER = RW / 32;
     static_assert(RW % 32 == 0, "row-warp totals fill whole lanes");
+};
 
-    __shared__ T s_rw[RW];
-    __shared__ T s_prefix;
-    __shared__ uint32_t s_tile;
+// One tile after its elements x are in registers: wide sum, warp scans, the
+// row-warp scan and look-back (warp 0), then the outputs. Contains CTA
+// barriers: every thread of the CTA calls it.
+template <typename T, typename Op, bool WIDE_SUM>
+__device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape<T>::ROWS][ScanShape<T>::VEC],
+                                          uint32_t t, uint32_t base, bool full, T* s_rw, T& s_prefix)
+{
+    constexpr int VEC = ScanShape<T>::VEC;
+    constexpr int ROWS = ScanShape<T>::ROWS;
+    constexpr int PER = ScanShape<T>::PER;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const Op op;
     const T identity = a.identity;
 
+    if (WIDE_SUM) {
+        // Exact sum of the valid elements, widened, one atomic per warp.
+        unsigned long long s = 0;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
+                if (idx < a.n) {
+                    if (std::is_signed<T>::value) s += (unsigned long long)(long long)x[r][j];
+                    else s += (unsigned long long)x[r][j];
+                }
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o);
+        if (lane == 0) atomicAdd(a.wide_sum, s);
+    }
+
+    // Per-row warp scans of the thread totals.
+    T winc[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        T acc = x[r][0];
+#pragma unroll
+        for (int j = 1; j < VEC; ++j) acc = op(acc, x[r][j]);
+        winc[r] = dev::warp_inclusive_scan(acc, op);
+        if (lane == 31) s_rw[r * (THREADS / 32) + warp] = winc[r];
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        // Exclusive scan of the row-warp totals, in sequence order.
+        T v[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) v[k] = s_rw[lane * PER + k];
+        T lt = v[0];
+#pragma unroll
+        for (int k = 1; k < PER; ++k) lt = op(lt, v[k]);
+        const T linc = dev::warp_inclusive_scan(lt, op);
+        const T up = __shfl_up_sync(FULL_MASK, linc, 1);
+        T run = lane == 0 ? identity : up;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            s_rw[lane * PER + k] = run;
+            run = op(run, v[k]);
+        }
+        const T agg = __shfl_sync(FULL_MASK, linc, 31);
+        const uint64_t my_seq = a.seq0 + t;
+        if (lane == 0) Status<T>::publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
+
+        // Warp-cooperative look-back: lane l inspects tile w_end-32+l;
+        // the nearest tile holding an inclusive prefix ends the walk.
+        T excl = identity;
+        if (t > 0) {
+            bool have = false;
+            int64_t w_end = t;
+            for (;;) {
+                const int64_t k = w_end - 32 + lane;
+                uint64_t flag = FLAG_PRE;
+                T val = identity;
+                bool gave_up = false;
+                if (k >= 0) {
+                    if (!Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) {
+                        const unsigned long long start = dev::globaltimer();
+                        for (uint32_t spin = 1;; ++spin) {
+                            if (Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) break;
+                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                gave_up = true;
+                                flag = FLAG_PRE;
+                                val = identity;
+                                break;
+                            }
+                            if (spin > 32) __nanosleep(64);
+                        }
+                    }
+                }
+                if (__any_sync(FULL_MASK, gave_up)) {
+                    if (lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                }
+                const uint32_t pre = __ballot_sync(FULL_MASK, flag == FLAG_PRE);
+                const int L = pre ? 31 - __clz(pre) : 0;
+                const T contrib = lane >= L ? val : identity;
+                const T wsum = dev::warp_reduce(contrib, op);
+                excl = have ? op(wsum, excl) : wsum;
+                have = true;
+                if (pre) break;
+                w_end -= 32;
+            }
+            if (lane == 0) Status<T>::publish(a.ring, my_seq, FLAG_PRE, op(excl, agg));
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+
+    const T prefix = s_prefix;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const T wexc = __shfl_up_sync(FULL_MASK, winc[r], 1);
+        // The first row-warp's exclusive value is the identity; combining
+        // it on the right would break operators whose identity only works
+        // from the left (the right projection), so it is skipped.
+        T run = (r == 0 && warp == 0) ? prefix : op(prefix, s_rw[r * (THREADS / 32) + warp]);
+        if (lane > 0) run = op(run, wexc);
+        T o[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const T inc = op(run, x[r][j]);
+            o[j] = a.exclusive ? run : inc;
+            run = inc;
+            if (a.total != nullptr && base + (r * THREADS + tid) * VEC + j == a.n - 1)
+                store_wide<T>(a.total, inc);
+        }
+        if (full && a.aligned) {
+            uint4 w;
+            memcpy(&w, o, 16);
+            *reinterpret_cast<uint4*>(a.out + base + (r * THREADS + tid) * VEC) = w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
+                if (idx < a.n) a.out[idx] = o[j];
+            }
+        }
+    }
+}
+
+template <typename T, typename Op, bool WIDE_SUM>
+__global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
+{
+    using S = ScanShape<T>;
+    __shared__ T s_rw[S::RW];
+    __shared__ T s_prefix;
+    __shared__ uint32_t s_tile;
+    const int tid = threadIdx.x;
     for (;;) {
         if (tid == 0) s_tile = atomicAdd(a.tile_ctr, 1u);
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= a.num_tiles) break;
-        const uint32_t base = t * TILE;
-        const bool full = base + TILE <= a.n;
-
-        T x[ROWS][VEC];
+        const uint32_t base = t * S::TILE;
+        const bool full = base + S::TILE <= a.n;
+        T x[S::ROWS][S::VEC];
         if (full && a.aligned) {
 #pragma unroll
-            for (int r = 0; r < ROWS; ++r) {
-                const uint4 w = dev::ld_stream(reinterpret_cast<const uint4*>(a.in + base + (r * THREADS + tid) * VEC));
+            for (int r = 0; r < S::ROWS; ++r) {
+                const uint4 w = dev::ld_stream(reinterpret_cast<const uint4*>(a.in + base + (r * THREADS + tid) * S::VEC));
                 memcpy(x[r], &w, 16);
             }
         } else {
 #pragma unroll
-            for (int r = 0; r < ROWS; ++r)
+            for (int r = 0; r < S::ROWS; ++r)
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) {
-                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
-                    x[r][j] = idx < a.n ? a.in[idx] : identity;
+                for (int j = 0; j < S::VEC; ++j) {
+                    const uint32_t idx = base + (r * THREADS + tid) * S::VEC + j;
+                    x[r][j] = idx < a.n ? a.in[idx] : a.identity;
                 }
         }
-
-        if (WIDE_SUM) {
-            // Exact sum of the valid elements, widened, one atomic per warp.
-            unsigned long long s = 0;
-#pragma unroll
-            for (int r = 0; r < ROWS; ++r)
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) {
-                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
-                    if (idx < a.n) {
-                        if (std::is_signed<T>::value) s += (unsigned long long)(long long)x[r][j];
-                        else s += (unsigned long long)x[r][j];
-                    }
-                }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o);
-            if (lane == 0) atomicAdd(a.wide_sum, s);
-        }
-
-        // Per-row warp scans of the thread totals.
-        T winc[ROWS];
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            T acc = x[r][0];
-#pragma unroll
-            for (int j = 1; j < VEC; ++j) acc = op(acc, x[r][j]);
-            winc[r] = dev::warp_inclusive_scan(acc, op);
-            if (lane == 31) s_rw[r * (THREADS / 32) + warp] = winc[r];
-        }
+        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix);
         __syncthreads();
+    }
+}
 
-        if (warp == 0) {
-            // Exclusive scan of the row-warp totals, in sequence order.
-            T v[PER];
+// The same scan with bulk-copy staging: while a CTA finishes tile t, the TMA
+// engine already copies its next tile into a shared-memory stage, so the
+// loads overlap the look-back and the stores.
+template <typename T, typename Op, bool WIDE_SUM>
+__global__ void __launch_bounds__(THREADS) k_scan_staged(ScanArgs<T> a)
+{
+    using S = ScanShape<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* stage = reinterpret_cast<T*>(smem_raw);
+    __shared__ T s_rw[S::RW];
+    __shared__ T s_prefix;
+    __shared__ uint32_t s_next;
+    __shared__ __align__(8) uint64_t s_bar;
+    const int tid = threadIdx.x;
+    auto bulk_tile = [&](uint32_t t) { return a.aligned && (uint64_t)(t + 1) * S::TILE <= a.n; };
+    auto issue = [&](uint32_t t) {
+        dev::fence_proxy_async();
+        dev::mbar_arrive_expect_tx(&s_bar, S::TILE * sizeof(T));
+        dev::bulk_g2s(stage, a.in + (size_t)t * S::TILE, S::TILE * sizeof(T), &s_bar);
+    };
+    if (tid == 0) {
+        dev::mbar_init(&s_bar, 1);
+        dev::fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t t = atomicAdd(a.tile_ctr, 1u);
+        s_next = t;
+        if (t < a.num_tiles && bulk_tile(t)) issue(t);
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (;;) {
+        const uint32_t t = s_next;
+        if (t >= a.num_tiles) break;
+        const uint32_t base = t * S::TILE;
+        const bool full = base + S::TILE <= a.n;
+        T x[S::ROWS][S::VEC];
+        if (bulk_tile(t)) {
+            if (!dev::mbar_wait_bounded(&s_bar, phase)) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+            phase ^= 1;
 #pragma unroll
-            for (int k = 0; k < PER; ++k) v[k] = s_rw[lane * PER + k];
-            T lt = v[0];
-#pragma unroll
-            for (int k = 1; k < PER; ++k) lt = op(lt, v[k]);
-            const T linc = dev::warp_inclusive_scan(lt, op);
-            const T up = __shfl_up_sync(FULL_MASK, linc, 1);
-            T run = lane == 0 ? identity : up;
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                s_rw[lane * PER + k] = run;
-                run = op(run, v[k]);
+            for (int r = 0; r < S::ROWS; ++r) {
+                const uint4 w = *reinterpret_cast<const uint4*>(stage + (r * THREADS + tid) * S::VEC);
+                memcpy(x[r], &w, 16);
             }
-            const T agg = __shfl_sync(FULL_MASK, linc, 31);
-            const uint64_t my_seq = a.seq0 + t;
-            if (lane == 0) Status<T>::publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
-
-            // Warp-cooperative look-back: lane l inspects tile w_end-32+l;
-            // the nearest tile holding an inclusive prefix ends the walk.
-            T excl = identity;
-            if (t > 0) {
-                bool have = false;
-                int64_t w_end = t;
-                for (;;) {
-                    const int64_t k = w_end - 32 + lane;
-                    uint64_t flag = FLAG_PRE;
-                    T val = identity;
-                    bool gave_up = false;
-                    if (k >= 0) {
-                        if (!Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) {
-                            const unsigned long long start = dev::globaltimer();
-                            for (uint32_t spin = 1;; ++spin) {
-                                if (Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) break;
-                                if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                    gave_up = true;
-                                    flag = FLAG_PRE;
-                                    val = identity;
-                                    break;
-                                }
-                                if (spin > 32) __nanosleep(64);
-                            }
-                        }
-                    }
-                    if (__any_sync(FULL_MASK, gave_up)) {
-                        if (lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                    }
-                    const uint32_t pre = __ballot_sync(FULL_MASK, flag == FLAG_PRE);
-                    const int L = pre ? 31 - __clz(pre) : 0;
-                    const T contrib = lane >= L ? val : identity;
-                    const T wsum = dev::warp_reduce(contrib, op);
-                    excl = have ? op(wsum, excl) : wsum;
-                    have = true;
-                    if (pre) break;
-                    w_end -= 32;
+        } else {
+#pragma unroll
+            for (int r = 0; r < S::ROWS; ++r)
+#pragma unroll
+                for (int j = 0; j < S::VEC; ++j) {
+                    const uint32_t idx = base + (r * THREADS + tid) * S::VEC + j;
+                    x[r][j] = idx < a.n ? a.in[idx] : a.identity;
                 }
-                if (lane == 0) Status<T>::publish(a.ring, my_seq, FLAG_PRE, op(excl, agg));
-            }
-            if (lane == 0) s_prefix = excl;
         }
-        __syncthreads();
-
-        const T prefix = s_prefix;
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            const T wexc = __shfl_up_sync(FULL_MASK, winc[r], 1);
-            // The first row-warp's exclusive value is the identity; combining
-            // it on the right would break operators whose identity only works
-            // from the left (the right projection), so it is skipped.
-            T run = (r == 0 && warp == 0) ? prefix : op(prefix, s_rw[r * (THREADS / 32) + warp]);
-            if (lane > 0) run = op(run, wexc);
-            T o[VEC];
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-                const T inc = op(run, x[r][j]);
-                o[j] = a.exclusive ? run : inc;
-                run = inc;
-                if (a.total != nullptr && base + (r * THREADS + tid) * VEC + j == a.n - 1)
-                    store_wide<T>(a.total, inc);
-            }
-            if (full && a.aligned) {
-                uint4 w;
-                memcpy(&w, o, 16);
-                *reinterpret_cast<uint4*>(a.out + base + (r * THREADS + tid) * VEC) = w;
-            } else {
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) {
-                    const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
-                    if (idx < a.n) a.out[idx] = o[j];
-                }
-            }
+        __syncthreads();  // stage consumed: fetch the next tile behind this one
+        if (tid == 0) {
+            const uint32_t nt = atomicAdd(a.tile_ctr, 1u);
+            s_next = nt;
+            if (nt < a.num_tiles && bulk_tile(nt)) issue(nt);
         }
+        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix);
         __syncthreads();
     }
 }
@@ -295,13 +376,16 @@ __global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
 std::map<const void*, int> g_occ;
 std::mutex g_occ_m;
 
-template <typename F> int blocks_per_sm(F* kernel)
+template <typename F> int blocks_per_sm(F* kernel, std::size_t smem = 0)
 {
     std::lock_guard<std::mutex> lock(g_occ_m);
     auto it = g_occ.find((const void*)kernel);
     if (it != g_occ.end()) return it->second;
+    check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    (int)cudaSharedmemCarveoutMaxShared),
+               "cudaFuncSetAttribute");
     int b = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, THREADS, 0),
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, THREADS, smem),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     b = std::max(b, 1);
     g_occ[(const void*)kernel] = b;
@@ -345,11 +429,17 @@ struct ScanLaunch {
         a.total = use_wide ? nullptr : total_dev;
         if (!use_wide) a.wide_sum = nullptr;
 
+        // The bulk-copy staged kernel (k_scan_staged) measured slower: a CTA
+        // that takes its next tile early publishes that tile's status late,
+        // which stalls every successor's look-back. The direct-load kernel is
+        // the default.
         auto kernel = use_wide ? &k_scan<T, Op, can_wide> : &k_scan<T, Op, false>;
-        const int grid = (int)std::min<std::size_t>(a.num_tiles, (std::size_t)ctx.sm_count * blocks_per_sm(kernel));
+        const std::size_t smem = 0;
+        const int grid =
+            (int)std::min<std::size_t>(a.num_tiles, (std::size_t)ctx.sm_count * blocks_per_sm(kernel, smem));
         {
             kernel_timer kt(ctx, "scan.lookback");
-            kernel<<<grid, THREADS, 0, ctx.stream>>>(a);
+            kernel<<<grid, THREADS, smem, ctx.stream>>>(a);
             check_cuda(cudaGetLastError(), "scan launch");
         }
         if (use_wide)

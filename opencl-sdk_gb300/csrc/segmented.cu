@@ -1,0 +1,712 @@
+// Batched segmented sort: every segment [offsets[i], offsets[i+1]) of a key
+// (+ value) array is sorted independently and stably, for many segments of
+// uneven length in one call whose launch sequence is fixed (every decision is
+// made on the device, so the call can be captured in a CUDA graph).
+//
+// No reference counterpart: the reference sorts one array per call
+// (detail::radix_sort, lib/src/Compute/Algorithm.cpp:453-527); sorting a batch
+// there means one call per array. The semantics per segment are the same as
+// that sort's: stable, the order-preserving key bijection of Algorithm.cpp:
+// 459-469, optional 32-bit values moved alongside.
+//
+// Size classes (decided by k_seg_classify):
+//   * tiny/small (<= WARP_CAP): one warp per segment, stable LSD radix sort in
+//     warp-private shared memory over the digit positions that vary inside the
+//     segment only;
+//   * medium (<= cta_cap): one CTA per segment, the same LSD in CTA shared
+//     memory;
+//   * large: a batched onesweep: the tiles of all large segments form one
+//     sequence, per-segment digit histograms come from one read of the keys,
+//     and the decoupled look-back of each digit pass stops at the first tile
+//     of its segment.
+// The small/medium path and the large path are independent and run on two
+// streams that fork from and join back to the context's stream.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "device_common.cuh"
+#include "runtime.hpp"
+#include "segmented.hpp"
+#include "sort_internal.hpp"
+
+namespace gbc {
+namespace seg {
+
+using dev::FULL_MASK;
+using onesweep::RADIX;
+using onesweep::RING_TILES;
+
+constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
+constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
+constexpr int WARP_CAP = 256;  // keys a warp sorts on its own
+constexpr int SMALL_THREADS = 256;
+constexpr int SMALL_WARPS = SMALL_THREADS / 32;
+
+template <typename K> struct Traits;
+template <> struct Traits<uint32_t> {
+    static constexpr int PASSES = 4;
+    static constexpr int CTA_CAP = 8192;
+};
+template <> struct Traits<uint64_t> {
+    static constexpr int PASSES = 8;
+    static constexpr int CTA_CAP = 6144;
+};
+
+__device__ __forceinline__ uint64_t pack_status(uint64_t flag, uint64_t seq, uint32_t v)
+{
+    return (flag << 62) | ((seq & TAG_MASK) << 32) | v;
+}
+
+//! Per-call control block (zeroed before each call).
+struct SegControl {
+    uint32_t n_warp, n_cta, n_large;  // list lengths
+    uint32_t large_tiles;             // tiles of all large segments
+    uint32_t warp_next, cta_next;     // work queue heads
+    uint32_t hist_next;
+    uint32_t tile_ctr[8];
+    uint32_t pad[5];
+};
+
+template <typename K> struct SegArgs {
+    const K* in_k;
+    K* out_k;
+    K* alt_k;
+    const uint32_t* in_v;
+    uint32_t* out_v;
+    uint32_t* alt_v;
+    const uint32_t* off;
+    uint32_t nseg;
+    uint32_t cta_cap;
+    dev::KeyXform<K> xf;
+    SegControl* ctl;
+    uint32_t* warp_list;
+    uint32_t* cta_list;
+    uint32_t* large_list;
+    uint32_t* tile_begin;   // per large segment (n_large + 1)
+    uint32_t* tile_seg;     // large tile -> index into large_list
+    uint32_t* seg_hist;     // [large][PASSES][256]: bin start (absolute) per pass
+    uint32_t max_large;
+    uint32_t max_tiles;
+    uint64_t* ring;
+    uint64_t seq0;
+    int* err;
+};
+
+// ---------------------------------------------------------------------------
+// Classification
+// ---------------------------------------------------------------------------
+template <typename K> __global__ void k_seg_classify(SegArgs<K> a)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nseg; i += stride) {
+        const uint32_t b = a.off[i], e = a.off[i + 1];
+        if (e < b) {
+            dev::raise_error(a.err, dev::ERR_BAD_SEGMENT);
+            continue;
+        }
+        const uint32_t len = e - b;
+        if (len == 0) continue;
+        if (len <= WARP_CAP) {
+            a.warp_list[atomicAdd(&a.ctl->n_warp, 1u)] = i;
+        } else if (len <= a.cta_cap) {
+            a.cta_list[atomicAdd(&a.ctl->n_cta, 1u)] = i;
+        } else {
+            const uint32_t j = atomicAdd(&a.ctl->n_large, 1u);
+            if (j < a.max_large) a.large_list[j] = i;
+            else dev::raise_error(a.err, dev::ERR_BAD_SEGMENT);
+        }
+    }
+}
+
+// One CTA: exclusive scan of the large segments' tile counts, then the
+// tile -> segment map.
+template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_plan(SegArgs<K> a)
+{
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const uint32_t nl = min(a.ctl->n_large, a.max_large);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < nl; base += 1024) {
+        const uint32_t j = base + threadIdx.x;
+        uint32_t cnt = 0;
+        if (j < nl) {
+            const uint32_t s = a.large_list[j];
+            cnt = (a.off[s + 1] - a.off[s] + TILE - 1) / TILE;
+        }
+        uint32_t x = dev::warp_inclusive_scan(cnt, [](uint32_t p, uint32_t q) { return p + q; });
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        uint32_t before = s_carry;
+        for (int w = 0; w < warp; ++w) before += s_warp[w];
+        if (j < nl) a.tile_begin[j] = before + x - cnt;
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry = before + x;
+        __syncthreads();
+    }
+    const uint32_t total = min(s_carry, a.max_tiles);
+    if (threadIdx.x == 0) {
+        a.tile_begin[nl] = total;
+        a.ctl->large_tiles = total;
+    }
+    __syncthreads();
+    // tile -> segment: warp w fills the tiles of segments w, w + 32, ...
+    for (uint32_t j = warp; j < nl; j += 32) {
+        const uint32_t t0 = a.tile_begin[j], t1 = min(a.tile_begin[j + 1], total);
+        for (uint32_t t = t0 + lane; t < t1; t += 32) a.tile_seg[t] = j;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory LSD sort of one segment by a group of GW warps (GW = 1: a
+// warp on its own; GW = SMALL_WARPS: the whole CTA). Stable: items are ranked
+// in index order (warp chunk, row, lane) and scattered by digit.
+// ---------------------------------------------------------------------------
+template <int GW> __device__ __forceinline__ void group_sync()
+{
+    if (GW == 1) __syncwarp();
+    else __syncthreads();
+}
+
+template <typename K, bool HAS_V, int GW>
+__device__ void group_sort(K* k0, K* k1, uint32_t* v0, uint32_t* v1, uint32_t* rd, uint32_t* hist,
+                           uint32_t* scratch, uint32_t len, dev::KeyXform<K> xf, int gw, int lane,
+                           bool& in_k1)
+{
+    constexpr int P = Traits<K>::PASSES;
+    // Which digit positions vary inside the segment.
+    K diff = 0;
+    const K first = xf(k0[0]);
+    for (uint32_t i = gw * 32 + lane; i < len; i += GW * 32) diff |= xf(k0[i]) ^ first;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) diff |= __shfl_xor_sync(FULL_MASK, diff, o);
+    if (GW > 1) {
+        // combine the warps' masks (scratch holds 2 x 32 words)
+        if (lane == 0) {
+            scratch[gw * 2] = (uint32_t)diff;
+            scratch[gw * 2 + 1] = (uint32_t)((uint64_t)diff >> 32);
+        }
+        __syncthreads();
+        uint64_t all = 0;
+        for (int w = 0; w < GW; ++w) all |= (uint64_t)scratch[w * 2] | ((uint64_t)scratch[w * 2 + 1] << 32);
+        diff = (K)all;
+        __syncthreads();
+    }
+    const uint32_t chunk = ((len + GW * 32 - 1) / (GW * 32)) * 32;  // items per warp, whole rows
+    const uint32_t rows = chunk / 32;
+    in_k1 = false;
+    for (int p = 0; p < P; ++p) {
+        if ((((uint64_t)diff >> (8 * p)) & 0xFF) == 0) continue;
+        const int shift = 8 * p;
+        for (int i = (GW > 1 ? threadIdx.x : lane); i < GW * RADIX; i += GW * 32) hist[i] = 0;
+        group_sync<GW>();
+        uint32_t* wh = hist + gw * RADIX;
+        for (uint32_t r = 0; r < rows; ++r) {
+            const uint32_t idx = gw * chunk + r * 32 + lane;
+            const bool valid = idx < len;
+            const uint32_t d = valid ? (uint32_t)(xf(k0[idx]) >> shift) & 0xFFu : 0xFFu;
+            const uint32_t peers = __match_any_sync(FULL_MASK, d);
+            const int leader = 31 - __clz(peers);
+            uint32_t before = 0;
+            if (lane == leader) {
+                before = wh[d];
+                wh[d] = before + __popc(peers);
+            }
+            before = __shfl_sync(FULL_MASK, before, leader);
+            if (valid) rd[idx] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
+            __syncwarp();
+        }
+        group_sync<GW>();
+        // digit starts and per-warp offsets
+        if (GW == 1) {
+            uint32_t c[8], s = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c[q] = hist[lane * 8 + q];
+                s += c[q];
+            }
+            const uint32_t incl = dev::warp_inclusive_scan(s, [](uint32_t x, uint32_t y) { return x + y; });
+            uint32_t run = incl - s;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                hist[lane * 8 + q] = run;
+                run += c[q];
+            }
+        } else {
+            uint32_t count = 0;
+            if (threadIdx.x < RADIX) {
+                for (int w = 0; w < GW; ++w) {
+                    const uint32_t c = hist[w * RADIX + threadIdx.x];
+                    hist[w * RADIX + threadIdx.x] = count;
+                    count += c;
+                }
+            }
+            const uint32_t start = dev::bins_exclusive_sum(count, scratch + 64);
+            if (threadIdx.x < RADIX)
+                for (int w = 0; w < GW; ++w) hist[w * RADIX + threadIdx.x] += start;
+        }
+        group_sync<GW>();
+        for (uint32_t r = 0; r < rows; ++r) {
+            const uint32_t idx = gw * chunk + r * 32 + lane;
+            if (idx < len) {
+                const uint32_t x = rd[idx];
+                const uint32_t pos = wh[x & 0xFF] + (x >> 8);
+                k1[pos] = k0[idx];
+                if (HAS_V) v1[pos] = v0[idx];
+            }
+        }
+        group_sync<GW>();
+        K* tk = k0;
+        k0 = k1;
+        k1 = tk;
+        uint32_t* tv = v0;
+        v0 = v1;
+        v1 = tv;
+        in_k1 = !in_k1;
+    }
+}
+
+template <typename K, bool HAS_V>
+__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr std::size_t per_warp = 2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + RADIX * 4;
+    unsigned char* base = smem + warp * per_warp;
+    K* k0 = reinterpret_cast<K*>(base);
+    K* k1 = k0 + WARP_CAP;
+    uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + WARP_CAP);
+    uint32_t* v1 = v0 + (HAS_V ? WARP_CAP : 0);
+    uint32_t* rd = v1 + (HAS_V ? WARP_CAP : 0);
+    uint32_t* hist = rd + WARP_CAP;
+    const uint32_t total = a.ctl->n_warp;
+    for (;;) {
+        uint32_t w = 0;
+        if (lane == 0) w = atomicAdd(&a.ctl->warp_next, 1u);
+        w = __shfl_sync(FULL_MASK, w, 0);
+        if (w >= total) break;
+        const uint32_t s = a.warp_list[w];
+        const uint32_t b = a.off[s], len = a.off[s + 1] - b;
+        for (uint32_t i = lane; i < len; i += 32) {
+            k0[i] = a.in_k[b + i];
+            if (HAS_V) v0[i] = a.in_v[b + i];
+        }
+        __syncwarp();
+        bool flipped = false;
+        if (len > 1) group_sort<K, HAS_V, 1>(k0, k1, v0, v1, rd, hist, nullptr, len, a.xf, 0, lane, flipped);
+        const K* rk = flipped ? k1 : k0;
+        const uint32_t* rv = flipped ? v1 : v0;
+        for (uint32_t i = lane; i < len; i += 32) {
+            a.out_k[b + i] = rk[i];
+            if (HAS_V) a.out_v[b + i] = rv[i];
+        }
+        __syncwarp();
+    }
+}
+
+template <typename K, bool HAS_V>
+__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t cap = a.cta_cap;
+    K* k0 = reinterpret_cast<K*>(smem);
+    K* k1 = k0 + cap;
+    uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + cap);
+    uint32_t* v1 = v0 + (HAS_V ? cap : 0);
+    uint32_t* rd = v1 + (HAS_V ? cap : 0);
+    uint32_t* hist = rd + cap;
+    __shared__ uint32_t scratch[64 + 8];
+    __shared__ uint32_t s_work;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t total = a.ctl->n_cta;
+    for (;;) {
+        if (threadIdx.x == 0) s_work = atomicAdd(&a.ctl->cta_next, 1u);
+        __syncthreads();
+        const uint32_t w = s_work;
+        if (w >= total) break;
+        const uint32_t s = a.cta_list[w];
+        const uint32_t b = a.off[s], len = a.off[s + 1] - b;
+        for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
+            k0[i] = a.in_k[b + i];
+            if (HAS_V) v0[i] = a.in_v[b + i];
+        }
+        __syncthreads();
+        bool flipped = false;
+        group_sort<K, HAS_V, SMALL_WARPS>(k0, k1, v0, v1, rd, hist, scratch, len, a.xf, warp, lane, flipped);
+        const K* rk = flipped ? k1 : k0;
+        const uint32_t* rv = flipped ? v1 : v0;
+        for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
+            a.out_k[b + i] = rk[i];
+            if (HAS_V) a.out_v[b + i] = rv[i];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Large segments: per-segment digit histograms -> absolute bin starts.
+// One CTA per large segment (work queue).
+// ---------------------------------------------------------------------------
+template <typename K> __global__ void __launch_bounds__(256) k_seg_large_hist(SegArgs<K> a)
+{
+    constexpr int P = Traits<K>::PASSES;
+    __shared__ uint32_t sh[2][P * RADIX];
+    __shared__ uint32_t s_scratch[8];
+    __shared__ uint32_t s_work;
+    const uint32_t nl = min(a.ctl->n_large, a.max_large);
+    for (;;) {
+        if (threadIdx.x == 0) s_work = atomicAdd(&a.ctl->hist_next, 1u);
+        for (int i = threadIdx.x; i < 2 * P * RADIX; i += 256) (&sh[0][0])[i] = 0;
+        __syncthreads();
+        const uint32_t j = s_work;
+        if (j >= nl) break;
+        const uint32_t s = a.large_list[j];
+        const uint32_t b = a.off[s], e = a.off[s + 1];
+        uint32_t* my = sh[(threadIdx.x >> 5) & 1];
+        for (uint32_t i = b + threadIdx.x; i < e; i += 256) {
+            const K t = a.xf(a.in_k[i]);
+#pragma unroll
+            for (int p = 0; p < P; ++p) atomicAdd(&my[p * RADIX + (uint32_t)((t >> (8 * p)) & 0xFF)], 1u);
+        }
+        __syncthreads();
+        for (int p = 0; p < P; ++p) {
+            const uint32_t c = sh[0][p * RADIX + (threadIdx.x & 255)] + sh[1][p * RADIX + (threadIdx.x & 255)];
+            const uint32_t ex = dev::bins_exclusive_sum(c, s_scratch);
+            a.seg_hist[((size_t)j * P + p) * RADIX + threadIdx.x] = b + ex;
+        }
+        __syncthreads();
+    }
+}
+
+// One digit pass over every large segment's tiles (cf. onesweep::k_pass).
+template <typename K, bool HAS_V, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int slot)
+{
+    constexpr int P = Traits<K>::PASSES;
+    constexpr int WARPS = THREADS / 32;
+    constexpr int TILE = THREADS * ITEMS;
+    const uint32_t num_tiles = a.ctl->large_tiles;
+    const int shift = 8 * slot;
+    // pass s writes out when (P - 1 - s) is even; P is even, so pass 0 reads
+    // the input and writes the scratch buffer.
+    const bool dst_out = ((P - 1 - slot) & 1) == 0;
+    K* dst_k = dst_out ? a.out_k : a.alt_k;
+    uint32_t* dst_v = dst_out ? a.out_v : a.alt_v;
+    const K* src_k = slot == 0 ? a.in_k : (dst_out ? a.alt_k : a.out_k);
+    const uint32_t* src_v = slot == 0 ? a.in_v : (dst_out ? a.alt_v : a.out_v);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);
+    K* s_keys = reinterpret_cast<K*>(warp_hist + WARPS * RADIX);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    __shared__ uint32_t s_bin_off[RADIX], s_local[RADIX];
+    __shared__ uint32_t s_scratch[8];
+    __shared__ uint32_t s_tile;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_abort = 0;
+    const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.max_tiles;
+
+    for (;;) {
+        if (tid == 0) s_tile = atomicAdd(&a.ctl->tile_ctr[slot], 1u);
+        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= num_tiles) break;
+        const uint32_t j = a.tile_seg[t];
+        const uint32_t s = a.large_list[j];
+        const uint32_t segb = a.off[s], sege = a.off[s + 1];
+        const uint32_t lt = t - a.tile_begin[j];
+        const uint32_t tile_base = segb + lt * TILE;
+        const uint32_t valid = min((uint32_t)TILE, sege - tile_base);
+        const bool first = lt == 0;
+
+        const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
+        K key[ITEMS];
+        uint32_t rd[ITEMS];
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t idx = wbase + i * 32;
+            if (idx < sege) {
+                key[i] = src_k[idx];
+                rd[i] = (uint32_t)(a.xf(key[i]) >> shift) & 0xFFu;
+            } else {
+                key[i] = 0;
+                rd[i] = 0xFFu;
+            }
+        }
+        uint32_t* wh = warp_hist + warp * RADIX;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i];
+            const uint32_t peers = __match_any_sync(FULL_MASK, d);
+            const int leader = 31 - __clz(peers);
+            uint32_t before = 0;
+            if (lane == leader) {
+                before = wh[d];
+                wh[d] = before + __popc(peers);
+            }
+            before = __shfl_sync(FULL_MASK, before, leader);
+            rd[i] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t count = 0;
+        if (tid < RADIX) {
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t c = warp_hist[w * RADIX + tid];
+                warp_hist[w * RADIX + tid] = count;
+                count += c;
+            }
+        }
+        uint32_t agg = count;
+        if (tid == RADIX - 1) agg -= (uint32_t)TILE - valid;
+        uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
+        if (tid < RADIX) dev::st_relaxed(&my_status[tid], pack_status(first ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
+        const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
+        if (tid < RADIX) s_local[tid] = local;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i] & 0xFFu;
+            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
+            s_keys[pos] = key[i];
+            rd[i] = pos;
+        }
+        if (HAS_V) {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t idx = wbase + i * 32;
+                s_vals[rd[i]] = idx < sege ? src_v[idx] : 0u;
+            }
+        }
+        if (tid < RADIX) {
+            uint32_t excl = 0;
+            if (!first) {
+                uint64_t k = t - 1;
+                for (;;) {
+                    const uint64_t seq = seq0 + k;
+                    const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
+                    const uint64_t want = seq & TAG_MASK;
+                    uint64_t w = dev::ld_relaxed(p);
+                    bool gave_up = false;
+                    if ((w >> 62) == 0 || ((w >> 32) & TAG_MASK) != want) {
+                        const unsigned long long start = dev::globaltimer();
+                        for (uint32_t spin = 1;; ++spin) {
+                            w = dev::ld_relaxed(p);
+                            if ((w >> 62) != 0 && ((w >> 32) & TAG_MASK) == want) break;
+                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                gave_up = true;
+                                break;
+                            }
+                            if (spin > 32) __nanosleep(64);
+                        }
+                    }
+                    if (gave_up) {
+                        dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                        s_abort = 1;
+                        break;
+                    }
+                    excl += (uint32_t)w;
+                    if ((w >> 62) == FLAG_PRE || k == 0) break;
+                    --k;
+                }
+                dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + agg));
+            }
+            s_bin_off[tid] = a.seg_hist[((size_t)j * P + slot) * RADIX + tid] + excl - s_local[tid];
+        }
+        __syncthreads();
+        const uint32_t limit = s_abort ? 0u : valid;
+        for (uint32_t q = tid; q < limit; q += THREADS) {
+            const K kk = s_keys[q];
+            const uint32_t d = (uint32_t)(a.xf(kk) >> shift) & 0xFFu;
+            const uint32_t o = s_bin_off[d] + q;
+            if (o >= segb && o < sege) {
+                dst_k[o] = kk;
+                if (HAS_V) dst_v[o] = s_vals[q];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host
+// ---------------------------------------------------------------------------
+template <typename K, bool HAS_V> struct LargeShape;
+template <bool HV> struct LargeShape<uint32_t, HV> {
+    static constexpr int THREADS = 256, ITEMS = 16;
+};
+template <bool HV> struct LargeShape<uint64_t, HV> {
+    static constexpr int THREADS = 256, ITEMS = 12;
+};
+
+template <typename F> static void set_smem(F* kernel, std::size_t bytes)
+{
+    if (bytes > 0)  // static shared memory adds to this against the 48 KiB default
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+                   "cudaFuncSetAttribute");
+}
+
+template <typename F> static int occupancy(F* kernel, int threads, std::size_t smem)
+{
+    int b = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    return std::max(b, 1);
+}
+
+template <typename K, bool HAS_V>
+void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uint32_t* out_v, std::size_t n,
+         const uint32_t* off, std::size_t nseg, dev::KeyXform<K> xf, const seg_options& opt)
+{
+    constexpr int P = Traits<K>::PASSES;
+    using LS = LargeShape<K, HAS_V>;
+    constexpr int TILE = LS::THREADS * LS::ITEMS;
+    // Largest segment one CTA sorts in shared memory: two copies of keys (and
+    // values) plus a packed rank per element, and 8 KiB of warp histograms,
+    // must fit the 227 KiB opt-in (u32: 12 B/elem keys-only, 20 B/elem with
+    // values; u64: 20 and 28 B/elem).
+    constexpr int MAX_CAP = sizeof(K) == 4 ? (HAS_V ? 10240 : 16384) : (HAS_V ? 7168 : 10240);
+    const uint32_t cta_cap =
+        (uint32_t)std::max<int>(WARP_CAP + 1, std::min<int>(opt.cta_cap > 0 ? opt.cta_cap : MAX_CAP, MAX_CAP));
+    const uint32_t max_large = (uint32_t)std::min<std::size_t>(nseg, n / (cta_cap + 1) + 1);
+    const uint32_t max_tiles = (uint32_t)(n / TILE + max_large + 1);
+
+    temp_buffer ctl(ctx.resource, sizeof(SegControl));
+    temp_buffer lists(ctx.resource, (2 * nseg + max_large + (max_large + 1)) * sizeof(uint32_t));
+    temp_buffer tile_seg(ctx.resource, (std::size_t)max_tiles * sizeof(uint32_t));
+    temp_buffer seg_hist(ctx.resource, (std::size_t)max_large * P * RADIX * sizeof(uint32_t));
+    const bool maybe_large = n > cta_cap;
+    temp_buffer alt_k(ctx.resource, maybe_large ? n * sizeof(K) : 0);
+    temp_buffer alt_v(ctx.resource, maybe_large && HAS_V ? n * sizeof(uint32_t) : 0);
+    check_cuda(cudaMemsetAsync(ctl.get(), 0, sizeof(SegControl), ctx.stream), "cudaMemsetAsync");
+
+    SegArgs<K> a;
+    a.in_k = in_k;
+    a.out_k = out_k;
+    a.alt_k = alt_k.as<K>();
+    a.in_v = in_v;
+    a.out_v = out_v;
+    a.alt_v = alt_v.as<uint32_t>();
+    a.off = off;
+    a.nseg = (uint32_t)nseg;
+    a.cta_cap = cta_cap;
+    a.xf = xf;
+    a.ctl = ctl.as<SegControl>();
+    uint32_t* l = lists.as<uint32_t>();
+    a.warp_list = l;
+    a.cta_list = l + nseg;
+    a.large_list = l + 2 * nseg;
+    a.tile_begin = l + 2 * nseg + max_large;
+    a.tile_seg = tile_seg.as<uint32_t>();
+    a.seg_hist = seg_hist.as<uint32_t>();
+    a.max_large = max_large;
+    a.max_tiles = max_tiles;
+    a.ring = ctx.lookback_ring;
+    a.seq0 = maybe_large ? ctx.reserve_seq((uint64_t)P * max_tiles) : 0;
+    a.err = ctx.d_error;
+
+    {
+        kernel_timer kt(ctx, "segsort.classify");
+        const int grid = (int)std::max<std::size_t>(1, std::min<std::size_t>((nseg + 255) / 256, (std::size_t)ctx.sm_count * 4));
+        k_seg_classify<K><<<grid, 256, 0, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "segmented sort classify launch");
+    }
+    // Fork: the large-segment path runs on the auxiliary stream.
+    cudaStream_t aux = ctx.aux_stream();
+    check_cuda(cudaEventRecord(ctx.fork_event, ctx.stream), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(aux, ctx.fork_event, 0), "cudaStreamWaitEvent");
+
+    {
+        kernel_timer kt(ctx, "segsort.small_warp");
+        constexpr std::size_t per_warp = 2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + RADIX * 4;
+        const std::size_t smem = per_warp * SMALL_WARPS;
+        auto kern = &k_seg_small_warp<K, HAS_V>;
+        set_smem(kern, smem);
+        const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
+        kern<<<grid, SMALL_THREADS, smem, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "segmented sort warp launch");
+    }
+    {
+        kernel_timer kt(ctx, "segsort.small_cta");
+        const std::size_t smem = (std::size_t)cta_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + SMALL_WARPS * RADIX * 4;
+        auto kern = &k_seg_small_cta<K, HAS_V>;
+        set_smem(kern, smem);
+        const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
+        kern<<<grid, SMALL_THREADS, smem, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "segmented sort cta launch");
+    }
+    if (maybe_large) {
+        k_seg_plan<K, TILE><<<1, 1024, 0, aux>>>(a);
+        check_cuda(cudaGetLastError(), "segmented sort plan launch");
+        auto hk = &k_seg_large_hist<K>;
+        k_seg_large_hist<K><<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
+        check_cuda(cudaGetLastError(), "segmented sort histogram launch");
+        auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS>;
+        const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 4 + (std::size_t)TILE * sizeof(K) +
+                                  (HAS_V ? (std::size_t)TILE * 4 : 0);
+        set_smem(pk, psmem);
+        const int pgrid = ctx.sm_count * occupancy(pk, LS::THREADS, psmem);
+        for (int s = 0; s < P; ++s) {
+            pk<<<pgrid, LS::THREADS, psmem, aux>>>(a, s);
+            check_cuda(cudaGetLastError(), "segmented sort pass launch");
+        }
+    }
+    // Join.
+    check_cuda(cudaEventRecord(ctx.join_event, aux), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(ctx.stream, ctx.join_event, 0), "cudaStreamWaitEvent");
+}
+
+}  // namespace seg
+
+uint32_t segsort_cta_cap(int key_bytes, bool has_values)
+{
+    return key_bytes == 4 ? (has_values ? 10240u : 16384u) : (has_values ? 7168u : 10240u);
+}
+
+std::string segsort_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
+{
+    // distribution class: average segment length, as a power of two
+    const std::size_t avg = num_segments ? n / num_segments : n;
+    return std::string("segsort:") + (key_bytes == 4 ? "u32" : "u64") + (has_values ? "kv" : "k") + ":" +
+           tuning_table::size_class(n) + ":avg" + tuning_table::size_class(avg);
+}
+
+void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
+                    const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, const uint32_t* offsets,
+                    std::size_t num_segments, bool descending, const seg_options& opt)
+{
+    if (key_bytes != 4 && key_bytes != 8) throw std::invalid_argument("segmented_sort: keys must be 32 or 64 bits");
+    if (key_kind < 0 || key_kind > 2) throw std::invalid_argument("segmented_sort: unknown key kind");
+    if ((vals_in == nullptr) != (vals_out == nullptr))
+        throw std::invalid_argument("segmented_sort: values need both an input and an output");
+    check_size(n);
+    if (num_segments == 0 || n == 0) return;
+    if (offsets == nullptr || keys_in == nullptr || keys_out == nullptr)
+        throw std::invalid_argument("segmented_sort: null argument");
+    if (num_segments > 0x7FFFFFFFu) throw std::length_error("segmented_sort: too many segments");
+    ctx.activate();
+    if (key_bytes == 4) {
+        const auto xf = dev::make_xform<uint32_t>(key_kind, descending);
+        if (vals_in)
+            seg::run<uint32_t, true>(ctx, static_cast<const uint32_t*>(keys_in), static_cast<uint32_t*>(keys_out),
+                                     vals_in, vals_out, n, offsets, num_segments, xf, opt);
+        else
+            seg::run<uint32_t, false>(ctx, static_cast<const uint32_t*>(keys_in), static_cast<uint32_t*>(keys_out),
+                                      nullptr, nullptr, n, offsets, num_segments, xf, opt);
+    } else {
+        const auto xf = dev::make_xform<uint64_t>(key_kind, descending);
+        if (vals_in)
+            seg::run<uint64_t, true>(ctx, static_cast<const uint64_t*>(keys_in), static_cast<uint64_t*>(keys_out),
+                                     vals_in, vals_out, n, offsets, num_segments, xf, opt);
+        else
+            seg::run<uint64_t, false>(ctx, static_cast<const uint64_t*>(keys_in), static_cast<uint64_t*>(keys_out),
+                                      nullptr, nullptr, n, offsets, num_segments, xf, opt);
+    }
+}
+
+}  // namespace gbc

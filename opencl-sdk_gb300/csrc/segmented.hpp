@@ -1,0 +1,35 @@
+// Batched (segmented) sort and scan: entry points and tunables.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "runtime.hpp"
+
+namespace gbc {
+
+//! Launch-shape choices of the segmented sort (picked by the autotuner).
+struct seg_options {
+    int cta_cap = 0;  // largest segment a single CTA sorts in shared memory (0: the type's maximum)
+};
+
+//! Sorts every segment [offsets[i], offsets[i+1]) independently and stably.
+//! offsets has num_segments + 1 monotone entries (device memory); keys_in ==
+//! keys_out sorts in place. Asynchronous; graph-capturable once the pool is
+//! warm (every temporary then comes from the cache).
+void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
+                    const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, const uint32_t* offsets,
+                    std::size_t num_segments, bool descending, const seg_options& opt);
+
+//! Scan restarted at every segment start (offsets as for segmented_sort;
+//! position 0 always starts a segment). Exclusive: a segment's first output
+//! is the identity.
+void segmented_scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t, op_kind op,
+                    const void* identity, bool exclusive, const uint32_t* offsets, std::size_t num_segments);
+
+std::string segsort_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
+
+//! Largest segment the segmented sort finishes in one CTA's shared memory.
+uint32_t segsort_cta_cap(int key_bytes, bool has_values);
+
+}  // namespace gbc

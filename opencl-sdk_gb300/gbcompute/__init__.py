@@ -168,6 +168,14 @@ _PROTOS = {
     "clc_histogram_even": (_i, [_vp, _vp, _sz, _i, _vp, _sz, C.c_double, C.c_double]),
     "clc_scan_ex": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp]),
     "clc_sort_ex": (_i, [_vp, _vp, _i, _vp, _sz, _i]),
+    "clc_segmented_sort": (_i, [_vp, _vp, _i, _vp, _sz, _vp, _sz, _i]),
+    "clc_segmented_sort_raw": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _vp, _sz, _i]),
+    "clc_segmented_scan": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp, _sz]),
+    "clc_segmented_scan_raw": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp, _sz]),
+    "clc_graph_begin": (_i, [_vp]),
+    "clc_graph_end": (_i, [_vp, C.POINTER(_vp)]),
+    "clc_graph_launch": (_i, [_vp, _vp]),
+    "clc_graph_release": (None, [_vp]),
     "clc_buffer_device_pointer": (_vp, [_vp]),
     "clc_buffer_wrap": (_i, [_vp, _vp, _sz, C.POINTER(_vp)]),
     "clc_context_stream": (_vp, [_vp]),
@@ -513,3 +521,72 @@ def tuning_sort_key(key_bytes: int, has_values: bool, n: int) -> str:
     buf = C.create_string_buffer(128)
     _raise_for(lib.clc_tuning_sort_key(key_bytes, int(has_values), n, buf, 128))
     return buf.value.decode()
+
+
+# ---- batched (segmented) forms and CUDA graphs ----------------------------------
+
+def segmented_sort(ctx: Context, keys: DeviceBuffer, offsets: DeviceBuffer, values: DeviceBuffer | None = None,
+                   descending: bool = False) -> None:
+    """Sorts every segment [offsets[i], offsets[i+1]) of keys (and values) in place."""
+    if offsets.dtype != np.dtype(np.uint32):
+        raise TypeError("segmented_sort: offsets must be uint32")
+    _raise_for(lib.clc_segmented_sort(ctx.handle, keys.handle, clc_type(keys.dtype),
+                                      values.handle if values is not None else None, keys.size, offsets.handle,
+                                      max(offsets.size - 1, 0), int(descending)))
+
+
+def segmented_sort_raw(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int, offsets: int,
+                       num_segments: int, vals_in: int = 0, vals_out: int = 0, descending: bool = False) -> None:
+    _raise_for(lib.clc_segmented_sort_raw(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype),
+                                          C.c_void_p(vals_in or None), C.c_void_p(vals_out or None), n,
+                                          C.c_void_p(offsets), num_segments, int(descending)))
+
+
+def segmented_scan(ctx: Context, inp: DeviceBuffer, out: DeviceBuffer, offsets: DeviceBuffer,
+                   op: binary_op | None = None, exclusive: bool = False) -> None:
+    op = op or ops.plus()
+    _raise_for(lib.clc_segmented_scan(ctx.handle, inp.handle, out.handle, inp.size, clc_type(inp.dtype),
+                                      op.expression.encode(), op.identity.encode(), int(exclusive), offsets.handle,
+                                      max(offsets.size - 1, 0)))
+
+
+def segmented_scan_raw(ctx: Context, inp: int, out: int, n: int, dtype, offsets: int, num_segments: int,
+                       op: binary_op | None = None, exclusive: bool = False) -> None:
+    op = op or ops.plus()
+    _raise_for(lib.clc_segmented_scan_raw(ctx.handle, C.c_void_p(inp), C.c_void_p(out), n, clc_type(dtype),
+                                          op.expression.encode(), op.identity.encode(), int(exclusive),
+                                          C.c_void_p(offsets), num_segments))
+
+
+class Graph:
+    """A CUDA graph of calls captured on a context's stream (clc_graph_*)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def launch(self) -> None:
+        _raise_for(lib.clc_graph_launch(self.ctx.handle, self.handle))
+
+    def release(self) -> None:
+        if self.handle:
+            lib.clc_graph_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def capture(ctx: Context, fn) -> Graph:
+    """Captures the library calls made by fn() into a graph (they do not run)."""
+    _raise_for(lib.clc_graph_begin(ctx.handle))
+    try:
+        fn()
+    finally:
+        h = C.c_void_p()
+        status = lib.clc_graph_end(ctx.handle, C.byref(h))
+    _raise_for(status)
+    return Graph(ctx, h)

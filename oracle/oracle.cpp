@@ -415,4 +415,48 @@ void orc_ref_reduce(const void* in, std::size_t n, int type, int op, const void*
 
 int orc_hardware_threads(void) { return hw_threads(0); }
 
+// ---- batched forms (no reference counterpart; std:: ground truth) ---------
+
+// Every segment [off[i], off[i+1]) sorted independently, stably.
+void orc_std_segmented_sort(void* keys, uint32_t* vals, std::size_t n, int key_bytes, int kind, int desc,
+                            const uint32_t* off, std::size_t nseg, int threads)
+{
+    (void)n;
+    parallel_for(nseg, hw_threads(threads), [&](std::size_t s0, std::size_t s1) {
+        for (std::size_t s = s0; s < s1; ++s) {
+            const std::size_t b = off[s], len = off[s + 1] - off[s];
+            if (key_bytes == 4)
+                std_sort_pairs<uint32_t>(static_cast<uint32_t*>(keys) + b, vals ? vals + b : nullptr, len, kind,
+                                         desc);
+            else
+                std_sort_pairs<uint64_t>(static_cast<uint64_t*>(keys) + b, vals ? vals + b : nullptr, len, kind,
+                                         desc);
+        }
+    });
+}
+
+// Scan restarted at position 0 and at every off[i] (i < nseg).
+void orc_std_segmented_scan(const void* in, void* out, std::size_t n, int type, int op, const void* identity,
+                            int exclusive, const uint32_t* off, std::size_t nseg)
+{
+    std::vector<char> head(n, 0);
+    if (n) head[0] = 1;
+    for (std::size_t i = 0; i < nseg; ++i)
+        if (off[i] < n) head[off[i]] = 1;
+    by_type(type, [&](auto tag) {
+        using T = decltype(tag);
+        T id;
+        std::memcpy(&id, identity, sizeof(T));
+        const T* p = static_cast<const T*>(in);
+        T* o = static_cast<T*>(out);
+        T run = id;
+        for (std::size_t i = 0; i < n; ++i) {
+            if (head[i]) run = id;
+            const T next = head[i] ? p[i] : wrap_apply<T>(op, run, p[i]);
+            o[i] = exclusive ? (head[i] ? id : run) : next;
+            run = next;
+        }
+    });
+}
+
 }  // extern "C"

@@ -60,6 +60,8 @@ def lib():
         L.orc_ref_scan.argtypes = [vp, vp, sz, i, i, vp, i, i]
         L.orc_ref_reduce.argtypes = [vp, sz, i, i, vp, vp, vp, i]
         L.orc_hardware_threads.restype = i
+        L.orc_std_segmented_sort.argtypes = [vp, vp, sz, i, i, i, vp, sz, i]
+        L.orc_std_segmented_scan.argtypes = [vp, vp, sz, i, i, vp, i, vp, sz]
         _lib = L
     return _lib
 
@@ -156,3 +158,34 @@ def histogram_even(x: np.ndarray, bins: int, lower: float, upper: float, threads
 
 def hardware_threads() -> int:
     return lib().orc_hardware_threads()
+
+
+# ---- batched forms ----------------------------------------------------------
+
+def std_segmented_sort(keys: np.ndarray, offsets: np.ndarray, values: np.ndarray | None = None,
+                       descending: bool = False, threads: int = 0):
+    k = np.ascontiguousarray(keys).copy()
+    off = np.ascontiguousarray(offsets, dtype=np.uint32)
+    v = None if values is None else np.ascontiguousarray(values, dtype=np.uint32).copy()
+    lib().orc_std_segmented_sort(_p(k), None if v is None else _p(v), k.size, k.dtype.itemsize, key_kind(k.dtype),
+                                 int(descending), _p(off), off.size - 1, threads)
+    return k, v
+
+
+def std_segmented_scan(x: np.ndarray, offsets: np.ndarray, op: int = OP_PLUS, identity=0,
+                       exclusive: bool = False) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    off = np.ascontiguousarray(offsets, dtype=np.uint32)
+    out = np.empty_like(x)
+    lib().orc_std_segmented_scan(_p(x), _p(out), x.size, _TYPES[x.dtype], op, _p(_ident(x.dtype, identity)),
+                                 int(exclusive), _p(off), off.size - 1)
+    return out
+
+
+def lognormal_segments(num_segments: int, median: float, sigma: float, lo: int, hi: int, seed: int) -> np.ndarray:
+    """Offsets of segments whose lengths are round(lognormal(ln median, sigma)) clipped to [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    lens = np.clip(np.rint(rng.lognormal(np.log(median), sigma, size=num_segments)), lo, hi).astype(np.int64)
+    off = np.zeros(num_segments + 1, dtype=np.int64)
+    np.cumsum(lens, out=off[1:])
+    return off.astype(np.uint32)

@@ -1,0 +1,126 @@
+"""Batched segmented sort and scan on the GPU against the std:: oracle (per
+segment std::stable_sort, restarted sequential scans), bit for bit, and their
+CUDA-graph capture and replay."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def offsets_from_lengths(lens):
+    off = np.zeros(len(lens) + 1, dtype=np.int64)
+    np.cumsum(lens, out=off[1:])
+    return off.astype(np.uint32)
+
+
+LAYOUTS = {
+    # tiny, small (warp), medium (CTA) and large (batched onesweep) segments mixed
+    "lognormal": lambda orc: orc.lognormal_segments(3000, 256, 2.0, 1, 1 << 17, seed=4),
+    "empty_and_single": lambda orc: offsets_from_lengths([0, 1, 0, 0, 2, 1, 0, 33, 0, 1]),
+    "one_large": lambda orc: offsets_from_lengths([300001]),
+    "cta_boundaries": lambda orc: offsets_from_lengths([256, 257, 6144, 6145, 8192, 8193, 255, 1]),
+}
+
+
+@pytest.mark.parametrize("layout", list(LAYOUTS))
+@pytest.mark.parametrize("key_dtype", [np.uint64, np.uint32, np.int32, np.float64])
+@pytest.mark.parametrize("with_values", [True, False])
+def test_segmented_sort(ctx, gbc, orc, layout, key_dtype, with_values):
+    off = LAYOUTS[layout](orc)
+    n = int(off[-1])
+    rng = np.random.default_rng(5)
+    raw = rng.integers(0, 2**63, size=n, dtype=np.uint64)
+    raw[::7] = raw[0]  # duplicates inside segments exercise stability
+    keys = raw.astype(key_dtype) if np.dtype(key_dtype).kind != "f" else raw.view(np.float64).astype(key_dtype)
+    if np.dtype(key_dtype).kind == "f":
+        keys = rng.standard_normal(n).astype(key_dtype)
+        keys[::11] = -0.0
+        keys[1::13] = 0.0
+    vals = np.arange(n, dtype=np.uint32)
+    kb = gbc.DeviceBuffer.from_host(ctx, keys)
+    vb = gbc.DeviceBuffer.from_host(ctx, vals) if with_values else None
+    ob = gbc.DeviceBuffer.from_host(ctx, off)
+    gbc.segmented_sort(ctx, kb, ob, vb)
+    ek, ev = orc.std_segmented_sort(keys, off, vals if with_values else None)
+    assert np.array_equal(kb.to_host().view(np.uint8), ek.view(np.uint8))
+    if with_values:
+        assert np.array_equal(vb.to_host(), ev)
+
+
+def test_segmented_sort_out_of_place_descending(ctx, gbc, orc):
+    off = orc.lognormal_segments(2000, 128, 2.0, 1, 1 << 16, seed=8)
+    n = int(off[-1])
+    rng = np.random.default_rng(9)
+    keys = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32) & np.uint32(0xFFFF)
+    vals = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    kin, vin = gbc.DeviceBuffer.from_host(ctx, keys), gbc.DeviceBuffer.from_host(ctx, vals)
+    kout, vout = gbc.DeviceBuffer(ctx, n, np.uint32), gbc.DeviceBuffer(ctx, n, np.uint32)
+    ob = gbc.DeviceBuffer.from_host(ctx, off)
+    gbc.segmented_sort_raw(ctx, kin.device_pointer, kout.device_pointer, np.uint32, n, ob.device_pointer,
+                           off.size - 1, vin.device_pointer, vout.device_pointer, descending=True)
+    ek, ev = orc.std_segmented_sort(keys, off, vals, descending=True)
+    assert np.array_equal(kout.to_host(), ek) and np.array_equal(vout.to_host(), ev)
+    assert np.array_equal(kin.to_host(), keys)
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.uint32])
+@pytest.mark.parametrize("exclusive", [False, True])
+@pytest.mark.parametrize("opname", ["plus", "maximum", "right"])
+def test_segmented_scan(ctx, gbc, orc, dtype, exclusive, opname):
+    off = orc.lognormal_segments(5000, 64, 2.0, 0, 1 << 15, seed=3)
+    n = int(off[-1])
+    rng = np.random.default_rng(6)
+    x = rng.integers(-1000, 1001, size=n, dtype=np.int64).astype(dtype)
+    if opname == "plus":
+        op, code, ident = gbc.ops.plus(), orc.OP_PLUS, 0
+    elif opname == "maximum":
+        op, code, ident = gbc.ops.maximum(dtype), orc.OP_MAX, np.iinfo(dtype).min
+    else:
+        op, code, ident = gbc.binary_op("b", "0"), orc.OP_RIGHT, 0
+    xb, yb, ob = gbc.DeviceBuffer.from_host(ctx, x), gbc.DeviceBuffer(ctx, n, dtype), gbc.DeviceBuffer.from_host(ctx, off)
+    gbc.segmented_scan(ctx, xb, yb, ob, op, exclusive)
+    assert np.array_equal(yb.to_host(), orc.std_segmented_scan(x, off, code, ident, exclusive))
+
+
+def test_graph_capture_replays_segmented_sort_and_scan(ctx, gbc, orc):
+    off = orc.lognormal_segments(4000, 256, 2.0, 1, 1 << 17, seed=12)
+    n = int(off[-1])
+    rng = np.random.default_rng(13)
+    keys = rng.integers(0, 2**64, size=n, dtype=np.uint64)
+    vals = np.arange(n, dtype=np.uint32)
+    x = rng.integers(-1000, 1001, size=n, dtype=np.int64).astype(np.int32)
+    kin, vin = gbc.DeviceBuffer.from_host(ctx, keys), gbc.DeviceBuffer.from_host(ctx, vals)
+    kout, vout = gbc.DeviceBuffer(ctx, n, np.uint64), gbc.DeviceBuffer(ctx, n, np.uint32)
+    xb, yb = gbc.DeviceBuffer.from_host(ctx, x), gbc.DeviceBuffer(ctx, n, np.int32)
+    ob = gbc.DeviceBuffer.from_host(ctx, off)
+
+    def batch():
+        gbc.segmented_sort_raw(ctx, kin.device_pointer, kout.device_pointer, np.uint64, n, ob.device_pointer,
+                               off.size - 1, vin.device_pointer, vout.device_pointer)
+        gbc.segmented_scan_raw(ctx, xb.device_pointer, yb.device_pointer, n, np.int32, ob.device_pointer,
+                               off.size - 1, exclusive=True)
+
+    batch()  # warms the pool: capture needs every temporary cached
+    ctx.finish()
+    g = gbc.capture(ctx, batch)
+    ek, ev = orc.std_segmented_sort(keys, off, vals)
+    ey = orc.std_segmented_scan(x, off, orc.OP_PLUS, 0, True)
+    for _ in range(2):
+        gbc.fill(ctx, kout, 0)
+        gbc.fill(ctx, yb, 0)
+        g.launch()
+        assert np.array_equal(kout.to_host(), ek)
+        assert np.array_equal(vout.to_host(), ev)
+        assert np.array_equal(yb.to_host(), ey)
+    g.release()
+    # the plain sort is graph-capturable too
+    k2 = gbc.DeviceBuffer.from_host(ctx, keys[:100000].astype(np.uint64))
+    k2o = gbc.DeviceBuffer(ctx, 100000, np.uint64)
+    f = lambda: gbc.sort_raw(ctx, k2.device_pointer, k2o.device_pointer, np.uint64, 100000)
+    f()
+    ctx.finish()
+    g2 = gbc.capture(ctx, f)
+    for _ in range(2):
+        g2.launch()
+        assert np.array_equal(k2o.to_host(), np.sort(keys[:100000]))
+    g2.release()

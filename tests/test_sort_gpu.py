@@ -177,3 +177,35 @@ def test_repeated_calls_and_memory_reuse(ctx, gbc, orc):
     s = ctx.memory_stats()
     assert s.current_allocations == 0
     assert s.total_allocations > before
+
+
+@pytest.mark.parametrize("key_dtype", [np.uint32, np.uint64])
+@pytest.mark.parametrize("with_values", [False, True])
+def test_every_compiled_variant(ctx, gbc, orc, key_dtype, with_values):
+    # Each launch shape the tuning table can select (plain loads, bulk-copy
+    # staging, match or ballot ranking) sorts identically, including partial
+    # last tiles and arrays whose address rules out bulk copies.
+    kb_ = np.dtype(key_dtype).itemsize
+    rng = np.random.default_rng(21)
+    for n in (1, 3, 4096, 4097, 12288 * 3 + 5, 200003):
+        raw = rng.integers(0, 2**63, size=n, dtype=np.uint64).astype(key_dtype)
+        raw[::11] = raw[0]
+        vals = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+        ek, ev = orc.std_sort(raw, vals if with_values else None)
+        key = gbc.tuning_sort_key(kb_, with_values, n)
+        try:
+            for var in range(gbc.tuning_sort_variants(kb_, with_values)):
+                ctx.tuning_set(key, var)
+                for shift in (0, 1):  # element offset 1: not 16-byte aligned
+                    kin = gbc.DeviceBuffer.from_host(ctx, np.concatenate([raw[:shift], raw]))
+                    vin = gbc.DeviceBuffer.from_host(ctx, np.concatenate([vals[:shift], vals]))
+                    kout = gbc.DeviceBuffer(ctx, n + shift, key_dtype)
+                    vout = gbc.DeviceBuffer(ctx, n + shift, np.uint32)
+                    kp = lambda b: b.device_pointer + shift * b.dtype.itemsize
+                    gbc.sort_raw(ctx, kp(kin), kp(kout), key_dtype, n, kp(vin) if with_values else 0,
+                                 kp(vout) if with_values else 0)
+                    assert np.array_equal(kout.to_host()[shift:], ek), (var, n, shift)
+                    if with_values:
+                        assert np.array_equal(vout.to_host()[shift:], ev), (var, n, shift)
+        finally:
+            ctx.tuning_set(key, 0)

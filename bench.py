@@ -372,6 +372,29 @@ def main() -> None:
         dist.destroy_process_group()
 
 
+def learned_mixture_keys(torch, n: int, seed: int):
+    """The learned-CDF configuration's float32 keys, generated on the device:
+    75% from 8 Gaussians (means uniform in [-1e3, 1e3], sigmas log-uniform in
+    [1e-2, 1e2]), 20% lognormal(0, 2), 5% exact copies of 1,000 values drawn
+    from the preceding keys; shuffled."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    n75, n20 = int(0.75 * n), int(0.20 * n)
+    n5 = n - n75 - n20
+    means = torch.rand(8, device="cuda", generator=g, dtype=torch.float64) * 2e3 - 1e3
+    sig = torch.exp(torch.rand(8, device="cuda", generator=g, dtype=torch.float64) * (2 * 4.605170185988091) -
+                    4.605170185988091)
+    comp = torch.randint(0, 8, (n75,), device="cuda", generator=g)
+    a = (means[comp] + sig[comp] * torch.randn(n75, device="cuda", generator=g, dtype=torch.float64)).float()
+    b = torch.exp(2.0 * torch.randn(n20, device="cuda", generator=g))
+    pool = torch.cat([a[:500], b[:500]])
+    c = pool[torch.randint(0, 1000, (n5,), device="cuda", generator=g)]
+    keys = torch.cat([a, b, c])
+    del a, b, c, comp
+    perm = torch.randperm(n, device="cuda", generator=g)
+    return keys[perm].contiguous()
+
+
 def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, warmup) -> dict:
     """The other configuration workloads, each timed the same way."""
     out = {}
@@ -433,6 +456,84 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                      ("reduce.",))
     entry("reduce_i32_n2^30", m, "Gelem/s", ms, 4 * m, True, prof, {"note": "includes the blocking result read"})
     del x
+
+    # learned-CDF sort of the 2^28-key float mixture vs the plain sort of the same keys
+    torch.cuda.empty_cache()
+    lk = learned_mixture_keys(torch, n, 5)
+    lout = torch.empty_like(lk)
+    pout = torch.empty_like(lk)
+    ms_plain, prof_p = timed(lambda: gbc.sort_raw(ctx, lk.data_ptr(), pout.data_ptr(), np.float32, n), steps, warmup,
+                             ("sort.",))
+    stats = []
+    ms_learn, prof_l = timed(lambda: stats.append(gbc.sort_learned(ctx, lk.data_ptr(), lout.data_ptr(), np.float32, n)),
+                             steps, warmup, ("learned.", "segsort.", "sort."))
+    ok = bool(torch.equal(lout, pout))
+    st = stats[-1].as_dict() if stats else {}
+    entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 20 * n, ok, prof_l,
+          {"plain_sort_ms": ms_plain, "plain_sort_gkeys": n / (ms_plain * 1e-3) / 1e9,
+           "speedup_vs_plain": ms_plain / ms_learn, "stats": st,
+           "note": "includes sampling, the sample sort and the MLP fit; bytes = 20n (count, scatter, finish)"})
+    del lk, lout, pout
+    torch.cuda.empty_cache()
+
+    # batched segmented sort: 200,000 lognormal segments (median 256, sigma 2,
+    # clipped to [1, 2^20]) of u64 keys + u32 values, plus the segmented
+    # exclusive scan of int32 over the same offsets, one CUDA graph
+    rng = np.random.default_rng(4)
+    lens = np.clip(np.rint(rng.lognormal(np.log(256), 2.0, 200000)), 1, 1 << 20).astype(np.int64)
+    offs = np.zeros(lens.size + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    total = int(offs[-1])
+    off_d = torch.from_numpy(offs.astype(np.int32)).cuda()
+    g4 = torch.Generator(device="cuda")
+    g4.manual_seed(4)
+    sk = torch.randint(-2**63, 2**63 - 1, (total,), dtype=torch.int64, device="cuda", generator=g4)
+    seg_start = torch.repeat_interleave(off_d[:-1].long(), torch.from_numpy(lens).cuda())
+    sv = (torch.arange(total, device="cuda") - seg_start).to(torch.int32)  # index within segment
+    del seg_start
+    sko, svo = torch.empty_like(sk), torch.empty_like(sv)
+    sx = torch.randint(-1000, 1001, (total,), dtype=torch.int32, device="cuda", generator=g4)
+    sy = torch.empty_like(sx)
+
+    def batch():
+        gbc.segmented_sort_raw(ctx, sk.data_ptr(), sko.data_ptr(), np.uint64, total, off_d.data_ptr(), lens.size,
+                               sv.data_ptr(), svo.data_ptr())
+        gbc.segmented_scan_raw(ctx, sx.data_ptr(), sy.data_ptr(), total, np.int32, off_d.data_ptr(), lens.size,
+                               exclusive=True)
+
+    batch()
+    ctx.finish()
+    graph = gbc.capture(ctx, batch)
+    ms_seg, prof_s = timed(graph.launch, steps, warmup, ("segsort.", "segscan.", "sort."))
+    # the plain per-array method: the plain sort called once per segment, timed on a bounded sample
+    sample_segs = 2000
+    ms_per_array_sample, _ = timed(lambda: [gbc.sort_raw(ctx, sk.data_ptr() + 8 * int(offs[i]),
+                                                         sko.data_ptr() + 8 * int(offs[i]), np.uint64, int(lens[i]),
+                                                         sv.data_ptr() + 4 * int(offs[i]),
+                                                         svo.data_ptr() + 4 * int(offs[i]))
+                                            for i in range(sample_segs)], 1, 1, ("sort.",))
+    per_array_est_ms = ms_per_array_sample * lens.size / sample_segs
+    graph.launch()
+    ctx.finish()
+    # parity: each segment sorted stably (torch's stable sort on (segment, key) as the independent check)
+    seg_id = torch.repeat_interleave(torch.arange(lens.size, device="cuda"), torch.from_numpy(lens).cuda())
+    ku = sk.view(torch.int64) ^ (-2**63)  # unsigned order as signed
+    order = torch.sort(ku, stable=True).indices
+    order = order[torch.sort(seg_id[order], stable=True).indices]
+    ok = bool(torch.equal(sko, sk[order])) and bool(torch.equal(svo, sv[order]))
+    csum = torch.cumsum(sx.to(torch.int64), 0)
+    base = torch.repeat_interleave(torch.cat([torch.zeros(1, device="cuda", dtype=torch.int64), csum[off_d[1:-1].long() - 1]]),
+                                   torch.from_numpy(lens).cuda())
+    ok = ok and bool(torch.equal(sy.to(torch.int64), csum - sx.to(torch.int64) - base))
+    graph.release()
+    entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, 32 * total, ok, prof_s,
+          {"segments": int(lens.size), "total_keys": total, "graph": True,
+           "includes": "segmented sort (u64 keys + u32 values) and segmented exclusive int32 scan",
+           "plain_per_array_estimate_ms": per_array_est_ms,
+           "speedup_vs_per_array": per_array_est_ms / ms_seg,
+           "note": "bytes: 24 B/pair (one read + one write) + 8 B/elem scan; large segments move more"})
+    del sk, sv, sko, svo, sx, sy, seg_id, order, csum, base
+    torch.cuda.empty_cache()
 
     # 256-bin histogram of 2^30 uniform bytes
     u8 = torch.randint(0, 256, (m,), dtype=torch.uint8, device="cuda", generator=gen)

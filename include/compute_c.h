@@ -209,6 +209,89 @@ GBC_EXPORT clc_status clc_scan_ex(clc_context ctx, clc_buffer in, clc_buffer out
 GBC_EXPORT clc_status clc_sort_ex(clc_context ctx, clc_buffer keys, clc_type key_type,
                                   clc_buffer values, size_t n, int descending);
 
+/* Batched segmented sort: every segment [offsets[i], offsets[i+1]) of the
+ * keys (and values) is sorted independently and stably, all segments in one
+ * call. offsets holds num_segments + 1 monotone uint32 entries in device
+ * memory. Keys: I32, U32, F32, I64, U64, F64; values: 32-bit or NULL. The
+ * launch sequence does not depend on the data (small, medium and large
+ * segments are told apart on the device), so the call can be captured with
+ * clc_graph_begin/end once it has run (the pool must be warm). */
+GBC_EXPORT clc_status clc_segmented_sort(clc_context ctx, clc_buffer keys, clc_type key_type, clc_buffer values,
+                                         size_t n, clc_buffer offsets, size_t num_segments, int descending);
+GBC_EXPORT clc_status clc_segmented_sort_raw(clc_context ctx, const void* keys_in, void* keys_out,
+                                             clc_type key_type, const uint32_t* vals_in, uint32_t* vals_out,
+                                             size_t n, const uint32_t* offsets, size_t num_segments,
+                                             int descending);
+/* Scan restarted at every segment start (position 0 always starts one);
+ * exclusive: each segment's first output is the identity. */
+GBC_EXPORT clc_status clc_segmented_scan(clc_context ctx, clc_buffer in, clc_buffer out, size_t n, clc_type type,
+                                         const char* op, const char* identity, int exclusive, clc_buffer offsets,
+                                         size_t num_segments);
+GBC_EXPORT clc_status clc_segmented_scan_raw(clc_context ctx, const void* in, void* out, size_t n, clc_type type,
+                                             const char* op, const char* identity, int exclusive,
+                                             const uint32_t* offsets, size_t num_segments);
+
+/* Learned-CDF sort of 32-bit keys (U32, I32, F32), out of place (keys_in is
+ * left unchanged): a monotone 1 -> 32 -> 32 -> 1 fp32 network is fitted on the
+ * GPU to a sample of the keys (fitting time is part of the call), its CDF
+ * partitions the keys into buckets in one pass, the segmented sort finishes
+ * the buckets, and a monotonicity check falls back to the plain radix sort.
+ * The output is bit-identical to clc_sort's. Blocks once (to read its
+ * statistics). options and stats may be NULL. */
+typedef struct clc_learned_options {
+    int sample;   /* sampled keys (0: 2^20) */
+    int points;   /* training points from the sorted sample (0: 8192) */
+    int buckets;  /* partition buckets (0: 32768) */
+    int grid;     /* CDF table segments (0: 8192) */
+    int steps;    /* Adam steps (-1: 64) */
+    float lr;     /* Adam learning rate (0: 0.02) */
+    int use_model;               /* 0: bucket by the normalised key alone (no network) */
+    const float* params_in;      /* host, clc_learned_param_count() floats, or NULL */
+    float* params_out;           /* host, receives the fitted parameters, or NULL */
+    const float* table_in;       /* host, replaces the CDF table (grid + 1 floats), or NULL */
+    float model_weight;          /* alpha in [0, 1]: table = alpha * network + (1 - alpha) * key (0.5) */
+} clc_learned_options;
+typedef struct clc_learned_stats {
+    unsigned buckets, nonempty_buckets, largest_bucket;
+    unsigned oversized_buckets, oversized_keys; /* buckets beyond one CTA's shared-memory sort */
+    unsigned violation;                         /* bucket order was not monotone */
+    unsigned fallback;                          /* the plain radix sort produced the output */
+    float first_loss, last_loss;                /* training loss at the first and last step */
+} clc_learned_stats;
+GBC_EXPORT void clc_learned_default_options(clc_learned_options* options);
+GBC_EXPORT clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                       size_t n, const clc_learned_options* options, clc_learned_stats* stats);
+/* One forward/backward pass of the network on the GPU over m points (host
+ * arrays): gradient of the mean squared error with respect to the raw
+ * parameters (weights are stored as v with w = v * v). */
+GBC_EXPORT int clc_learned_param_count(void);
+GBC_EXPORT clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const float* xs,
+                                                const float* ys, size_t m, float* grad, float* loss);
+
+/* reduce_by_key over grouped keys (equal keys adjacent, e.g. after a sort):
+ * for run r, keys_out[r] is its key, sums_out[r] the sum of its uint32 values
+ * as uint64 and counts_out[r] (if not NULL) its length. hist16 (NULL or 65,536
+ * uint32 bins, zeroed by the call) counts the low 16 bits of every key.
+ * Keys: any 4- or 8-byte type (equality of bit patterns). *num_runs (if not
+ * NULL) receives the number of runs and makes the call blocking; otherwise it
+ * is asynchronous. All pointers are device pointers except num_runs. */
+GBC_EXPORT clc_status clc_reduce_by_key_raw(clc_context ctx, const void* keys, clc_type key_type,
+                                            const uint32_t* values, size_t n, void* keys_out,
+                                            unsigned long long* sums_out, uint32_t* counts_out, uint32_t* hist16,
+                                            size_t* num_runs);
+
+/* CUDA graphs: calls made on ctx between clc_graph_begin and clc_graph_end
+ * are captured (not run) into a graph that clc_graph_launch replays on the
+ * context's stream. Every call captured must have run once before on the same
+ * context with the same sizes, so that its temporaries come from the pool;
+ * a call that would allocate during capture fails with CLC_ERROR_UNSUPPORTED.
+ * Blocking calls (reads, reduce, finish) cannot be captured. */
+typedef struct clc_graph_s* clc_graph;
+GBC_EXPORT clc_status clc_graph_begin(clc_context ctx);
+GBC_EXPORT clc_status clc_graph_end(clc_context ctx, clc_graph* out);
+GBC_EXPORT clc_status clc_graph_launch(clc_context ctx, clc_graph graph);
+GBC_EXPORT void clc_graph_release(clc_graph graph);
+
 /* Device pointer of a buffer (NULL for a zero-byte buffer). */
 GBC_EXPORT void* clc_buffer_device_pointer(clc_buffer buffer);
 /* Wraps existing device memory of the context's device as a buffer that does

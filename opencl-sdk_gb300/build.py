@@ -28,6 +28,10 @@ SOURCES = [
     "scan.cu",
     "reduce.cu",
     "histogram.cu",
+    "segmented.cu",
+    "segscan.cu",
+    "learned.cu",
+    "reduce_by_key.cu",
 ]
 
 COMMON = [

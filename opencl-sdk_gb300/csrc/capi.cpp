@@ -25,7 +25,9 @@
 #include <new>
 #include <string>
 
+#include "learned.hpp"
 #include "runtime.hpp"
+#include "segmented.hpp"
 #include "sort_internal.hpp"
 
 struct clc_context_s {
@@ -41,6 +43,12 @@ struct clc_buffer_s {
 
 struct clc_kernel_s {
     int unused;
+};
+
+struct clc_graph_s {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    int device;
 };
 
 namespace {
@@ -661,6 +669,194 @@ clc_status clc_histogram_even_raw(clc_context ctx, const void* in, size_t n, clc
         require(bins == 0 || hist != nullptr, "clc: null histogram");
         gbc::histogram_even(*ctx->ctx, in, n, elem_of(type), hist, bins, lower, upper);
     });
+}
+
+// ---- batched / segmented --------------------------------------------------
+
+clc_status clc_segmented_sort_raw(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                  const uint32_t* vals_in, uint32_t* vals_out, size_t n, const uint32_t* offsets,
+                                  size_t num_segments, int descending)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        int bytes, kind;
+        key_kind_of(key_type, bytes, kind);
+        gbc::seg_options opt;
+        gbc::launch_shape shape;
+        if (ctx->ctx->tuning.lookup(gbc::segsort_tuning_key(bytes, vals_in != nullptr, n, num_segments), shape))
+            opt.cta_cap = shape.variant;
+        gbc::segmented_sort(*ctx->ctx, keys_in, keys_out, bytes, kind, vals_in, vals_out, n, offsets,
+                            num_segments, descending != 0, opt);
+    });
+}
+
+clc_status clc_segmented_sort(clc_context ctx, clc_buffer keys, clc_type key_type, clc_buffer values, size_t n,
+                              clc_buffer offsets, size_t num_segments, int descending)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        require_fits(keys, n, key_type);
+        if (values != nullptr) require_fits(values, n, CLC_TYPE_U32);
+        if (num_segments > 0) require_fits(offsets, num_segments + 1, CLC_TYPE_U32);
+        uint32_t* v = values != nullptr ? static_cast<uint32_t*>(values->ptr) : nullptr;
+        const clc_status s =
+            clc_segmented_sort_raw(ctx, keys->ptr, keys->ptr, key_type, v, v, n,
+                                   num_segments > 0 ? static_cast<const uint32_t*>(offsets->ptr) : nullptr,
+                                   num_segments, descending);
+        if (s != CLC_SUCCESS) throw std::runtime_error(last_error);
+    });
+}
+
+clc_status clc_segmented_scan_raw(clc_context ctx, const void* in, void* out, size_t n, clc_type type,
+                                  const char* op, const char* identity, int exclusive, const uint32_t* offsets,
+                                  size_t num_segments)
+{
+    return guarded([&] {
+        require(ctx != nullptr && op != nullptr && identity != nullptr, "clc: null argument");
+        const gbc::op_kind k = parse_op(op);
+        unsigned char id[8];
+        parse_identity(identity, type, id);
+        gbc::segmented_scan(*ctx->ctx, in, out, n, elem_of(type), k, id, exclusive != 0, offsets, num_segments);
+    });
+}
+
+clc_status clc_segmented_scan(clc_context ctx, clc_buffer in, clc_buffer out, size_t n, clc_type type,
+                              const char* op, const char* identity, int exclusive, clc_buffer offsets,
+                              size_t num_segments)
+{
+    return guarded([&] {
+        require(ctx != nullptr && op != nullptr && identity != nullptr, "clc: null argument");
+        require_fits(in, n, type);
+        require_fits(out, n, type);
+        if (num_segments > 0) require_fits(offsets, num_segments + 1, CLC_TYPE_U32);
+        const gbc::op_kind k = parse_op(op);
+        unsigned char id[8];
+        parse_identity(identity, type, id);
+        gbc::segmented_scan(*ctx->ctx, in->ptr, out->ptr, n, elem_of(type), k, id, exclusive != 0,
+                            num_segments > 0 ? static_cast<const uint32_t*>(offsets->ptr) : nullptr, num_segments);
+    });
+}
+
+clc_status clc_reduce_by_key_raw(clc_context ctx, const void* keys, clc_type key_type, const uint32_t* values,
+                                 size_t n, void* keys_out, unsigned long long* sums_out, uint32_t* counts_out,
+                                 uint32_t* hist16, size_t* num_runs)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        const std::size_t kb = gbc::elem_size(elem_of(key_type));
+        require(kb == 4 || kb == 8, "clc_reduce_by_key: keys must be 4 or 8 bytes");
+        auto& c = *ctx->ctx;
+        uint32_t* dcount = num_runs != nullptr ? reinterpret_cast<uint32_t*>(c.d_small + 1024) : nullptr;
+        gbc::reduce_by_key(c, keys, (int)kb, values, n, keys_out, sums_out, counts_out, hist16, dcount);
+        if (num_runs != nullptr) {
+            gbc::check_cuda(cudaMemcpyAsync(c.pinned, dcount, 4, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync");
+            c.finish();
+            uint32_t r;
+            std::memcpy(&r, c.pinned, 4);
+            *num_runs = r;
+        }
+    });
+}
+
+// ---- learned-CDF sort -------------------------------------------------------
+
+void clc_learned_default_options(clc_learned_options* o)
+{
+    if (o == nullptr) return;
+    *o = clc_learned_options{0, 0, 0, 0, -1, 0.f, 1, nullptr, nullptr, nullptr, 0.5f};
+}
+
+int clc_learned_param_count(void) { return gbc::learned::NPARAM; }
+
+clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type, size_t n,
+                            const clc_learned_options* options, clc_learned_stats* stats)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        require(key_type == CLC_TYPE_U32 || key_type == CLC_TYPE_I32 || key_type == CLC_TYPE_F32,
+                "clc_sort_learned: keys must be U32, I32 or F32");
+        int bytes, kind;
+        key_kind_of(key_type, bytes, kind);
+        gbc::learned_options o;
+        if (options != nullptr) {
+            o.sample = options->sample;
+            o.points = options->points;
+            o.buckets = options->buckets;
+            o.grid = options->grid;
+            o.steps = options->steps;
+            o.lr = options->lr;
+            o.use_model = options->use_model != 0;
+            o.params_in = options->params_in;
+            o.params_out = options->params_out;
+            o.table_in = options->table_in;
+            o.model_weight = std::min(1.f, std::max(0.f, options->model_weight));
+        }
+        gbc::learned_stats s;
+        gbc::learned_sort(*ctx->ctx, keys_in, keys_out, kind, n, o, &s);
+        if (stats != nullptr)
+            *stats = clc_learned_stats{s.buckets, s.nonempty_buckets, s.largest_bucket, s.oversized_buckets,
+                                       s.oversized_keys, s.violation, s.fallback, s.first_loss, s.last_loss};
+    });
+}
+
+clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const float* xs, const float* ys, size_t m,
+                                     float* grad, float* loss)
+{
+    return guarded([&] {
+        require(ctx != nullptr && params != nullptr && xs != nullptr && ys != nullptr && grad != nullptr &&
+                    loss != nullptr,
+                "clc: null argument");
+        gbc::mlp_gradients(*ctx->ctx, params, xs, ys, m, grad, loss);
+    });
+}
+
+// ---- CUDA graphs ------------------------------------------------------------
+
+clc_status clc_graph_begin(clc_context ctx)
+{
+    if (ctx == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null context");
+    return guarded([&] {
+        ctx->ctx->activate();
+        gbc::check_cuda(cudaStreamBeginCapture(ctx->ctx->stream, cudaStreamCaptureModeThreadLocal),
+                        "cudaStreamBeginCapture");
+    });
+}
+
+clc_status clc_graph_end(clc_context ctx, clc_graph* out)
+{
+    if (ctx == nullptr || out == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    *out = nullptr;
+    return guarded([&] {
+        ctx->ctx->activate();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->ctx->stream, &g);
+        ctx->ctx->upstream->flush_deferred();
+        gbc::check_cuda(e, "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+        if (ei != cudaSuccess) cudaGraphDestroy(g);
+        gbc::check_cuda(ei, "cudaGraphInstantiate");
+        *out = new clc_graph_s{g, exec, ctx->ctx->device};
+    });
+}
+
+clc_status clc_graph_launch(clc_context ctx, clc_graph graph)
+{
+    if (ctx == nullptr || graph == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    return guarded([&] {
+        require(graph->device == ctx->ctx->device, "clc: graph belongs to another device");
+        ctx->ctx->activate();
+        gbc::check_cuda(cudaGraphLaunch(graph->exec, ctx->ctx->stream), "cudaGraphLaunch");
+    });
+}
+
+void clc_graph_release(clc_graph graph)
+{
+    if (graph == nullptr) return;
+    cudaSetDevice(graph->device);
+    cudaGraphExecDestroy(graph->exec);
+    cudaGraphDestroy(graph->graph);
+    delete graph;
 }
 
 // ---- buffers and context extras ------------------------------------------

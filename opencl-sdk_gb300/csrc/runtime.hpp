@@ -243,6 +243,14 @@ void reduce(device_context& ctx, const void* in, std::size_t n, elem t, op_kind 
 void histogram_even(device_context& ctx, const void* in, std::size_t n, elem t,
                     uint32_t* hist, std::size_t bins, double lower, double upper);
 
+//! Runs of equal adjacent keys (4- or 8-byte): per run its key, the uint64
+//! sum of its uint32 values and (if counts_out) its length, in run order;
+//! hist (65536 bins, or null) counts key & 0xFFFF of every key; the number of
+//! runs goes to num_runs_device (or nowhere if null). Asynchronous.
+void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const uint32_t* vals, std::size_t n,
+                   void* keys_out, unsigned long long* sums_out, uint32_t* counts_out, uint32_t* hist,
+                   uint32_t* num_runs_device);
+
 //! Launches one scan tile whose predecessor never publishes (the failure
 //! path of the bounded look-back wait); the next finish() reports it.
 void selftest_lookback_timeout(device_context& ctx);

@@ -178,7 +178,7 @@ template <typename K> __global__ void k_precopy(SortArgs<K> a)
 // counter so every look-back waits only on CTAs that are already running).
 // ---------------------------------------------------------------------------
 template <typename K, bool HAS_V, int THREADS, int ITEMS, bool MATCH>
-__global__ void __launch_bounds__(THREADS) k_pass(SortArgs<K> a, int slot)
+__device__ __forceinline__ void pass_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
@@ -373,6 +373,19 @@ __global__ void __launch_bounds__(THREADS) k_pass(SortArgs<K> a, int slot)
         }
         __syncthreads();
     }
+}
+
+// The digit pass with the compiler's default register budget, and with a
+// minimum number of resident CTAs per SM (which caps registers).
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool MATCH>
+__global__ void __launch_bounds__(THREADS) k_pass(SortArgs<K> a, int slot)
+{
+    pass_body<K, HAS_V, THREADS, ITEMS, MATCH>(a, slot);
+}
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool MATCH, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int slot)
+{
+    pass_body<K, HAS_V, THREADS, ITEMS, MATCH>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -796,6 +809,7 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_PV(K, HV, T, I, M) PassVariant<K>{T, I, M, false, &k_pass<K, HV, T, I, M>}
 #define GBC_PT(K, HV, T, I, M, B) PassVariant<K>{T, I, M, true, &k_pass_tma<K, HV, T, I, M, B>}
 #define GBC_PE(K, HV, I, B) PassVariant<K>{256, I, false, false, &k_pass_early<K, HV, 256, I, B>}
+#define GBC_PM(K, HV, T, I, B) PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
@@ -803,12 +817,12 @@ template <bool HV> struct Variants<uint32_t, HV> {
         static const PassVariant<uint32_t> v[count] = {
             GBC_PV(uint32_t, HV, 256, 16, false),
             GBC_PV(uint32_t, HV, 256, 16, true),
-            GBC_PE(uint32_t, HV, 16, 2),
-            GBC_PE(uint32_t, HV, 16, 3),
+            GBC_PM(uint32_t, HV, 256, 16, 3),
+            GBC_PM(uint32_t, HV, 256, 12, 4),
+            GBC_PM(uint32_t, HV, 256, 8, 5),
             GBC_PE(uint32_t, HV, 12, 4),
-            GBC_PE(uint32_t, HV, 24, 2),
             GBC_PT(uint32_t, HV, 512, 12, false, 1),
-            GBC_PT(uint32_t, HV, 256, 16, false, 2),
+            GBC_PM(uint32_t, HV, 256, 20, 2),
         };
         return v[std::min(std::max(i, 0), count - 1)];
     }
@@ -830,6 +844,7 @@ template <bool HV> struct Variants<uint64_t, HV> {
 #undef GBC_PV
 #undef GBC_PT
 #undef GBC_PE
+#undef GBC_PM
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {

@@ -172,6 +172,11 @@ _PROTOS = {
     "clc_segmented_sort_raw": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _vp, _sz, _i]),
     "clc_segmented_scan": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp, _sz]),
     "clc_segmented_scan_raw": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp, _sz]),
+    "clc_reduce_by_key_raw": (_i, [_vp, _vp, _i, _vp, _sz, _vp, _vp, _vp, _vp, C.POINTER(_sz)]),
+    "clc_learned_default_options": (None, [_vp]),
+    "clc_sort_learned": (_i, [_vp, _vp, _vp, _i, _sz, _vp, _vp]),
+    "clc_learned_param_count": (_i, []),
+    "clc_learned_mlp_gradients": (_i, [_vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "clc_graph_begin": (_i, [_vp]),
     "clc_graph_end": (_i, [_vp, C.POINTER(_vp)]),
     "clc_graph_launch": (_i, [_vp, _vp]),
@@ -590,3 +595,62 @@ def capture(ctx: Context, fn) -> Graph:
         status = lib.clc_graph_end(ctx.handle, C.byref(h))
     _raise_for(status)
     return Graph(ctx, h)
+
+
+# ---- learned-CDF sort ---------------------------------------------------------
+
+class LearnedOptions(C.Structure):
+    _fields_ = [("sample", C.c_int), ("points", C.c_int), ("buckets", C.c_int), ("grid", C.c_int),
+                ("steps", C.c_int), ("lr", C.c_float), ("use_model", C.c_int), ("params_in", C.c_void_p),
+                ("params_out", C.c_void_p), ("table_in", C.c_void_p), ("model_weight", C.c_float)]
+
+
+class LearnedStats(C.Structure):
+    _fields_ = [("buckets", C.c_uint), ("nonempty_buckets", C.c_uint), ("largest_bucket", C.c_uint),
+                ("oversized_buckets", C.c_uint), ("oversized_keys", C.c_uint), ("violation", C.c_uint),
+                ("fallback", C.c_uint), ("first_loss", C.c_float), ("last_loss", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+def learned_options(**kw) -> LearnedOptions:
+    o = LearnedOptions()
+    lib.clc_learned_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def sort_learned(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int,
+                 options: LearnedOptions | None = None) -> LearnedStats:
+    """Learned-CDF sort of 32-bit keys, out of place; returns its statistics."""
+    st = LearnedStats()
+    _raise_for(lib.clc_sort_learned(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype), n,
+                                    C.byref(options) if options is not None else None, C.byref(st)))
+    return st
+
+
+def learned_param_count() -> int:
+    return lib.clc_learned_param_count()
+
+
+def learned_mlp_gradients(ctx: Context, params: np.ndarray, xs: np.ndarray, ys: np.ndarray):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(xs, dtype=np.float32)
+    y = np.ascontiguousarray(ys, dtype=np.float32)
+    g = np.zeros_like(p)
+    loss = np.zeros(1, dtype=np.float32)
+    _raise_for(lib.clc_learned_mlp_gradients(ctx.handle, p.ctypes.data, x.ctypes.data, y.ctypes.data, x.size,
+                                             g.ctypes.data, loss.ctypes.data))
+    return g, float(loss[0])
+
+
+def reduce_by_key_raw(ctx: Context, keys: int, key_dtype, values: int, n: int, keys_out: int, sums_out: int,
+                      counts_out: int = 0, hist16: int = 0, want_count: bool = True):
+    """Runs of equal adjacent keys: key, uint64 sum of values, length; returns the run count (blocking) or None."""
+    runs = C.c_size_t(0)
+    _raise_for(lib.clc_reduce_by_key_raw(ctx.handle, C.c_void_p(keys), clc_type(key_dtype), C.c_void_p(values), n,
+                                         C.c_void_p(keys_out), C.c_void_p(sums_out), C.c_void_p(counts_out or None),
+                                         C.c_void_p(hist16 or None), C.byref(runs) if want_count else None))
+    return runs.value if want_count else None

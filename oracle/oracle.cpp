@@ -415,6 +415,62 @@ void orc_ref_reduce(const void* in, std::size_t n, int type, int op, const void*
 
 int orc_hardware_threads(void) { return hw_threads(0); }
 
+// ---- learned-CDF network (no reference counterpart) -----------------------
+// 1 -> H -> H -> 1, ReLU, weights stored as v with w = v * v; loss = mean of
+// (yhat - y)^2. Gradient with respect to the raw parameters, in double.
+// Layout: v1[H], b1[H], v2[H][H] (row = output unit), b2[H], v3[H], b3.
+void orc_mlp_grad(const float* params, const float* xs, const float* ys, std::size_t m, int h, float* grad,
+                  double* loss)
+{
+    const int H = h;
+    const int OV1 = 0, OB1 = H, OV2 = 2 * H, OB2 = 2 * H + H * H, OV3 = 3 * H + H * H, OB3 = 4 * H + H * H;
+    const int NP = OB3 + 1;
+    std::vector<double> w(NP), g(NP, 0.0);
+    for (int i = 0; i < NP; ++i) {
+        const bool is_w = i < OB1 || (i >= OV2 && i < OB2) || (i >= OV3 && i < OB3);
+        w[i] = is_w ? (double)params[i] * params[i] : params[i];
+    }
+    double l = 0;
+    std::vector<double> z1(H), h1(H), z2(H), h2(H), d2(H), d1(H);
+    for (std::size_t p = 0; p < m; ++p) {
+        const double x = xs[p];
+        for (int j = 0; j < H; ++j) {
+            z1[j] = w[OV1 + j] * x + w[OB1 + j];
+            h1[j] = z1[j] > 0 ? z1[j] : 0;
+        }
+        double yhat = w[OB3];
+        for (int k = 0; k < H; ++k) {
+            double z = w[OB2 + k];
+            for (int j = 0; j < H; ++j) z += w[OV2 + k * H + j] * h1[j];
+            z2[k] = z;
+            h2[k] = z > 0 ? z : 0;
+            yhat += w[OV3 + k] * h2[k];
+        }
+        const double err = yhat - ys[p];
+        l += err * err;
+        const double gy = 2 * err / (double)m;
+        g[OB3] += gy;
+        for (int k = 0; k < H; ++k) {
+            g[OV3 + k] += gy * h2[k];
+            d2[k] = z2[k] > 0 ? gy * w[OV3 + k] : 0;
+            g[OB2 + k] += d2[k];
+            for (int j = 0; j < H; ++j) g[OV2 + k * H + j] += d2[k] * h1[j];
+        }
+        for (int j = 0; j < H; ++j) {
+            double s = 0;
+            for (int k = 0; k < H; ++k) s += d2[k] * w[OV2 + k * H + j];
+            d1[j] = z1[j] > 0 ? s : 0;
+            g[OV1 + j] += d1[j] * x;
+            g[OB1 + j] += d1[j];
+        }
+    }
+    for (int i = 0; i < NP; ++i) {
+        const bool is_w = i < OB1 || (i >= OV2 && i < OB2) || (i >= OV3 && i < OB3);
+        grad[i] = (float)(is_w ? g[i] * 2.0 * params[i] : g[i]);
+    }
+    *loss = l / (double)m;
+}
+
 // ---- batched forms (no reference counterpart; std:: ground truth) ---------
 
 // Every segment [off[i], off[i+1]) sorted independently, stably.
@@ -460,3 +516,30 @@ void orc_std_segmented_scan(const void* in, void* out, std::size_t n, int type, 
 }
 
 }  // extern "C"
+
+extern "C" {
+// Runs of equal adjacent keys: key, uint64 sum of values, length; histogram of
+// the low 16 key bits (65536 bins). Returns the number of runs.
+std::size_t orc_std_reduce_by_key(const void* keys, int key_bytes, const uint32_t* vals, std::size_t n,
+                                  void* keys_out, unsigned long long* sums, uint32_t* counts, uint32_t* hist)
+{
+    auto key = [&](std::size_t i) -> uint64_t {
+        return key_bytes == 4 ? static_cast<const uint32_t*>(keys)[i] : static_cast<const uint64_t*>(keys)[i];
+    };
+    std::fill(hist, hist + 65536, 0u);
+    std::size_t r = 0;
+    for (std::size_t i = 0; i < n;) {
+        std::size_t j = i;
+        unsigned long long s = 0;
+        while (j < n && key(j) == key(i)) s += vals[j++];
+        if (key_bytes == 4) static_cast<uint32_t*>(keys_out)[r] = (uint32_t)key(i);
+        else static_cast<uint64_t*>(keys_out)[r] = key(i);
+        sums[r] = s;
+        counts[r] = (uint32_t)(j - i);
+        hist[key(i) & 0xFFFF] += (uint32_t)(j - i);
+        ++r;
+        i = j;
+    }
+    return r;
+}
+}

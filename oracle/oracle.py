@@ -62,6 +62,9 @@ def lib():
         L.orc_hardware_threads.restype = i
         L.orc_std_segmented_sort.argtypes = [vp, vp, sz, i, i, i, vp, sz, i]
         L.orc_std_segmented_scan.argtypes = [vp, vp, sz, i, i, vp, i, vp, sz]
+        L.orc_mlp_grad.argtypes = [vp, vp, vp, sz, i, vp, C.POINTER(C.c_double)]
+        L.orc_std_reduce_by_key.argtypes = [vp, i, vp, sz, vp, vp, vp, vp]
+        L.orc_std_reduce_by_key.restype = sz
         _lib = L
     return _lib
 
@@ -189,3 +192,39 @@ def lognormal_segments(num_segments: int, median: float, sigma: float, lo: int, 
     off = np.zeros(num_segments + 1, dtype=np.int64)
     np.cumsum(lens, out=off[1:])
     return off.astype(np.uint32)
+
+
+def mlp_grad(params: np.ndarray, xs: np.ndarray, ys: np.ndarray, hidden: int = 32):
+    """Gradient (raw parameters) and loss of the learned-CDF network, in double."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(xs, dtype=np.float32)
+    y = np.ascontiguousarray(ys, dtype=np.float32)
+    g = np.zeros_like(p)
+    loss = C.c_double(0)
+    lib().orc_mlp_grad(_p(p), _p(x), _p(y), x.size, hidden, _p(g), C.byref(loss))
+    return g, loss.value
+
+
+def std_reduce_by_key(keys: np.ndarray, vals: np.ndarray):
+    """(unique keys, uint64 sums, run lengths, 65536-bin histogram of key & 0xFFFF)."""
+    k = np.ascontiguousarray(keys)
+    v = np.ascontiguousarray(vals, dtype=np.uint32)
+    ko = np.empty_like(k)
+    sums = np.empty(k.size, dtype=np.uint64)
+    counts = np.empty(k.size, dtype=np.uint32)
+    hist = np.zeros(65536, dtype=np.uint32)
+    r = lib().orc_std_reduce_by_key(_p(k), k.dtype.itemsize, _p(v), k.size, _p(ko), _p(sums), _p(counts), _p(hist))
+    return ko[:r], sums[:r], counts[:r], hist
+
+
+def zipf_keys(n: int, s: float, distinct: int, seed: int) -> np.ndarray:
+    """Zipf(s) ranks over `distinct` values (inverse CDF), mapped to 64-bit keys by splitmix64 (a bijection)."""
+    rng = np.random.default_rng(seed)
+    w = 1.0 / np.arange(1, distinct + 1, dtype=np.float64) ** s
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    ranks = np.searchsorted(cdf, rng.random(n)).astype(np.uint64)
+    z = ranks + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))

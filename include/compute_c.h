@@ -233,28 +233,32 @@ GBC_EXPORT clc_status clc_segmented_scan_raw(clc_context ctx, const void* in, vo
 
 /* Learned-CDF sort of 32-bit keys (U32, I32, F32), out of place (keys_in is
  * left unchanged): a monotone 1 -> 32 -> 32 -> 1 fp32 network is fitted on the
- * GPU to a sample of the keys (fitting time is part of the call), its CDF
- * partitions the keys into buckets in one pass, the segmented sort finishes
- * the buckets, and a monotonicity check falls back to the plain radix sort.
- * The output is bit-identical to clc_sort's. Blocks once (to read its
- * statistics). options and stats may be NULL. */
+ * GPU to a sample of the keys (fitting time is part of the call) and compiled
+ * into bucket splitters; one counting pass and one scatter pass partition the
+ * keys into the buckets, the segmented sort finishes them, and a boundary
+ * check proves the result ordered. A model that would leave more than half of
+ * the keys in buckets too large for one CTA's shared-memory sort (judged on
+ * the sample, before the partition), or a failed check, sends the input to
+ * the plain radix sort. The output is bit-identical to clc_sort's. Blocks
+ * twice (to read the estimate and the statistics). options and stats may be
+ * NULL. */
 typedef struct clc_learned_options {
     int sample;   /* sampled keys (0: 2^20) */
     int points;   /* training points from the sorted sample (0: 8192) */
-    int buckets;  /* partition buckets (0: 32768) */
-    int grid;     /* CDF table segments (0: 8192) */
-    int steps;    /* Adam steps (-1: 64) */
-    float lr;     /* Adam learning rate (0: 0.02) */
-    int use_model;               /* 0: bucket by the normalised key alone (no network) */
-    const float* params_in;      /* host, clc_learned_param_count() floats, or NULL */
-    float* params_out;           /* host, receives the fitted parameters, or NULL */
-    const float* table_in;       /* host, replaces the CDF table (grid + 1 floats), or NULL */
-    float model_weight;          /* alpha in [0, 1]: table = alpha * network + (1 - alpha) * key (0.5) */
+    int buckets;  /* partition buckets (0: about n / 8192, at least 4096, as many as shared memory holds) */
+    int steps;    /* Adam steps (-1: 32) */
+    float lr;     /* Adam learning rate (0: 0.05) */
+    int use_model;                 /* 0: equal-width buckets over the sampled key range (no network) */
+    const float* params_in;        /* host, clc_learned_param_count() floats, or NULL (data-driven init) */
+    float* params_out;             /* host, receives the fitted parameters, or NULL */
+    const unsigned* splitters_in;  /* host, buckets - 1 order-preserving keys replacing the compiled ones, or NULL */
 } clc_learned_options;
 typedef struct clc_learned_stats {
     unsigned buckets, nonempty_buckets, largest_bucket;
     unsigned oversized_buckets, oversized_keys; /* buckets beyond one CTA's shared-memory sort */
-    unsigned violation;                         /* bucket order was not monotone */
+    unsigned constant_keys;                     /* keys in oversized buckets holding one key value */
+    unsigned estimated_oversized_keys;          /* the same, predicted from the sample */
+    unsigned violation;                         /* the boundary check failed */
     unsigned fallback;                          /* the plain radix sort produced the output */
     float first_loss, last_loss;                /* training loss at the first and last step */
 } clc_learned_stats;
@@ -262,11 +266,14 @@ GBC_EXPORT void clc_learned_default_options(clc_learned_options* options);
 GBC_EXPORT clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
                                        size_t n, const clc_learned_options* options, clc_learned_stats* stats);
 /* One forward/backward pass of the network on the GPU over m points (host
- * arrays): gradient of the mean squared error with respect to the raw
- * parameters (weights are stored as v with w = v * v). */
+ * arrays): keys in the order-preserving 32-bit domain and target CDF values;
+ * the first layer sees (key - centres[j]) * inv_span. Returns the gradient of
+ * the mean squared error with respect to the raw parameters (weights are
+ * stored as v with w = exp(v)) and the loss. */
 GBC_EXPORT int clc_learned_param_count(void);
-GBC_EXPORT clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const float* xs,
-                                                const float* ys, size_t m, float* grad, float* loss);
+GBC_EXPORT clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const unsigned* centres,
+                                                float inv_span, const unsigned* keys, const float* ys, size_t m,
+                                                float* grad, float* loss);
 
 /* reduce_by_key over grouped keys (equal keys adjacent, e.g. after a sort):
  * for run r, keys_out[r] is its key, sums_out[r] the sum of its uint32 values

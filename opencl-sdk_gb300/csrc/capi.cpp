@@ -763,7 +763,7 @@ clc_status clc_reduce_by_key_raw(clc_context ctx, const void* keys, clc_type key
 void clc_learned_default_options(clc_learned_options* o)
 {
     if (o == nullptr) return;
-    *o = clc_learned_options{0, 0, 0, 0, -1, 0.f, 1, nullptr, nullptr, nullptr, 0.5f};
+    *o = clc_learned_options{0, 0, 0, -1, 0.f, 1, nullptr, nullptr, nullptr};
 }
 
 int clc_learned_param_count(void) { return gbc::learned::NPARAM; }
@@ -782,31 +782,31 @@ clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out
             o.sample = options->sample;
             o.points = options->points;
             o.buckets = options->buckets;
-            o.grid = options->grid;
             o.steps = options->steps;
             o.lr = options->lr;
             o.use_model = options->use_model != 0;
             o.params_in = options->params_in;
             o.params_out = options->params_out;
-            o.table_in = options->table_in;
-            o.model_weight = std::min(1.f, std::max(0.f, options->model_weight));
+            o.splitters_in = options->splitters_in;
         }
         gbc::learned_stats s;
         gbc::learned_sort(*ctx->ctx, keys_in, keys_out, kind, n, o, &s);
         if (stats != nullptr)
-            *stats = clc_learned_stats{s.buckets, s.nonempty_buckets, s.largest_bucket, s.oversized_buckets,
-                                       s.oversized_keys, s.violation, s.fallback, s.first_loss, s.last_loss};
+            *stats = clc_learned_stats{s.buckets,       s.nonempty_buckets,         s.largest_bucket,
+                                       s.oversized_buckets, s.oversized_keys,      s.constant_keys,
+                                       s.estimated_oversized_keys, s.violation,    s.fallback,
+                                       s.first_loss,    s.last_loss};
     });
 }
 
-clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const float* xs, const float* ys, size_t m,
-                                     float* grad, float* loss)
+clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const unsigned* centres, float inv_span,
+                                     const unsigned* keys, const float* ys, size_t m, float* grad, float* loss)
 {
     return guarded([&] {
-        require(ctx != nullptr && params != nullptr && xs != nullptr && ys != nullptr && grad != nullptr &&
-                    loss != nullptr,
+        require(ctx != nullptr && params != nullptr && centres != nullptr && keys != nullptr && ys != nullptr &&
+                    grad != nullptr && loss != nullptr,
                 "clc: null argument");
-        gbc::mlp_gradients(*ctx->ctx, params, xs, ys, m, grad, loss);
+        gbc::mlp_gradients(*ctx->ctx, params, centres, inv_span, keys, ys, m, grad, loss);
     });
 }
 

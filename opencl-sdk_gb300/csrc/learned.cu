@@ -1,28 +1,44 @@
 // Learned-CDF sort: a small monotone MLP fitted on the GPU to a sample of the
-// keys predicts each key's CDF and scatters the keys into buckets in one pass;
-// the buckets are then finished by the segmented sort (shared-memory sorts,
-// with oversized buckets routed to its batched onesweep radix sort), and any
+// keys models their CDF; the model is compiled into bucket splitters, the keys
+// are partitioned into the buckets in one counting pass and one scatter pass,
+// the buckets are finished by the segmented sort (shared-memory sorts, with
+// oversized buckets routed to its batched onesweep radix sort), and any
 // monotonicity violation sends the whole input to the plain radix sort.
 //
 // No reference counterpart. The output is the plain radix sort's output bit
-// for bit (the reference's key order, Algorithm.cpp:459-469): bucket order is a
-// monotone function of the key, each bucket is sorted exactly, and the check
-// proves the concatenation ordered.
+// for bit (the reference's key order, Algorithm.cpp:459-469): the bucket of a
+// key is a monotone function of the key, each bucket is sorted exactly, and
+// the boundary check proves the concatenation ordered.
+//
+// The network, 1 -> H -> H -> 1 on a key u in the order-preserving 32-bit
+// domain:
+//   d_j  = (float)(u - c_j) * inv_span          (the difference is exact)
+//   h1_j = clamp(w1_j * d_j + b1_j, 0, 1)
+//   h2_k = clamp(b2_k + sum_j w2_kj * h1_j, 0, 1)
+//   F(u) = b3 + sum_k w3_k * h2_k
+// with every weight w = exp(v) > 0, so F is non-decreasing in u by
+// construction (round-to-nearest float arithmetic is monotone too). The
+// centres c_j sit at the sample quantiles (j + 1/2) / H, so the first layer
+// resolves clusters far narrower than float precision over the whole key
+// range; clamp rather than ReLU keeps F from being convex, so it can follow
+// a multi-modal CDF.
 //
 // Steps (all on the context's stream):
-//   1. sample S keys at a fixed stride, in the order-preserving u32 form, and
-//      sort the sample with the plain radix sort;
-//   2. training points: x = the normalised key of sample quantile i/M,
-//      y = (i + 0.5) / M;
-//   3. fit 1 -> H -> H -> 1 (ReLU, weights w = v^2 >= 0, so the network is
-//      monotone non-decreasing by construction) with full-batch Adam, one
-//      kernel launch per step: each CTA runs forward and backward for its
-//      points, the last CTA to finish sums the partial gradients and updates;
-//   4. compile: evaluate alpha * network(x) + (1 - alpha) * x on a GRID + 1
-//      point table; a key's bucket is floor(B * interp(table, x(key))),
-//      monotone in the key;
-//   5. count keys per (CTA chunk, bucket), exclusive offsets bucket-major,
-//      scatter (shared-memory cursors per bucket);
+//   1. sample S keys at a fixed stride (order-preserving form) and sort them
+//      with the plain radix sort;
+//   2. frame (key range, centres), data-driven initial parameters (the ramps
+//      of layer 1 span consecutive sample quantiles, layer 2 ~ identity, so
+//      the initial F interpolates the sample CDF) and M training points
+//      (x = sample quantile i/M, y = (i + 1/2)/M);
+//   3. full-batch Adam on the mean squared error, all steps in one
+//      cooperative launch: every CTA runs forward and backward for its
+//      points, writes its gradient sums, and after one grid barrier every CTA
+//      sums all partial gradients in the same order and applies the same
+//      update to its own copy of the parameters;
+//   4. splitters: s_b = min{u : F(u) >= b / B} by bisection over the key
+//      domain, b = 1 .. B-1; a lookup table over the top bits of (u - umin)
+//      narrows each key's search to the splitters inside its cell;
+//   5. count keys per (CTA chunk, bucket), exclusive offsets, scatter;
 //   6. segmented sort of the B buckets; 7. boundary check; fallback if needed.
 #include <algorithm>
 #include <cmath>
@@ -42,10 +58,18 @@ constexpr int OFF_V1 = 0, OFF_B1 = H, OFF_V2 = 2 * H, OFF_B2 = 2 * H + H * H, OF
               OFF_B3 = 4 * H + H * H;
 static_assert(OFF_B3 + 1 == NPARAM, "parameter layout");
 
-constexpr int TRAIN_THREADS = 256;  // one training point per thread
+constexpr int TRAIN_THREADS = 256;          // one training point per thread and round
 constexpr int PSTRIDE = TRAIN_THREADS + 1;  // padded row of per-point activations
+constexpr int LUT_BITS = 12;                // splitter lookup table: 2^12 cells
+constexpr int NCELLS = 1 << LUT_BITS;
+constexpr int PART_THREADS = 1024;
 
-__device__ __forceinline__ float relu(float z) { return z > 0.f ? z : 0.f; }
+__host__ __device__ __forceinline__ bool is_weight(int i)
+{
+    return i < OFF_B1 || (i >= OFF_V2 && i < OFF_B2) || (i >= OFF_V3 && i < OFF_B3);
+}
+
+__device__ __forceinline__ float clamp01(float z) { return fminf(fmaxf(z, 0.f), 1.f); }
 
 // Order-preserving u32 view of a key (floats: sign ? ~k : k | sign).
 __device__ __forceinline__ uint32_t ordered(uint32_t k, int kind)
@@ -55,15 +79,35 @@ __device__ __forceinline__ uint32_t ordered(uint32_t k, int kind)
     return k;
 }
 
-struct Norm {
-    uint32_t umin;
-    float inv_range;
-    __device__ __forceinline__ float operator()(uint32_t u) const
-    {
-        const uint32_t d = u > umin ? u - umin : 0u;
-        return fminf((float)d * inv_range, 1.0f);
-    }
+// Key range of the sample and the first layer's centres.
+struct Frame {
+    uint32_t umin, umax;
+    float inv_span;
+    uint32_t pad;
+    uint32_t c[H];
 };
+
+__device__ __forceinline__ float feature(uint32_t u, uint32_t c, float inv_span)
+{
+    return (float)((long long)u - (long long)c) * inv_span;
+}
+
+// F(u) with the effective weights w (exp applied) and centres c in shared memory.
+__device__ float network(const float* w, const uint32_t* c, float inv_span, uint32_t u)
+{
+    float h1[H];
+#pragma unroll
+    for (int j = 0; j < H; ++j) h1[j] = clamp01(fmaf(w[OFF_V1 + j], feature(u, c[j], inv_span), w[OFF_B1 + j]));
+    float y = w[OFF_B3];
+#pragma unroll 4
+    for (int k = 0; k < H; ++k) {
+        float z = w[OFF_B2 + k];
+#pragma unroll
+        for (int j = 0; j < H; ++j) z = fmaf(w[OFF_V2 + k * H + j], h1[j], z);
+        y = fmaf(w[OFF_V3 + k], clamp01(z), y);
+    }
+    return y;
+}
 
 // ---- 1. sample ---------------------------------------------------------------
 __global__ void k_sample(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ sample, uint32_t s,
@@ -76,234 +120,290 @@ __global__ void k_sample(const uint32_t* __restrict__ keys, uint32_t n, uint32_t
     }
 }
 
-// ---- 2. training points --------------------------------------------------
-// stats[0] = umin, stats[1] = umax (ordered), from the sorted sample.
-__global__ void k_points(const uint32_t* __restrict__ sorted, uint32_t s, float* __restrict__ xs,
-                         float* __restrict__ ys, uint32_t m, uint32_t* __restrict__ range)
+// ---- 2. frame, initial parameters, training points ---------------------------
+__global__ void k_frame(const uint32_t* __restrict__ sorted, uint32_t s, Frame* fr, float* params, int init_params)
 {
     const uint32_t umin = sorted[0], umax = sorted[s - 1];
-    const float inv = umax > umin ? 1.0f / (float)(umax - umin) : 0.f;
-    const Norm norm{umin, inv};
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        range[0] = umin;
-        range[1] = umax;
+    const float span = (float)max(umax - umin, 1u);
+    const int t = threadIdx.x;
+    if (t == 0) {
+        fr->umin = umin;
+        fr->umax = umax;
+        fr->inv_span = 1.0f / span;
+        fr->pad = 0;
     }
+    if (t < H) {
+        const uint32_t qa = sorted[min((uint32_t)(((uint64_t)t * s) / H), s - 1)];
+        const uint32_t qb = sorted[min((uint32_t)(((uint64_t)(t + 1) * s) / H), s - 1)];
+        fr->c[t] = qa + (qb - qa) / 2;
+        if (init_params) {
+            // ramp from 0 at qa to 1 at qb: w1 = span / width, b1 = 1/2
+            params[OFF_V1 + t] = logf(span / (float)max(qb - qa, 1u));
+            params[OFF_B1 + t] = 0.5f;
+        }
+    }
+    if (!init_params) return;
+    for (int i = t; i < H * H; i += blockDim.x)
+        params[OFF_V2 + i] = (i / H == i % H) ? 0.f : logf(1e-3f);  // w2 ~ identity
+    if (t < H) {
+        params[OFF_B2 + t] = 0.f;
+        params[OFF_V3 + t] = logf(1.0f / (float)H);  // output = mean of h2
+    }
+    if (t == 0) params[OFF_B3] = 0.f;
+}
+
+__global__ void k_points(const uint32_t* __restrict__ sorted, uint32_t s, uint32_t* __restrict__ xs,
+                         float* __restrict__ ys, uint32_t m)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m) {
         const uint32_t q = (uint32_t)(((uint64_t)(2 * i + 1) * s) / (2 * (uint64_t)m));
-        xs[i] = norm(sorted[min(q, s - 1)]);
+        xs[i] = sorted[min(q, s - 1)];
         ys[i] = ((float)i + 0.5f) / (float)m;
     }
 }
 
 // ---- 3. training -------------------------------------------------------------
-__global__ void k_init_params(float* p, float* adam_m, float* adam_s)
-{
-    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) {
-        float v = 0.f;
-        if (i < OFF_B1) v = 1.0f;                                                     // w1 = 1
-        else if (i < OFF_V2) v = -((float)(i - OFF_B1) + 0.5f) / (float)H;            // ramps across [0, 1]
-        else if (i < OFF_B2) {                                                        // w2 ~ (0.25 .. 2.25) / H
-            const uint32_t h = (uint32_t)(i - OFF_V2) * 2654435761u;
-            v = sqrtf((0.25f + 2.0f * (float)(h >> 8) / 16777216.0f) / (float)H);
-        } else if (i < OFF_V3) v = 0.f;
-        else if (i < OFF_B3) v = sqrtf(1.0f / (float)H);
-        else v = 0.f;
-        p[i] = v;
-        adam_m[i] = 0.f;
-        adam_s[i] = 0.f;
-    }
-}
-
-// Forward and backward for one point per thread; per-CTA gradient sums to
-// partial[blockIdx.x]; the last CTA sums the partials and (when lr > 0)
-// applies one Adam step. grad_out (optional) receives the summed gradient with
-// respect to the raw parameters, loss_out[step] the mean squared error.
 struct TrainArgs {
-    float* params;
-    float* adam_m;
-    float* adam_s;
-    const float* xs;
+    float* params;       // NPARAM raw parameters: read at the start, written by CTA 0 at the end
+    const Frame* frame;
+    const uint32_t* xs;  // m training keys (order-preserving form)
     const float* ys;
     uint32_t m;
-    float* partial;  // [gridDim.x][NPARAM + 1]
-    uint32_t* ticket;
-    float* grad_out;
-    float* loss_out;
-    int step;  // 1-based Adam step
-    float lr;
+    float* partial;      // [2][gridDim.x][NPARAM + 1]
+    uint32_t* barrier;   // zero before the launch
+    float* grad_out;     // optional: gradient at the starting parameters
+    float* loss_out;     // optional: [steps] loss before each update
+    int steps;           // >= 1
+    float lr;            // 0: gradients only
+    int* err;
 };
 
-__global__ void __launch_bounds__(TRAIN_THREADS) k_train_step(TrainArgs a)
+__global__ void __launch_bounds__(TRAIN_THREADS, 1) k_train(TrainArgs a)
 {
     extern __shared__ float sm[];
-    float* w = sm;                                 // NPARAM: weights squared, biases copied
-    float* H1 = w + NPARAM;                        // [H][PSTRIDE]
-    float* D2 = H1 + H * PSTRIDE;                  // [H][PSTRIDE]
-    float* D1 = D2 + H * PSTRIDE;                  // [H][PSTRIDE]
-    float* H2 = D1 + H * PSTRIDE;                  // [H][PSTRIDE]
-    float* X = H2 + H * PSTRIDE;                   // [PSTRIDE]
-    float* G = X + PSTRIDE;                        // [PSTRIDE]
+    float* p = sm;              // this CTA's copy of the raw parameters
+    float* am = p + NPARAM;     // Adam first moment
+    float* as = am + NPARAM;    // Adam second moment
+    float* w = as + NPARAM;     // effective parameters: exp(v) for weights
+    float* H1 = w + NPARAM;     // [H][PSTRIDE] per-point activations and deltas
+    float* D2 = H1 + H * PSTRIDE;
+    float* D1 = D2 + H * PSTRIDE;
+    float* P1 = D1 + H * PSTRIDE;  // d1 * feature
+    float* H2 = P1 + H * PSTRIDE;
+    float* G = H2 + H * PSTRIDE;   // [PSTRIDE] output deltas
+    __shared__ uint32_t s_c[H];
     __shared__ float s_red[TRAIN_THREADS / 32];
-    __shared__ bool s_last;
+    __shared__ int s_abort;
     const int tid = threadIdx.x;
     for (int i = tid; i < NPARAM; i += TRAIN_THREADS) {
-        const float v = a.params[i];
-        const bool is_w = i < OFF_B1 || (i >= OFF_V2 && i < OFF_B2) || (i >= OFF_V3 && i < OFF_B3);
-        w[i] = is_w ? v * v : v;
+        p[i] = a.params[i];
+        am[i] = 0.f;
+        as[i] = 0.f;
     }
+    if (tid < H) s_c[tid] = a.frame->c[tid];
+    if (tid == 0) s_abort = 0;
+    const float inv_span = a.frame->inv_span;
+    const uint32_t per_round = gridDim.x * TRAIN_THREADS;
+    const uint32_t rounds = (a.m + per_round - 1) / per_round;
+    const float inv_m = 1.0f / (float)a.m;
     __syncthreads();
 
-    const uint32_t p = blockIdx.x * TRAIN_THREADS + tid;
-    const bool valid = p < a.m;
-    const float x = valid ? a.xs[p] : 0.f;
-    const float y = valid ? a.ys[p] : 0.f;
-    float h1[H], h2[H];
-    uint32_t on1 = 0, on2 = 0;
+    for (int step = 0; step < a.steps; ++step) {
+        for (int i = tid; i < NPARAM; i += TRAIN_THREADS) w[i] = is_weight(i) ? expf(p[i]) : p[i];
+        __syncthreads();
+        // This CTA's gradient sums with respect to the effective parameters:
+        // thread t owns dW2[t / 8][4 (t % 8) .. + 3] and, for t < 5H + 1, one
+        // of dw1, db1, db2, dw3 (kinds 0..3) or db3 (t = 5H).
+        const int k2 = tid >> 3, j2 = (tid & 7) * 4;
+        float acc2[4] = {0.f, 0.f, 0.f, 0.f};
+        float acc1 = 0.f, lsum = 0.f;
+        for (uint32_t r = 0; r < rounds; ++r) {
+            const uint32_t pi = (r * gridDim.x + blockIdx.x) * TRAIN_THREADS + tid;
+            const bool valid = pi < a.m;
+            const uint32_t u = valid ? a.xs[pi] : s_c[0];
+            const float yv = valid ? a.ys[pi] : 0.f;
+            float h1[H], h2[H];
+            uint32_t on1 = 0, on2 = 0;
 #pragma unroll
-    for (int j = 0; j < H; ++j) {
-        const float z = w[OFF_V1 + j] * x + w[OFF_B1 + j];
-        h1[j] = relu(z);
-        on1 |= (z > 0.f ? 1u : 0u) << j;
-    }
-    float yhat = w[OFF_B3];
+            for (int j = 0; j < H; ++j) {
+                const float z = fmaf(w[OFF_V1 + j], feature(u, s_c[j], inv_span), w[OFF_B1 + j]);
+                h1[j] = clamp01(z);
+                on1 |= (z > 0.f && z < 1.f ? 1u : 0u) << j;
+            }
+            float yhat = w[OFF_B3];
 #pragma unroll 4
-    for (int k = 0; k < H; ++k) {
-        float z = w[OFF_B2 + k];
+            for (int k = 0; k < H; ++k) {
+                float z = w[OFF_B2 + k];
 #pragma unroll
-        for (int j = 0; j < H; ++j) z += w[OFF_V2 + k * H + j] * h1[j];
-        h2[k] = relu(z);
-        on2 |= (z > 0.f ? 1u : 0u) << k;
-        yhat += w[OFF_V3 + k] * h2[k];
-    }
-    const float err = valid ? yhat - y : 0.f;
-    const float g = 2.f * err / (float)a.m;
-    float d2[H];
+                for (int j = 0; j < H; ++j) z = fmaf(w[OFF_V2 + k * H + j], h1[j], z);
+                h2[k] = clamp01(z);
+                on2 |= (z > 0.f && z < 1.f ? 1u : 0u) << k;
+                yhat = fmaf(w[OFF_V3 + k], h2[k], yhat);
+            }
+            const float e = valid ? yhat - yv : 0.f;
+            lsum += e * e;
+            const float g = 2.f * e * inv_m;
+            float d2[H];
 #pragma unroll
-    for (int k = 0; k < H; ++k) d2[k] = ((on2 >> k) & 1) ? g * w[OFF_V3 + k] : 0.f;
+            for (int k = 0; k < H; ++k) d2[k] = ((on2 >> k) & 1) ? g * w[OFF_V3 + k] : 0.f;
 #pragma unroll
-    for (int j = 0; j < H; ++j) {
-        float s = 0.f;
+            for (int j = 0; j < H; ++j) {
+                float s = 0.f;
 #pragma unroll
-        for (int k = 0; k < H; ++k) s += d2[k] * w[OFF_V2 + k * H + j];
-        D1[j * PSTRIDE + tid] = ((on1 >> j) & 1) ? s : 0.f;
-        H1[j * PSTRIDE + tid] = h1[j];
-        D2[j * PSTRIDE + tid] = d2[j];
-        H2[j * PSTRIDE + tid] = h2[j];
-    }
-    X[tid] = x;
-    G[tid] = g;
-    // loss partial
-    float l = err * err;
+                for (int k = 0; k < H; ++k) s = fmaf(d2[k], w[OFF_V2 + k * H + j], s);
+                const float d1 = ((on1 >> j) & 1) ? s : 0.f;
+                D1[j * PSTRIDE + tid] = d1;
+                P1[j * PSTRIDE + tid] = d1 * feature(u, s_c[j], inv_span);
+                H1[j * PSTRIDE + tid] = h1[j];
+                D2[j * PSTRIDE + tid] = d2[j];
+                H2[j * PSTRIDE + tid] = h2[j];
+            }
+            G[tid] = g;
+            __syncthreads();
+            for (int q = 0; q < TRAIN_THREADS; ++q) {
+                const float d = D2[k2 * PSTRIDE + q];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(dev::FULL_MASK, l, o);
-    if ((tid & 31) == 0) s_red[tid >> 5] = l;
-    __syncthreads();
-
-    // Gradient sums over this CTA's points, with respect to the weights w
-    // (converted to the raw v = sqrt(w) parameters by the last CTA).
-    float* out = a.partial + (size_t)blockIdx.x * (NPARAM + 1);
-    {
-        // dW2[k][j] = sum_p D2[k][p] H1[j][p]: thread t owns k = t / 8, j = 4 (t % 8) .. + 3
-        const int k = tid >> 3, j0 = (tid & 7) * 4;
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int q = 0; q < TRAIN_THREADS; ++q) {
-            const float d = D2[k * PSTRIDE + q];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[r] += d * H1[(j0 + r) * PSTRIDE + q];
+                for (int i = 0; i < 4; ++i) acc2[i] = fmaf(d, H1[(j2 + i) * PSTRIDE + q], acc2[i]);
+            }
+            if (tid < 5 * H + 1) {
+                const int kind = tid / H, u1 = tid % H;
+                for (int q = 0; q < TRAIN_THREADS; ++q) {
+                    switch (kind) {
+                    case 0: acc1 += P1[u1 * PSTRIDE + q]; break;
+                    case 1: acc1 += D1[u1 * PSTRIDE + q]; break;
+                    case 2: acc1 += D2[u1 * PSTRIDE + q]; break;
+                    case 3: acc1 = fmaf(G[q], H2[u1 * PSTRIDE + q], acc1); break;
+                    default: acc1 += G[q]; break;
+                    }
+                }
+            }
+            __syncthreads();  // the buffers are rewritten by the next round
         }
+        float* out = a.partial + ((size_t)(step & 1) * gridDim.x + blockIdx.x) * (NPARAM + 1);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) out[OFF_V2 + k * H + j0 + r] = acc[r];
-    }
-    if (tid < 5 * H + 1) {
-        // 0..H-1: dW1, H..2H-1: db1, 2H..3H-1: db2, 3H..4H-1: dW3, 4H..5H-1: unused, 5H: db3
-        const int kind = tid / H, u = tid % H;
-        float acc = 0.f;
-        for (int q = 0; q < TRAIN_THREADS; ++q) {
-            switch (kind) {
-            case 0: acc += D1[u * PSTRIDE + q] * X[q]; break;
-            case 1: acc += D1[u * PSTRIDE + q]; break;
-            case 2: acc += D2[u * PSTRIDE + q]; break;
-            case 3: acc += G[q] * H2[u * PSTRIDE + q]; break;
-            default: acc += G[q]; break;
+        for (int i = 0; i < 4; ++i) out[OFF_V2 + k2 * H + j2 + i] = acc2[i];
+        if (tid < 5 * H + 1) {
+            const int kind = tid / H, u1 = tid % H;
+            if (kind == 0) out[OFF_V1 + u1] = acc1;
+            else if (kind == 1) out[OFF_B1 + u1] = acc1;
+            else if (kind == 2) out[OFF_B2 + u1] = acc1;
+            else if (kind == 3) out[OFF_V3 + u1] = acc1;
+            else out[OFF_B3] = acc1;
+        }
+        lsum = dev::warp_reduce(lsum, [](float x, float y) { return x + y; });
+        if ((tid & 31) == 0) s_red[tid >> 5] = lsum;
+        __syncthreads();
+        if (tid == 0) {
+            float l = 0.f;
+            for (int i = 0; i < TRAIN_THREADS / 32; ++i) l += s_red[i];
+            out[NPARAM] = l;
+        }
+        // Grid barrier (the launch is cooperative, so every CTA is resident);
+        // the partial buffers alternate between steps, so one barrier a step
+        // suffices. The wait is bounded.
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            atomicAdd(a.barrier, 1u);
+            const uint32_t target = (uint32_t)(step + 1) * gridDim.x;
+            const unsigned long long t0 = dev::globaltimer();
+            uint32_t spin = 0;
+            while (dev::ld_acquire(a.barrier) < target) {
+                if ((++spin & 63) == 0 && dev::globaltimer() - t0 > dev::SPIN_LIMIT_NS) {
+                    dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                    s_abort = 1;
+                    break;
+                }
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (s_abort) return;
+        // Every CTA sums the partials in CTA order and applies the same update.
+        const float b1c = 1.f - powf(0.9f, (float)(step + 1)), b2c = 1.f - powf(0.999f, (float)(step + 1));
+        const float* base = a.partial + (size_t)(step & 1) * gridDim.x * (NPARAM + 1);
+        for (int i = tid; i <= NPARAM; i += TRAIN_THREADS) {
+            float sum = 0.f;
+            for (uint32_t c = 0; c < gridDim.x; ++c) sum += __ldcg(base + (size_t)c * (NPARAM + 1) + i);
+            if (i == NPARAM) {
+                if (blockIdx.x == 0 && a.loss_out != nullptr) a.loss_out[step] = sum * inv_m;
+                continue;
+            }
+            const float grad = is_weight(i) ? sum * w[i] : sum;  // d exp(v) / dv = exp(v)
+            if (step == 0 && blockIdx.x == 0 && a.grad_out != nullptr) a.grad_out[i] = grad;
+            if (a.lr > 0.f) {
+                const float m1 = 0.9f * am[i] + 0.1f * grad;
+                const float s1 = 0.999f * as[i] + 0.001f * grad * grad;
+                am[i] = m1;
+                as[i] = s1;
+                p[i] -= a.lr * (m1 / b1c) / (sqrtf(s1 / b2c) + 1e-8f);
             }
         }
-        if (kind == 0) out[OFF_V1 + u] = acc;
-        else if (kind == 1) out[OFF_B1 + u] = acc;
-        else if (kind == 2) out[OFF_B2 + u] = acc;
-        else if (kind == 3) out[OFF_V3 + u] = acc;
-        else if (kind == 5) out[OFF_B3] = acc;
+        __syncthreads();
     }
-    if (tid == 0) {
-        float l2 = 0.f;
-        for (int i = 0; i < TRAIN_THREADS / 32; ++i) l2 += s_red[i];
-        out[NPARAM] = l2;
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-
-    // Last CTA: sum the partials in CTA order and update.
-    const float b1c = 1.f - powf(0.9f, (float)a.step), b2c = 1.f - powf(0.999f, (float)a.step);
-    for (int i = tid; i <= NPARAM; i += TRAIN_THREADS) {
-        float sum = 0.f;
-        for (uint32_t c = 0; c < gridDim.x; ++c) sum += *((volatile float*)(a.partial + (size_t)c * (NPARAM + 1) + i));
-        if (i == NPARAM) {
-            if (a.loss_out) a.loss_out[a.step - 1] = sum / (float)a.m;
-            continue;
-        }
-        const float v = a.params[i];
-        const bool is_w = i < OFF_B1 || (i >= OFF_V2 && i < OFF_B2) || (i >= OFF_V3 && i < OFF_B3);
-        const float grad = is_w ? sum * 2.f * v : sum;  // d/dv of w = v^2
-        if (a.grad_out) a.grad_out[i] = grad;
-        if (a.lr > 0.f) {
-            const float m1 = 0.9f * a.adam_m[i] + 0.1f * grad;
-            const float s1 = 0.999f * a.adam_s[i] + 0.001f * grad * grad;
-            a.adam_m[i] = m1;
-            a.adam_s[i] = s1;
-            a.params[i] = v - a.lr * (m1 / b1c) / (sqrtf(s1 / b2c) + 1e-8f);
-        }
-    }
-    if (tid == 0) *a.ticket = 0;  // ready for the next step's launch
+    if (blockIdx.x == 0)
+        for (int i = tid; i < NPARAM; i += TRAIN_THREADS) a.params[i] = p[i];
 }
 
-// ---- 4. compile the network into a CDF table -----------------------------
-__global__ void k_table(const float* __restrict__ params, float* __restrict__ table, int grid_pts, float alpha)
+// ---- 4. splitters and their lookup table -----------------------------------
+// sp[b - 1] = min{u in [umin, umax + 1] : F(u) >= b / B}, saturated to 2^32-1;
+// without the model, equal-width buckets over [umin, umax].
+__global__ void k_splitters(const float* __restrict__ params, const Frame* __restrict__ fr, uint32_t buckets,
+                            uint32_t* __restrict__ sp, int use_model)
 {
     __shared__ float w[NPARAM];
-    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) {
-        const float v = params[i];
-        const bool is_w = i < OFF_B1 || (i >= OFF_V2 && i < OFF_B2) || (i >= OFF_V3 && i < OFF_B3);
-        w[i] = is_w ? v * v : v;
-    }
+    __shared__ uint32_t c[H];
+    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) w[i] = is_weight(i) ? expf(params[i]) : params[i];
+    if (threadIdx.x < H) c[threadIdx.x] = fr->c[threadIdx.x];
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > grid_pts) return;
-    const float x = (float)i / (float)grid_pts;
-    float h1[H];
-#pragma unroll
-    for (int j = 0; j < H; ++j) h1[j] = relu(w[OFF_V1 + j] * x + w[OFF_B1 + j]);
-    float y = w[OFF_B3];
-    for (int k = 0; k < H; ++k) {
-        float z = w[OFF_B2 + k];
-#pragma unroll
-        for (int j = 0; j < H; ++j) z += w[OFF_V2 + k * H + j] * h1[j];
-        y += w[OFF_V3 + k] * relu(z);
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (b >= buckets) return;
+    const uint32_t umin = fr->umin, umax = fr->umax;
+    uint64_t lo = umin, hi = (uint64_t)umax + 1;
+    if (!use_model) {
+        lo = umin + ((uint64_t)b * ((uint64_t)(umax - umin) + 1)) / buckets;
+    } else {
+        const float target = (float)b / (float)buckets;
+        const float inv_span = fr->inv_span;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (network(w, c, inv_span, (uint32_t)mid) >= target) hi = mid;
+            else lo = mid + 1;
+        }
     }
-    // alpha * F(x) + (1 - alpha) * x: the linear share bounds the slope from
-    // below, so modes the network cannot resolve are never merged.
-    table[i] = alpha * fminf(fmaxf(y, 0.f), 1.f) + (1.f - alpha) * x;
+    sp[b - 1] = (uint32_t)min(lo, (uint64_t)0xFFFFFFFFu);
 }
 
-// The identity table: bucket by the normalised key alone (the method without
-// the network, for comparison).
-__global__ void k_table_linear(float* table, int grid_pts)
+__device__ __forceinline__ int lut_shift(uint32_t umin, uint32_t umax)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= grid_pts) table[i] = (float)i / (float)grid_pts;
+    const uint32_t span = umax - umin;
+    const int bits = span == 0 ? 0 : 32 - __clz(span);
+    return max(0, bits - LUT_BITS);
+}
+
+// lut[c] = number of splitters <= the first key of cell c; lut[NCELLS] = B - 1.
+__global__ void k_lut(const uint32_t* __restrict__ sp, uint32_t buckets, const Frame* __restrict__ fr,
+                      uint16_t* __restrict__ lut)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > (uint32_t)NCELLS) return;
+    if (c == (uint32_t)NCELLS) {
+        lut[c] = (uint16_t)(buckets - 1);
+        return;
+    }
+    const uint64_t start = (uint64_t)fr->umin + ((uint64_t)c << lut_shift(fr->umin, fr->umax));
+    uint32_t lo = 0, hi = buckets - 1;
+    if (start > 0xFFFFFFFFull) {
+        lo = hi;
+    } else {
+        while (lo < hi) {
+            const uint32_t m = (lo + hi) >> 1;
+            if (sp[m] <= (uint32_t)start) lo = m + 1;
+            else hi = m;
+        }
+    }
+    lut[c] = (uint16_t)lo;
 }
 
 // ---- 5. partition ----------------------------------------------------------
@@ -312,51 +412,61 @@ struct PartArgs {
     uint32_t* out;
     uint32_t n;
     int kind;
-    const uint32_t* range;  // umin, umax
-    const float* table;
-    int grid_pts;
+    const Frame* frame;
+    const uint32_t* sp;     // buckets - 1 splitters
+    const uint16_t* lut;    // NCELLS + 1 entries
     uint32_t buckets;
-    uint32_t* counts;   // [gridDim.x][buckets]: counts, then absolute start offsets
-    uint32_t* bucket_off;  // [buckets + 1]
+    uint32_t* counts;       // [gridDim.x][buckets]: counts, then exclusive column offsets
+    uint32_t* bucket_off;   // [buckets + 1]
 };
 
-struct BucketFn {
-    Norm norm;
-    const float* table;
-    int grid_pts;
-    uint32_t buckets;
+// Bucket of a key: the number of splitters <= u, searched among the splitters
+// of u's lookup cell only.
+struct Bucketer {
+    const uint32_t* sp;
+    const uint16_t* lut;
+    uint32_t umin;
+    int shift;
     __device__ __forceinline__ uint32_t operator()(uint32_t u) const
     {
-        const float s = norm(u) * (float)grid_pts;
-        const int i = min((int)s, grid_pts - 1);
-        const float f = s - (float)i;
-        const float lo = table[i];
-        const float c = lo + (table[i + 1] - lo) * f;
-        return min((uint32_t)(c * (float)buckets), buckets - 1);
+        if (u < umin) return 0;
+        const uint32_t c = min((u - umin) >> shift, (uint32_t)NCELLS - 1);
+        uint32_t lo = lut[c], hi = lut[c + 1];
+        while (lo < hi) {
+            const uint32_t m = (lo + hi) >> 1;
+            if (sp[m] <= u) lo = m + 1;
+            else hi = m;
+        }
+        return lo;
     }
 };
 
-__device__ __forceinline__ BucketFn make_bucket_fn(const PartArgs& a, const float* table)
+__host__ __device__ constexpr std::size_t part_smem_bytes(uint32_t buckets)
 {
-    const uint32_t umin = a.range[0], umax = a.range[1];
-    return BucketFn{Norm{umin, umax > umin ? 1.0f / (float)(umax - umin) : 0.f}, table, a.grid_pts, a.buckets};
+    return (std::size_t)buckets * 4 + (std::size_t)(buckets - 1) * 4 + (std::size_t)(NCELLS + 1) * 2;
 }
 
-constexpr int PART_THREADS = 1024;
+// Loads the splitters and the table into shared memory; returns the bucketer.
+__device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* sh)
+{
+    uint32_t* sp = sh + a.buckets;
+    uint16_t* lut = reinterpret_cast<uint16_t*>(sp + (a.buckets - 1));
+    for (uint32_t i = threadIdx.x; i + 1 < a.buckets; i += PART_THREADS) sp[i] = a.sp[i];
+    for (int i = threadIdx.x; i <= NCELLS; i += PART_THREADS) lut[i] = a.lut[i];
+    const uint32_t umin = a.frame->umin, umax = a.frame->umax;
+    return Bucketer{sp, lut, umin, lut_shift(umin, umax)};
+}
 
 __global__ void __launch_bounds__(PART_THREADS) k_count(PartArgs a)
 {
     extern __shared__ uint32_t sh[];
-    uint32_t* hist = sh;                                          // buckets
-    float* table = reinterpret_cast<float*>(sh + a.buckets);      // grid + 1
+    uint32_t* hist = sh;  // buckets
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) hist[i] = 0;
-    for (int i = threadIdx.x; i <= a.grid_pts; i += PART_THREADS) table[i] = a.table[i];
+    const Bucketer bk = load_bucketer(a, sh);
     __syncthreads();
-    const BucketFn bf = make_bucket_fn(a, table);
     const uint32_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
-    const uint32_t b0 = blockIdx.x * chunk, b1 = min(a.n, b0 + chunk);
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += PART_THREADS)
-        atomicAdd(&hist[bf(ordered(a.keys[i], a.kind))], 1u);
+    const uint32_t b0 = min(a.n, blockIdx.x * chunk), b1 = min(a.n, b0 + chunk);
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += PART_THREADS) atomicAdd(&hist[bk(ordered(a.keys[i], a.kind))], 1u);
     __syncthreads();
     uint32_t* row = a.counts + (size_t)blockIdx.x * a.buckets;
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) row[i] = hist[i];
@@ -399,28 +509,28 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(const uint32_t* totals, ui
     if (threadIdx.x == 0) bucket_off[buckets] = s_carry;
 }
 
+// Keys only, so the order inside a bucket is free: shared-memory cursors.
 __global__ void __launch_bounds__(PART_THREADS) k_scatter(PartArgs a)
 {
     extern __shared__ uint32_t sh[];
     uint32_t* cursor = sh;
-    float* table = reinterpret_cast<float*>(sh + a.buckets);
     const uint32_t* row = a.counts + (size_t)blockIdx.x * a.buckets;
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) cursor[i] = a.bucket_off[i] + row[i];
-    for (int i = threadIdx.x; i <= a.grid_pts; i += PART_THREADS) table[i] = a.table[i];
+    const Bucketer bk = load_bucketer(a, sh);
     __syncthreads();
-    const BucketFn bf = make_bucket_fn(a, table);
     const uint32_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
-    const uint32_t b0 = blockIdx.x * chunk, b1 = min(a.n, b0 + chunk);
+    const uint32_t b0 = min(a.n, blockIdx.x * chunk), b1 = min(a.n, b0 + chunk);
     for (uint32_t i = b0 + threadIdx.x; i < b1; i += PART_THREADS) {
         const uint32_t k = a.keys[i];
-        const uint32_t pos = atomicAdd(&cursor[bf(ordered(k, a.kind))], 1u);
+        const uint32_t pos = atomicAdd(&cursor[bk(ordered(k, a.kind))], 1u);
         if (pos < a.n) a.out[pos] = k;
     }
 }
 
 // ---- 6/7. statistics and the boundary check ----------------------------------
 // stats: [0] violation flag, [1] keys in oversized buckets, [2] oversized
-// buckets, [3] largest bucket, [4] non-empty buckets.
+// buckets, [3] largest bucket, [4] non-empty buckets, [5] keys in oversized
+// buckets that hold one key value.
 __global__ void k_check(const uint32_t* __restrict__ out, const uint32_t* __restrict__ bucket_off, uint32_t buckets,
                         int kind, uint32_t cap, uint32_t* stats)
 {
@@ -431,11 +541,61 @@ __global__ void k_check(const uint32_t* __restrict__ out, const uint32_t* __rest
     if (len > cap) {
         atomicAdd(&stats[1], len);
         atomicAdd(&stats[2], 1u);
+        if (out[s] == out[e - 1]) atomicAdd(&stats[5], len);
     }
     if (len > 0) atomicAdd(&stats[4], 1u);
     atomicMax(&stats[3], len);
     // every bucket's first key must not precede the previous key
     if (s > 0 && len > 0 && ordered(out[s - 1], kind) > ordered(out[s], kind)) atomicExch(&stats[0], 1u);
+}
+
+// Expected bucket sizes from the sorted sample (S keys): the sample keys of
+// bucket b are those in [sp[b-1], sp[b]). est[0] receives the sample keys in
+// buckets whose size scaled to n would exceed cap.
+__global__ void k_estimate(const uint32_t* __restrict__ sorted, uint32_t s, const uint32_t* __restrict__ sp,
+                           uint32_t buckets, uint32_t n, uint32_t cap, uint32_t* est)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= buckets) return;
+    auto lower = [&](uint32_t v) {
+        uint32_t lo = 0, hi = s;
+        while (lo < hi) {
+            const uint32_t m = (lo + hi) >> 1;
+            if (sorted[m] < v) lo = m + 1;
+            else hi = m;
+        }
+        return lo;
+    };
+    const uint32_t lo = b == 0 ? 0u : lower(sp[b - 1]);
+    const uint32_t hi = b + 1 == buckets ? s : lower(sp[b]);
+    const uint32_t cnt = hi > lo ? hi - lo : 0u;
+    if ((uint64_t)cnt * n > (uint64_t)cap * s) atomicAdd(est, cnt);
+}
+
+// Points per cooperative training launch: at most one CTA per SM.
+static uint32_t train_grid(const device_context& ctx, uint32_t m)
+{
+    return std::max<uint32_t>(1, std::min<uint32_t>((m + TRAIN_THREADS - 1) / TRAIN_THREADS, ctx.sm_count));
+}
+
+constexpr std::size_t TRAIN_SMEM = (std::size_t)(4 * NPARAM + 5 * H * PSTRIDE + PSTRIDE) * 4;
+
+static void launch_train(device_context& ctx, TrainArgs& ta, uint32_t grid)
+{
+    static bool smem_set = false;
+    if (!smem_set) {
+        check_cuda(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM),
+                   "cudaFuncSetAttribute");
+        smem_set = true;
+    }
+    int per_sm = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_train, TRAIN_THREADS, TRAIN_SMEM),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if ((uint64_t)per_sm * ctx.sm_count < grid) throw std::invalid_argument("learned training: grid does not fit on the device");
+    void* args[] = {&ta};
+    check_cuda(cudaLaunchCooperativeKernel((const void*)k_train, dim3(grid), dim3(TRAIN_THREADS), args, TRAIN_SMEM,
+                                           ctx.stream),
+               "learned train launch");
 }
 
 }  // namespace learned
@@ -461,31 +621,48 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     }
     const uint32_t nn = (uint32_t)n;
     const uint32_t S = (uint32_t)std::min<std::size_t>(opt.sample > 0 ? opt.sample : (1u << 20), n);
-    const uint32_t M = (uint32_t)std::max<uint32_t>(TRAIN_THREADS, std::min<uint32_t>(opt.points > 0 ? opt.points : 8192, S));
-    const uint32_t buckets = (uint32_t)std::max<int>(2, opt.buckets > 0 ? opt.buckets : 32768);
-    const int grid_pts = opt.grid > 0 ? opt.grid : 8192;
-    const int steps = opt.steps >= 0 ? opt.steps : 64;
-    const int G = (int)((M + TRAIN_THREADS - 1) / TRAIN_THREADS);
-    const std::size_t part_smem = (std::size_t)buckets * 4 + (std::size_t)(grid_pts + 1) * 4;
-    if (part_smem > ctx.smem_optin)
-        throw std::invalid_argument("sort_learned: buckets + table do not fit in shared memory");
+    const uint32_t M = std::max<uint32_t>(
+        1, std::min<uint32_t>({(uint32_t)(opt.points > 0 ? opt.points : 8192), S, (uint32_t)(TRAIN_THREADS * ctx.sm_count)}));
+    // Buckets: about 8192 keys each by default, as many as the partition
+    // kernels' shared memory holds (counters, splitters and the table).
+    const uint32_t max_buckets = (uint32_t)std::min<std::size_t>(
+        65536, (ctx.smem_optin - (std::size_t)(NCELLS + 1) * 2 + 4) / 8);
+    uint32_t buckets;
+    if (opt.buckets > 0) {
+        buckets = (uint32_t)opt.buckets;
+        if (buckets < 2 || buckets > max_buckets)
+            throw std::invalid_argument("sort_learned: buckets must be in [2, " + std::to_string(max_buckets) + "]");
+    } else {
+        const uint32_t want = (uint32_t)((n / 8192 + 1023) / 1024 * 1024);
+        buckets = std::max<uint32_t>(4096, std::min<uint32_t>(want, max_buckets / 1024 * 1024));
+    }
+    const int steps = opt.steps >= 0 ? opt.steps : 32;
+    const float lr = opt.lr > 0 ? opt.lr : 0.05f;
+    const uint32_t G = train_grid(ctx, M);
+    const std::size_t part_smem = part_smem_bytes(buckets);
 
-    // Scratch: sample, points, params (+ Adam), partials, table, counts, offsets.
+    // Scratch: sample, points, params, frame, partials, splitters, table,
+    // counts, offsets, totals, small words.
     const std::size_t rows = (std::size_t)ctx.sm_count;
     temp_buffer sample(ctx.resource, (std::size_t)S * 4);
     temp_buffer pts(ctx.resource, (std::size_t)2 * M * 4);
-    temp_buffer prm(ctx.resource, (std::size_t)3 * NPARAM * 4);
-    temp_buffer partial(ctx.resource, (std::size_t)G * (NPARAM + 1) * 4);
-    temp_buffer table(ctx.resource, (std::size_t)(grid_pts + 1) * 4);
+    temp_buffer prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16);
+    temp_buffer partial(ctx.resource, (std::size_t)2 * G * (NPARAM + 1) * 4);
+    temp_buffer spl(ctx.resource, (std::size_t)buckets * 4 + (std::size_t)(NCELLS + 1) * 2 + 16);
     temp_buffer counts(ctx.resource, rows * buckets * 4);
     temp_buffer boff(ctx.resource, ((std::size_t)buckets + 1) * 4);
     temp_buffer totals(ctx.resource, (std::size_t)buckets * 4);
-    temp_buffer misc(ctx.resource, 64 + (std::size_t)std::max(steps, 1) * 4);
-    uint32_t* range = misc.as<uint32_t>();          // [0..1]
-    uint32_t* ticket = range + 2;                   // [2]
-    uint32_t* dstats = range + 4;                   // [4..8]
+    const std::size_t misc_bytes = 64 + (std::size_t)std::max(steps, 1) * 4;
+    temp_buffer misc(ctx.resource, misc_bytes);
+    uint32_t* barrier = misc.as<uint32_t>();        // [0]
+    uint32_t* dstats = barrier + 4;                 // [4..10]
     float* losses = reinterpret_cast<float*>(misc.as<unsigned char>() + 64);
-    check_cuda(cudaMemsetAsync(misc.get(), 0, 64 + (std::size_t)std::max(steps, 1) * 4, ctx.stream), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(misc.get(), 0, misc_bytes, ctx.stream), "cudaMemsetAsync");
+    float* params = prm.as<float>();
+    Frame* frame = reinterpret_cast<Frame*>(
+        (reinterpret_cast<uintptr_t>(prm.as<unsigned char>() + (std::size_t)NPARAM * 4) + 15) & ~(uintptr_t)15);
+    uint32_t* sp = spl.as<uint32_t>();
+    uint16_t* lut = reinterpret_cast<uint16_t*>(sp + buckets);
 
     const uint32_t* in = static_cast<const uint32_t*>(keys_in);
     uint32_t* out = static_cast<uint32_t*>(keys_out);
@@ -495,49 +672,68 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         check_cuda(cudaGetLastError(), "learned sample launch");
     }
     radix_sort(ctx, sample.get(), sample.get(), 4, 0, nullptr, nullptr, S, false);
-    float* xs = pts.as<float>();
-    float* ys = xs + M;
-    k_points<<<(M + 255) / 256, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, xs, ys, M, range);
-    check_cuda(cudaGetLastError(), "learned points launch");
-
-    float* params = prm.as<float>();
-    if (opt.params_in != nullptr) {
+    uint32_t* xs = pts.as<uint32_t>();
+    float* ys = reinterpret_cast<float*>(xs + M);
+    const bool own_init = opt.params_in == nullptr;
+    if (!own_init)
         check_cuda(cudaMemcpyAsync(params, opt.params_in, NPARAM * 4, cudaMemcpyHostToDevice, ctx.stream),
                    "cudaMemcpyAsync");
-        check_cuda(cudaMemsetAsync(params + NPARAM, 0, 2 * NPARAM * 4, ctx.stream), "cudaMemsetAsync");
-    } else {
-        k_init_params<<<1, 256, 0, ctx.stream>>>(params, params + NPARAM, params + 2 * NPARAM);
-        check_cuda(cudaGetLastError(), "learned init launch");
-    }
-    const std::size_t train_smem = (std::size_t)(NPARAM + 4 * H * PSTRIDE + 2 * PSTRIDE) * 4;
-    static bool smem_set = false;
-    if (!smem_set) {
-        check_cuda(cudaFuncSetAttribute(k_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem),
-                   "cudaFuncSetAttribute");
-        smem_set = true;
-    }
-    if (opt.use_model) {
-        for (int s = 1; s <= steps; ++s) {
-            kernel_timer kt(ctx, "learned.train_step");
-            TrainArgs ta{params, params + NPARAM, params + 2 * NPARAM, xs, ys, M, partial.as<float>(), ticket, nullptr,
-                         losses, s, opt.lr > 0 ? opt.lr : 0.02f};
-            k_train_step<<<G, TRAIN_THREADS, train_smem, ctx.stream>>>(ta);
-            check_cuda(cudaGetLastError(), "learned train launch");
-        }
-        kernel_timer kt(ctx, "learned.table");
-        k_table<<<(grid_pts + 1 + 255) / 256, 256, 0, ctx.stream>>>(params, table.as<float>(), grid_pts,
-                                                                   opt.model_weight);
-    } else {
-        k_table_linear<<<(grid_pts + 1 + 255) / 256, 256, 0, ctx.stream>>>(table.as<float>(), grid_pts);
-    }
-    check_cuda(cudaGetLastError(), "learned table launch");
-    if (opt.table_in != nullptr)
-        check_cuda(cudaMemcpyAsync(table.get(), opt.table_in, (std::size_t)(grid_pts + 1) * 4, cudaMemcpyHostToDevice,
-                                   ctx.stream),
-                   "cudaMemcpyAsync");
+    k_frame<<<1, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, frame, params, own_init ? 1 : 0);
+    k_points<<<(M + 255) / 256, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, xs, ys, M);
+    check_cuda(cudaGetLastError(), "learned frame launch");
 
-    PartArgs pa{in, out, nn, key_kind, range, table.as<float>(), grid_pts, buckets, counts.as<uint32_t>(),
-                boff.as<uint32_t>()};
+    const bool train = opt.use_model && steps > 0;
+    std::vector<float> hl(std::max(steps, 1));
+    auto read_losses = [&] {
+        if (!train) return;
+        check_cuda(cudaMemcpyAsync(hl.data(), losses, steps * 4, cudaMemcpyDeviceToHost, ctx.stream),
+                   "cudaMemcpyAsync");
+        if (opt.params_out != nullptr)
+            check_cuda(cudaMemcpyAsync(opt.params_out, params, NPARAM * 4, cudaMemcpyDeviceToHost, ctx.stream),
+                       "cudaMemcpyAsync");
+        ctx.finish();
+        st.first_loss = hl[0];
+        st.last_loss = hl[steps - 1];
+    };
+    if (train) {
+        kernel_timer kt(ctx, "learned.train");
+        TrainArgs ta{params, frame, xs, ys, M, partial.as<float>(), barrier, nullptr, losses, steps, lr,
+                     ctx.d_error};
+        launch_train(ctx, ta, G);
+    }
+    {
+        kernel_timer kt(ctx, "learned.splitters");
+        if (opt.splitters_in != nullptr)
+            check_cuda(cudaMemcpyAsync(sp, opt.splitters_in, (std::size_t)(buckets - 1) * 4, cudaMemcpyHostToDevice,
+                                       ctx.stream),
+                       "cudaMemcpyAsync");
+        else
+            k_splitters<<<(buckets + 127) / 128, 128, 0, ctx.stream>>>(params, frame, buckets, sp,
+                                                                       opt.use_model ? 1 : 0);
+        k_lut<<<(NCELLS + 1 + 255) / 256, 256, 0, ctx.stream>>>(sp, buckets, frame, lut);
+        check_cuda(cudaGetLastError(), "learned splitter launch");
+    }
+
+    // A model that would leave most keys in oversized buckets cannot beat the
+    // plain sort: decide from the sample, before the partition.
+    const uint32_t cap = segsort_cta_cap(4, false);
+    k_estimate<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, sp, buckets, nn, cap,
+                                                               dstats + 6);
+    check_cuda(cudaGetLastError(), "learned estimate launch");
+    uint32_t est = 0;
+    check_cuda(cudaMemcpyAsync(&est, dstats + 6, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    ctx.finish();
+    st.buckets = buckets;
+    st.estimated_oversized_keys = (uint32_t)std::min<uint64_t>(n, (uint64_t)est * n / S);
+    if ((uint64_t)est * 2 > S) {
+        read_losses();
+        st.fallback = 1;
+        radix_sort(ctx, keys_in, keys_out, 4, key_kind, nullptr, nullptr, n, false);
+        if (stats_host) *stats_host = st;
+        return;
+    }
+
+    PartArgs pa{in, out, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), boff.as<uint32_t>()};
     static std::size_t smem_part_set = 0;
     if (smem_part_set < part_smem) {
         check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
@@ -566,29 +762,23 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     segmented_sort(ctx, out, out, 4, key_kind, nullptr, nullptr, n, boff.as<uint32_t>(), buckets, false, so);
     {
         kernel_timer kt(ctx, "learned.check");
-        k_check<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(out, boff.as<uint32_t>(), buckets, key_kind,
-                                                                segsort_cta_cap(4, false), dstats);
+        k_check<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(out, boff.as<uint32_t>(), buckets, key_kind, cap,
+                                                                dstats);
         check_cuda(cudaGetLastError(), "learned check launch");
     }
     // Read the statistics (and losses); a violation sends the input to the
-    // plain radix sort.
-    std::vector<uint32_t> hs(5);
-    check_cuda(cudaMemcpyAsync(hs.data(), dstats, 5 * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
-    std::vector<float> hl(std::max(steps, 1));
-    if (steps > 0 && opt.use_model)
-        check_cuda(cudaMemcpyAsync(hl.data(), losses, steps * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
-    if (opt.params_out != nullptr)
-        check_cuda(cudaMemcpyAsync(opt.params_out, params, NPARAM * 4, cudaMemcpyDeviceToHost, ctx.stream),
-                   "cudaMemcpyAsync");
-    ctx.finish();
+    // plain radix sort. (The bucket of a key is the result of a binary search
+    // over the splitters, which is monotone in the key for any splitter
+    // array, so the check guards the implementation rather than the model.)
+    std::vector<uint32_t> hs(6);
+    check_cuda(cudaMemcpyAsync(hs.data(), dstats, 6 * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    read_losses();
     st.violation = hs[0];
     st.oversized_keys = hs[1];
     st.oversized_buckets = hs[2];
     st.largest_bucket = hs[3];
     st.nonempty_buckets = hs[4];
-    st.buckets = buckets;
-    st.first_loss = (steps > 0 && opt.use_model) ? hl[0] : 0.f;
-    st.last_loss = (steps > 0 && opt.use_model) ? hl[steps - 1] : 0.f;
+    st.constant_keys = hs[5];
     if (st.violation) {
         st.fallback = 1;
         radix_sort(ctx, keys_in, keys_out, 4, key_kind, nullptr, nullptr, n, false);
@@ -596,35 +786,35 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     if (stats_host) *stats_host = st;
 }
 
-void mlp_gradients(device_context& ctx, const float* params_host, const float* xs_host, const float* ys_host,
-                   std::size_t m, float* grad_host, float* loss_host)
+void mlp_gradients(device_context& ctx, const float* params_host, const uint32_t* centres_host, float inv_span,
+                   const uint32_t* keys_host, const float* ys_host, std::size_t m, float* grad_host, float* loss_host)
 {
     using namespace learned;
     if (m == 0 || m > (1u << 24)) throw std::invalid_argument("mlp_gradients: 0 < m <= 2^24");
     ctx.activate();
-    const int G = (int)((m + TRAIN_THREADS - 1) / TRAIN_THREADS);
-    temp_buffer prm(ctx.resource, (std::size_t)3 * NPARAM * 4);
+    const uint32_t G = train_grid(ctx, (uint32_t)m);
+    temp_buffer prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16);
     temp_buffer pts(ctx.resource, (std::size_t)2 * m * 4);
-    temp_buffer partial(ctx.resource, (std::size_t)G * (NPARAM + 1) * 4);
-    temp_buffer misc(ctx.resource, 64 + 2 * NPARAM * 4);
+    temp_buffer partial(ctx.resource, (std::size_t)2 * G * (NPARAM + 1) * 4);
+    temp_buffer misc(ctx.resource, 64 + (std::size_t)NPARAM * 4);
     float* params = prm.as<float>();
-    float* xs = pts.as<float>();
-    float* ys = xs + m;
-    uint32_t* ticket = misc.as<uint32_t>();
+    Frame* frame = reinterpret_cast<Frame*>(
+        (reinterpret_cast<uintptr_t>(prm.as<unsigned char>() + (std::size_t)NPARAM * 4) + 15) & ~(uintptr_t)15);
+    uint32_t* xs = pts.as<uint32_t>();
+    float* ys = reinterpret_cast<float*>(xs + m);
+    uint32_t* barrier = misc.as<uint32_t>();
     float* loss = reinterpret_cast<float*>(misc.as<unsigned char>() + 16);
     float* grad = reinterpret_cast<float*>(misc.as<unsigned char>() + 64);
-    check_cuda(cudaMemsetAsync(misc.get(), 0, 64 + 2 * NPARAM * 4, ctx.stream), "cudaMemsetAsync");
-    check_cuda(cudaMemsetAsync(params, 0, 3 * NPARAM * 4, ctx.stream), "cudaMemsetAsync");
+    Frame hf{};
+    hf.inv_span = inv_span;
+    std::memcpy(hf.c, centres_host, sizeof(hf.c));
+    check_cuda(cudaMemsetAsync(misc.get(), 0, 64 + (std::size_t)NPARAM * 4, ctx.stream), "cudaMemsetAsync");
     check_cuda(cudaMemcpyAsync(params, params_host, NPARAM * 4, cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
-    check_cuda(cudaMemcpyAsync(xs, xs_host, m * 4, cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
+    check_cuda(cudaMemcpyAsync(frame, &hf, sizeof(Frame), cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
+    check_cuda(cudaMemcpyAsync(xs, keys_host, m * 4, cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
     check_cuda(cudaMemcpyAsync(ys, ys_host, m * 4, cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
-    const std::size_t train_smem = (std::size_t)(NPARAM + 4 * H * PSTRIDE + 2 * PSTRIDE) * 4;
-    check_cuda(cudaFuncSetAttribute(k_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem),
-               "cudaFuncSetAttribute");
-    TrainArgs ta{params, params + NPARAM, params + 2 * NPARAM, xs, ys, (uint32_t)m, partial.as<float>(), ticket, grad,
-                 loss, 1, 0.f};
-    k_train_step<<<G, TRAIN_THREADS, train_smem, ctx.stream>>>(ta);
-    check_cuda(cudaGetLastError(), "mlp gradient launch");
+    TrainArgs ta{params, frame, xs, ys, (uint32_t)m, partial.as<float>(), barrier, grad, loss, 1, 0.f, ctx.d_error};
+    launch_train(ctx, ta, G);
     check_cuda(cudaMemcpyAsync(grad_host, grad, NPARAM * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
     check_cuda(cudaMemcpyAsync(loss_host, loss, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
     ctx.finish();

@@ -8,22 +8,20 @@
 
 namespace gbc {
 namespace learned {
-constexpr int H = 32;                     // hidden width: 1 -> H -> H -> 1
-constexpr int NPARAM = 4 * H + H * H + 1;  // v1, b1, v2, b2, v3, b3
+constexpr int H = 32;                      // hidden width: 1 -> H -> H -> 1
+constexpr int NPARAM = 4 * H + H * H + 1;  // v1, b1, v2, b2, v3, b3 (weights are exp(v))
 }  // namespace learned
 
 struct learned_options {
-    int sample = 0;        // sampled keys (0: 2^20)
-    int points = 0;        // training points taken from the sorted sample (0: 8192)
-    int buckets = 0;       // partition buckets (0: 32768)
-    int grid = 0;          // CDF table resolution (0: 8192 segments)
-    int steps = -1;        // Adam steps (-1: 64)
-    float lr = 0.f;        // Adam learning rate (0: 0.02)
-    bool use_model = true; // false: bucket by the normalised key alone (no network)
-    float model_weight = 0.5f;  // alpha: table = alpha * network + (1 - alpha) * identity
-    const float* params_in = nullptr;  // host: start from these parameters instead of the default init
-    float* params_out = nullptr;       // host: receives the fitted parameters
-    const float* table_in = nullptr;   // host: replaces the compiled CDF table (grid + 1 floats)
+    int sample = 0;     // sampled keys (0: 2^20)
+    int points = 0;     // training points taken from the sorted sample (0: 8192)
+    int buckets = 0;    // partition buckets (0: from n, up to what shared memory holds)
+    int steps = -1;     // Adam steps (-1: 32)
+    float lr = 0.f;     // Adam learning rate (0: 0.05)
+    bool use_model = true;  // false: equal-width buckets over the sampled key range (no network)
+    const float* params_in = nullptr;       // host: start from these parameters instead of the data-driven init
+    float* params_out = nullptr;            // host: receives the fitted parameters
+    const uint32_t* splitters_in = nullptr; // host: replaces the compiled splitters (buckets - 1 values)
 };
 
 struct learned_stats {
@@ -32,20 +30,27 @@ struct learned_stats {
     uint32_t largest_bucket = 0;
     uint32_t oversized_buckets = 0;  // larger than one CTA's shared-memory sort
     uint32_t oversized_keys = 0;
+    uint32_t constant_keys = 0;      // keys in oversized buckets that hold one key value
+    uint32_t estimated_oversized_keys = 0;  // predicted from the sample before the partition
     uint32_t violation = 0;          // bucket order was not monotone
     uint32_t fallback = 0;           // the plain radix sort produced the output
     float first_loss = 0.f, last_loss = 0.f;
 };
 
 //! Out-of-place sort of 32-bit keys (kind 0 unsigned, 1 signed, 2 float) by a
-//! learned CDF partition; output identical to radix_sort's. Synchronises once
-//! (to read the statistics and decide on the fallback).
+//! learned CDF partition; output identical to radix_sort's. Synchronises
+//! twice: after the splitters (a model that would leave more than half of the
+//! keys in oversized buckets sends the input to the plain radix sort) and at
+//! the end (statistics, boundary check).
 void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_kind, std::size_t n,
                   const learned_options& opt, learned_stats* stats_host);
 
 //! One forward/backward pass of the network over m points on the GPU:
 //! gradient of the mean squared error with respect to the raw parameters.
-void mlp_gradients(device_context& ctx, const float* params_host, const float* xs_host, const float* ys_host,
-                   std::size_t m, float* grad_host, float* loss_host);
+//! Points are keys in the order-preserving 32-bit domain; the network's first
+//! layer sees (key - centre[j]) * inv_span.
+void mlp_gradients(device_context& ctx, const float* params_host, const uint32_t* centres_host, float inv_span,
+                   const uint32_t* keys_host, const float* ys_host, std::size_t m, float* grad_host,
+                   float* loss_host);
 
 }  // namespace gbc

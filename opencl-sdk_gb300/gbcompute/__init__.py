@@ -176,7 +176,7 @@ _PROTOS = {
     "clc_learned_default_options": (None, [_vp]),
     "clc_sort_learned": (_i, [_vp, _vp, _vp, _i, _sz, _vp, _vp]),
     "clc_learned_param_count": (_i, []),
-    "clc_learned_mlp_gradients": (_i, [_vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "clc_learned_mlp_gradients": (_i, [_vp, _vp, _vp, C.c_float, _vp, _vp, _sz, _vp, _vp]),
     "clc_graph_begin": (_i, [_vp]),
     "clc_graph_end": (_i, [_vp, C.POINTER(_vp)]),
     "clc_graph_launch": (_i, [_vp, _vp]),
@@ -600,15 +600,16 @@ def capture(ctx: Context, fn) -> Graph:
 # ---- learned-CDF sort ---------------------------------------------------------
 
 class LearnedOptions(C.Structure):
-    _fields_ = [("sample", C.c_int), ("points", C.c_int), ("buckets", C.c_int), ("grid", C.c_int),
-                ("steps", C.c_int), ("lr", C.c_float), ("use_model", C.c_int), ("params_in", C.c_void_p),
-                ("params_out", C.c_void_p), ("table_in", C.c_void_p), ("model_weight", C.c_float)]
+    _fields_ = [("sample", C.c_int), ("points", C.c_int), ("buckets", C.c_int), ("steps", C.c_int),
+                ("lr", C.c_float), ("use_model", C.c_int), ("params_in", C.c_void_p), ("params_out", C.c_void_p),
+                ("splitters_in", C.c_void_p)]
 
 
 class LearnedStats(C.Structure):
     _fields_ = [("buckets", C.c_uint), ("nonempty_buckets", C.c_uint), ("largest_bucket", C.c_uint),
-                ("oversized_buckets", C.c_uint), ("oversized_keys", C.c_uint), ("violation", C.c_uint),
-                ("fallback", C.c_uint), ("first_loss", C.c_float), ("last_loss", C.c_float)]
+                ("oversized_buckets", C.c_uint), ("oversized_keys", C.c_uint), ("constant_keys", C.c_uint),
+                ("estimated_oversized_keys", C.c_uint), ("violation", C.c_uint), ("fallback", C.c_uint),
+                ("first_loss", C.c_float), ("last_loss", C.c_float)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -635,14 +636,18 @@ def learned_param_count() -> int:
     return lib.clc_learned_param_count()
 
 
-def learned_mlp_gradients(ctx: Context, params: np.ndarray, xs: np.ndarray, ys: np.ndarray):
+def learned_mlp_gradients(ctx: Context, params: np.ndarray, centres: np.ndarray, inv_span: float, keys: np.ndarray,
+                          ys: np.ndarray):
+    """Gradient (raw parameters) and loss of the network's mean squared error
+    over the points (keys in the order-preserving u32 domain, targets ys)."""
     p = np.ascontiguousarray(params, dtype=np.float32)
-    x = np.ascontiguousarray(xs, dtype=np.float32)
+    c = np.ascontiguousarray(centres, dtype=np.uint32)
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
     y = np.ascontiguousarray(ys, dtype=np.float32)
     g = np.zeros_like(p)
     loss = np.zeros(1, dtype=np.float32)
-    _raise_for(lib.clc_learned_mlp_gradients(ctx.handle, p.ctypes.data, x.ctypes.data, y.ctypes.data, x.size,
-                                             g.ctypes.data, loss.ctypes.data))
+    _raise_for(lib.clc_learned_mlp_gradients(ctx.handle, p.ctypes.data, c.ctypes.data, C.c_float(inv_span),
+                                             k.ctypes.data, y.ctypes.data, k.size, g.ctypes.data, loss.ctypes.data))
     return g, float(loss[0])
 
 

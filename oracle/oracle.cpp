@@ -416,34 +416,37 @@ void orc_ref_reduce(const void* in, std::size_t n, int type, int op, const void*
 int orc_hardware_threads(void) { return hw_threads(0); }
 
 // ---- learned-CDF network (no reference counterpart) -----------------------
-// 1 -> H -> H -> 1, ReLU, weights stored as v with w = v * v; loss = mean of
-// (yhat - y)^2. Gradient with respect to the raw parameters, in double.
-// Layout: v1[H], b1[H], v2[H][H] (row = output unit), b2[H], v3[H], b3.
-void orc_mlp_grad(const float* params, const float* xs, const float* ys, std::size_t m, int h, float* grad,
-                  double* loss)
+// 1 -> H -> H -> 1 on a key u (order-preserving u32 domain):
+//   d_j = (u - c_j) * inv_span, h1_j = clamp(w1_j d_j + b1_j, 0, 1),
+//   h2_k = clamp(b2_k + sum_j w2_kj h1_j, 0, 1), yhat = b3 + sum_k w3_k h2_k,
+// weights stored as v with w = exp(v); loss = mean of (yhat - y)^2. Gradient
+// with respect to the raw parameters, in double (clamp' = 1 strictly inside
+// (0, 1)). Layout: v1[H], b1[H], v2[H][H] (row = output unit), b2[H], v3[H], b3.
+void orc_mlp_grad(const float* params, const uint32_t* centres, float inv_span, const uint32_t* keys,
+                  const float* ys, std::size_t m, int h, float* grad, double* loss)
 {
     const int H = h;
     const int OV1 = 0, OB1 = H, OV2 = 2 * H, OB2 = 2 * H + H * H, OV3 = 3 * H + H * H, OB3 = 4 * H + H * H;
     const int NP = OB3 + 1;
+    auto is_w = [&](int i) { return i < OB1 || (i >= OV2 && i < OB2) || (i >= OV3 && i < OB3); };
     std::vector<double> w(NP), g(NP, 0.0);
-    for (int i = 0; i < NP; ++i) {
-        const bool is_w = i < OB1 || (i >= OV2 && i < OB2) || (i >= OV3 && i < OB3);
-        w[i] = is_w ? (double)params[i] * params[i] : params[i];
-    }
+    for (int i = 0; i < NP; ++i) w[i] = is_w(i) ? std::exp((double)params[i]) : (double)params[i];
     double l = 0;
-    std::vector<double> z1(H), h1(H), z2(H), h2(H), d2(H), d1(H);
+    std::vector<double> d(H), z1(H), h1(H), z2(H), h2(H), d2(H);
+    auto inside = [](double z) { return z > 0 && z < 1; };
+    auto clamp01 = [](double z) { return z < 0 ? 0.0 : (z > 1 ? 1.0 : z); };
     for (std::size_t p = 0; p < m; ++p) {
-        const double x = xs[p];
         for (int j = 0; j < H; ++j) {
-            z1[j] = w[OV1 + j] * x + w[OB1 + j];
-            h1[j] = z1[j] > 0 ? z1[j] : 0;
+            d[j] = (double)((int64_t)keys[p] - (int64_t)centres[j]) * (double)inv_span;
+            z1[j] = w[OV1 + j] * d[j] + w[OB1 + j];
+            h1[j] = clamp01(z1[j]);
         }
         double yhat = w[OB3];
         for (int k = 0; k < H; ++k) {
             double z = w[OB2 + k];
             for (int j = 0; j < H; ++j) z += w[OV2 + k * H + j] * h1[j];
             z2[k] = z;
-            h2[k] = z > 0 ? z : 0;
+            h2[k] = clamp01(z);
             yhat += w[OV3 + k] * h2[k];
         }
         const double err = yhat - ys[p];
@@ -452,22 +455,19 @@ void orc_mlp_grad(const float* params, const float* xs, const float* ys, std::si
         g[OB3] += gy;
         for (int k = 0; k < H; ++k) {
             g[OV3 + k] += gy * h2[k];
-            d2[k] = z2[k] > 0 ? gy * w[OV3 + k] : 0;
+            d2[k] = inside(z2[k]) ? gy * w[OV3 + k] : 0;
             g[OB2 + k] += d2[k];
             for (int j = 0; j < H; ++j) g[OV2 + k * H + j] += d2[k] * h1[j];
         }
         for (int j = 0; j < H; ++j) {
             double s = 0;
             for (int k = 0; k < H; ++k) s += d2[k] * w[OV2 + k * H + j];
-            d1[j] = z1[j] > 0 ? s : 0;
-            g[OV1 + j] += d1[j] * x;
-            g[OB1 + j] += d1[j];
+            const double d1 = inside(z1[j]) ? s : 0;
+            g[OV1 + j] += d1 * d[j];
+            g[OB1 + j] += d1;
         }
     }
-    for (int i = 0; i < NP; ++i) {
-        const bool is_w = i < OB1 || (i >= OV2 && i < OB2) || (i >= OV3 && i < OB3);
-        grad[i] = (float)(is_w ? g[i] * 2.0 * params[i] : g[i]);
-    }
+    for (int i = 0; i < NP; ++i) grad[i] = (float)(is_w(i) ? g[i] * w[i] : g[i]);
     *loss = l / (double)m;
 }
 

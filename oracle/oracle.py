@@ -62,7 +62,7 @@ def lib():
         L.orc_hardware_threads.restype = i
         L.orc_std_segmented_sort.argtypes = [vp, vp, sz, i, i, i, vp, sz, i]
         L.orc_std_segmented_scan.argtypes = [vp, vp, sz, i, i, vp, i, vp, sz]
-        L.orc_mlp_grad.argtypes = [vp, vp, vp, sz, i, vp, C.POINTER(C.c_double)]
+        L.orc_mlp_grad.argtypes = [vp, vp, C.c_float, vp, vp, sz, i, vp, C.POINTER(C.c_double)]
         L.orc_std_reduce_by_key.argtypes = [vp, i, vp, sz, vp, vp, vp, vp]
         L.orc_std_reduce_by_key.restype = sz
         _lib = L
@@ -194,14 +194,16 @@ def lognormal_segments(num_segments: int, median: float, sigma: float, lo: int, 
     return off.astype(np.uint32)
 
 
-def mlp_grad(params: np.ndarray, xs: np.ndarray, ys: np.ndarray, hidden: int = 32):
+def mlp_grad(params: np.ndarray, centres: np.ndarray, inv_span: float, keys: np.ndarray, ys: np.ndarray,
+             hidden: int = 32):
     """Gradient (raw parameters) and loss of the learned-CDF network, in double."""
     p = np.ascontiguousarray(params, dtype=np.float32)
-    x = np.ascontiguousarray(xs, dtype=np.float32)
+    c = np.ascontiguousarray(centres, dtype=np.uint32)
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
     y = np.ascontiguousarray(ys, dtype=np.float32)
     g = np.zeros_like(p)
     loss = C.c_double(0)
-    lib().orc_mlp_grad(_p(p), _p(x), _p(y), x.size, hidden, _p(g), C.byref(loss))
+    lib().orc_mlp_grad(_p(p), _p(c), C.c_float(inv_span), _p(k), _p(y), k.size, hidden, _p(g), C.byref(loss))
     return g, loss.value
 
 

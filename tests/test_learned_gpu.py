@@ -1,24 +1,42 @@
 """Learned-CDF sort on the GPU: the network's gradients against the CPU
 oracle, output bit-identical to the plain radix sort, the gain of the trained
-network over bucketing without it, and the fallback on a monotonicity
-violation."""
+network over bucketing without it, and the fallback to the plain radix sort
+for a deliberately bad network."""
 import numpy as np
 import pytest
 from helpers import learned_mixture
 
 pytestmark = pytest.mark.gpu
 
+H = 32
 
-def test_mlp_gradients_match_oracle(ctx, gbc, orc):
-    rng = np.random.default_rng(1)
-    npar = gbc.learned_param_count()
-    params = rng.uniform(0.05, 0.6, npar).astype(np.float32)
-    params[32:64] = rng.uniform(-1, 0, 32)  # b1: ramps inside [0, 1]
-    xs = rng.uniform(0, 1, 3000).astype(np.float32)
-    ys = np.sort(rng.uniform(0, 1, 3000)).astype(np.float32)
-    g_gpu, loss_gpu = gbc.learned_mlp_gradients(ctx, params, xs, ys)
-    g_cpu, loss_cpu = orc.mlp_grad(params, xs, ys)
-    # fp32 on the GPU against double on the host: relative 1e-3 of the largest
+
+def network_case(rng, m):
+    """Random parameters near the data-driven initialisation, so that most
+    units sit inside their linear range, and m points."""
+    keys = np.sort(rng.integers(0, 1 << 32, m, dtype=np.uint64)).astype(np.uint32)
+    q = keys[np.minimum(np.arange(H + 1) * m // H, m - 1)].astype(np.int64)
+    centres = (q[:-1] + (q[1:] - q[:-1]) // 2).astype(np.uint32)
+    span = float(max(int(keys[-1]) - int(keys[0]), 1))
+    width = np.maximum(q[1:] - q[:-1], 1).astype(np.float64)
+    p = np.zeros(4 * H + H * H + 1, dtype=np.float32)
+    p[0:H] = np.log(span / width) + rng.uniform(-1.0, 0.0, H)            # v1
+    p[H:2 * H] = rng.uniform(0.3, 0.7, H)                                 # b1
+    p[2 * H:2 * H + H * H] = np.log(rng.uniform(0.01, 0.05, H * H))       # v2
+    p[2 * H + H * H:3 * H + H * H] = rng.uniform(-0.4, 0.0, H)            # b2
+    p[3 * H + H * H:4 * H + H * H] = np.log(rng.uniform(0.5, 1.5, H) / H)  # v3
+    p[-1] = 0.01
+    ys = ((np.arange(m) + 0.5) / m).astype(np.float32)
+    return p, centres, np.float32(1.0 / span), keys, ys
+
+
+@pytest.mark.parametrize("m", [3000, 70001])
+def test_mlp_gradients_match_oracle(ctx, gbc, orc, m):
+    p, c, inv_span, keys, ys = network_case(np.random.default_rng(m), m)
+    g_gpu, loss_gpu = gbc.learned_mlp_gradients(ctx, p, c, inv_span, keys, ys)
+    g_cpu, loss_cpu = orc.mlp_grad(p, c, inv_span, keys, ys)
+    assert np.count_nonzero(g_cpu) > 0.9 * g_cpu.size  # most units are active
+    # fp32 on the GPU against double on the host: 1e-3 of the largest entry
     scale = np.max(np.abs(g_cpu))
     assert np.max(np.abs(g_gpu - g_cpu)) <= 1e-3 * scale
     assert abs(loss_gpu - loss_cpu) <= 1e-4 * max(loss_cpu, 1e-6)
@@ -52,33 +70,67 @@ def test_learned_sort_is_bit_identical_to_plain(ctx, gbc, n):
 
 
 def test_trained_network_beats_bucketing_without_it(ctx, gbc):
-    # The method without the network buckets by the normalised key alone; the
-    # fitted CDF spreads the mixture's keys far more evenly, so fewer keys
-    # land in buckets too large for one CTA's shared-memory sort.
+    # Without the network the keys are bucketed by equal-width ranges of the
+    # key domain; the mixture's narrow clusters then fill a few buckets far
+    # beyond one CTA's shared-memory sort. The fitted CDF spreads them.
     keys = learned_mixture(1 << 22, seed=11)
-    opts = dict(buckets=4096, grid=4096)
+    opts = dict(buckets=4096)
     out_l, st_l = learned(ctx, gbc, keys, **opts)
     out_u, st_u = learned(ctx, gbc, keys, use_model=0, **opts)
-    assert np.array_equal(out_l.view(np.uint32), out_u.view(np.uint32))
-    assert st_l.largest_bucket < st_u.largest_bucket
-    assert st_l.oversized_keys < st_u.oversized_keys
-    assert st_l.nonempty_buckets > st_u.nonempty_buckets
+    out_0, st_0 = learned(ctx, gbc, keys, steps=0, **opts)  # initialised, not trained
+    ref = plain_sort(ctx, gbc, keys).view(np.uint32)
+    for out in (out_l, out_u, out_0):
+        assert np.array_equal(out.view(np.uint32), ref)
+    assert st_l.fallback == 0
+    assert st_u.oversized_keys > keys.size // 2   # without the network most keys are in oversized buckets
+    assert st_l.oversized_keys * 4 < st_u.oversized_keys
+    assert st_l.largest_bucket * 4 < st_u.largest_bucket
+    assert st_l.nonempty_buckets > 2 * st_u.nonempty_buckets
+    # training lowers the fit error of the initialised network
+    assert st_l.last_loss < 0.5 * st_l.first_loss
 
 
 @pytest.mark.parametrize("dtype", [np.uint32, np.int32])
 def test_learned_integer_keys_and_small_sizes(ctx, gbc, dtype):
     rng = np.random.default_rng(3)
-    for n in (2, 5, 4097, 300000):
+    for n in (2, 5, 255, 4097, 300000):
         keys = rng.integers(np.iinfo(dtype).min, np.iinfo(dtype).max, size=n, dtype=np.int64).astype(dtype)
         keys[::9] = keys[0]
         out, st = learned(ctx, gbc, keys, sample=min(n, 1 << 16))
         assert np.array_equal(out, np.sort(keys))
 
 
-def test_monotonicity_violation_falls_back(ctx, gbc):
+def test_bad_network_falls_back_to_plain_sort(ctx, gbc):
+    # Every weight ~ 0: the network's CDF is flat, every splitter lands past
+    # the largest sampled key and all keys would share one bucket; the sample
+    # estimate sends the input to the plain radix sort.
     keys = learned_mixture(1 << 20, seed=2)
-    grid = 1024
-    bad = np.linspace(1.0, 0.0, grid + 1).astype(np.float32)  # a decreasing CDF
-    out, st = learned(ctx, gbc, keys, grid=grid, table_in=bad.ctypes.data)
-    assert st.violation == 1 and st.fallback == 1
+    bad = np.zeros(gbc.learned_param_count(), dtype=np.float32)
+    bad[0:H] = -30.0
+    bad[2 * H:2 * H + H * H] = -30.0
+    bad[3 * H + H * H:4 * H + H * H] = -30.0
+    out, st = learned(ctx, gbc, keys, steps=0, params_in=bad.ctypes.data)
+    assert st.fallback == 1 and st.estimated_oversized_keys > keys.size // 2
     assert np.array_equal(out.view(np.uint32), plain_sort(ctx, gbc, keys).view(np.uint32))
+
+
+def ordered_u32(keys):
+    k = keys.view(np.uint32)
+    return np.where(k >> 31 == 1, ~k, k | np.uint32(0x80000000)).astype(np.uint32)
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_given_splitters_any_order_stays_exact(ctx, gbc, reverse):
+    # The bucket of a key is a binary search over the splitters, monotone in
+    # the key for any splitter array: even an unsorted one cannot break order.
+    keys = learned_mixture(1 << 21, seed=9)
+    B = 4096
+    u = np.sort(ordered_u32(keys))
+    sp = u[(np.arange(1, B) * u.size) // B].astype(np.uint32)
+    if reverse:
+        sp = sp[::-1].copy()
+    out, st = learned(ctx, gbc, keys, buckets=B, splitters_in=sp.ctypes.data)
+    assert np.array_equal(out.view(np.uint32), plain_sort(ctx, gbc, keys).view(np.uint32))
+    assert st.violation == 0
+    if not reverse:
+        assert st.fallback == 0 and st.nonempty_buckets > B * 3 // 4

@@ -140,3 +140,33 @@ def test_histogram_float_rule(orc):
             b = min(int(np.float32(v - np.float32(0)) * scale), 9)
             exp[b] += 1
     assert h.tolist() == exp.tolist()
+
+
+def test_network_gradient_matches_finite_differences(orc):
+    # The oracle's analytic gradient of the learned-CDF network against
+    # central differences of its own loss (parameters in float, loss in double).
+    H = 32
+    rng = np.random.default_rng(4)
+    m = 400
+    keys = np.sort(rng.integers(0, 1 << 32, m, dtype=np.uint64)).astype(np.uint32)
+    q = keys[np.minimum(np.arange(H + 1) * m // H, m - 1)].astype(np.int64)
+    centres = (q[:-1] + (q[1:] - q[:-1]) // 2).astype(np.uint32)
+    span = float(int(keys[-1]) - int(keys[0]))
+    p = np.zeros(4 * H + H * H + 1, dtype=np.float32)
+    p[0:H] = np.log(span / np.maximum(q[1:] - q[:-1], 1)) - 0.5
+    p[H:2 * H] = rng.uniform(0.3, 0.7, H)
+    p[2 * H:2 * H + H * H] = np.log(rng.uniform(0.01, 0.05, H * H))
+    p[2 * H + H * H:3 * H + H * H] = rng.uniform(-0.4, 0.0, H)
+    p[3 * H + H * H:4 * H + H * H] = np.log(np.full(H, 1.0 / H))
+    ys = ((np.arange(m) + 0.5) / m).astype(np.float32)
+    g, _ = orc.mlp_grad(p, centres, np.float32(1.0 / span), keys, ys)
+    picks = [0, 5, H + 3, 2 * H + 7, 2 * H + 33 * 5, 2 * H + H * H + 2, 3 * H + H * H + 9, 4 * H + H * H]
+    for i in picks:
+        eps = np.float32(1e-2)
+        up, dn = p.copy(), p.copy()
+        up[i] += eps
+        dn[i] -= eps
+        _, lu = orc.mlp_grad(up, centres, np.float32(1.0 / span), keys, ys)
+        _, ld = orc.mlp_grad(dn, centres, np.float32(1.0 / span), keys, ys)
+        fd = (lu - ld) / (float(up[i]) - float(dn[i]))
+        assert abs(fd - g[i]) <= 2e-2 * max(abs(g[i]), 1e-3 * np.max(np.abs(g))), (i, fd, g[i])

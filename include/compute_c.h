@@ -247,7 +247,7 @@ typedef struct clc_learned_options {
     int points;   /* training points from the sorted sample (0: 8192) */
     int buckets;  /* partition buckets (0: about n / 8192, at least 4096, as many as shared memory holds) */
     int steps;    /* Adam steps (-1: 32) */
-    float lr;     /* Adam learning rate (0: 0.05) */
+    float lr;     /* Adam learning rate (0: 0.01) */
     int use_model;                 /* 0: equal-width buckets over the sampled key range (no network) */
     const float* params_in;        /* host, clc_learned_param_count() floats, or NULL (data-driven init) */
     float* params_out;             /* host, receives the fitted parameters, or NULL */

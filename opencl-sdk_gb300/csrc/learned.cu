@@ -637,7 +637,7 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         buckets = std::max<uint32_t>(4096, std::min<uint32_t>(want, max_buckets / 1024 * 1024));
     }
     const int steps = opt.steps >= 0 ? opt.steps : 32;
-    const float lr = opt.lr > 0 ? opt.lr : 0.05f;
+    const float lr = opt.lr > 0 ? opt.lr : 0.01f;
     const uint32_t G = train_grid(ctx, M);
     const std::size_t part_smem = part_smem_bytes(buckets);
 

@@ -17,7 +17,7 @@ struct learned_options {
     int points = 0;     // training points taken from the sorted sample (0: 8192)
     int buckets = 0;    // partition buckets (0: from n, up to what shared memory holds)
     int steps = -1;     // Adam steps (-1: 32)
-    float lr = 0.f;     // Adam learning rate (0: 0.05)
+    float lr = 0.f;     // Adam learning rate (0: 0.01)
     bool use_model = true;  // false: equal-width buckets over the sampled key range (no network)
     const float* params_in = nullptr;       // host: start from these parameters instead of the data-driven init
     float* params_out = nullptr;            // host: receives the fitted parameters

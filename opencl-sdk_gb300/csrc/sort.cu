@@ -389,240 +389,30 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 }
 
 // ---------------------------------------------------------------------------
-// K2 with bulk-copy staging: the same digit pass, but each persistent CTA
-// takes its next tile while it finishes the current one and has the TMA
-// engine copy that tile's keys (and values) into a shared-memory stage; the
-// copy overlaps the look-back and the write-out of the current tile, and the
-// loads cost no registers. Partial tiles and unaligned arrays use plain loads
-// into the same stage.
+// K2, second form. The first form executes about 4.3 warp instructions per
+// key and keeps the ALU pipe ~64% busy while DRAM runs at ~15%: it is bound
+// by instruction issue (8 ballots per row of keys) and by its look-back,
+// which walks back one tile per round trip. Here:
+//   * rows are ranked by shared-memory peer masks: each lane ORs its bit into
+//     its digit's mask word, reads the word back (its peers), and the lowest
+//     peer bumps the warp's count for the digit and clears the word.
+//     BALLOT_ROWS of every 4 rows keep the ballot form, which loads the ALU
+//     pipe instead of the shared-memory pipe;
+//   * the look-back reads LBW predecessors' status words per round trip:
+//     tiles start a few tens of nanoseconds apart, so the nearest inclusive
+//     prefix is typically several tiles back. (Handing the whole look-back to
+//     one warp, 8 digits per lane with 16-byte status loads, made the sort
+//     twice as slow, and so did taking the next tile's index early: a tile
+//     taken before the CTA can work on it publishes its counts late);
+//   * IDENT: the key transform is the identity (unsigned ascending keys).
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool MATCH, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) k_pass_tma(SortArgs<K> a, int slot)
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int BALLOT_ROWS, bool IDENT, int LBW>
+__device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
     static_assert(THREADS >= RADIX, "one thread per bin");
-
-    const uint32_t act = a.ctl->plan.num_active;
-    if (slot >= (int)act) return;
-    const uint32_t shift = a.ctl->plan.shift[slot];
-    const bool dst_out = ((act - 1 - slot) & 1) == 0;
-    K* dst_k = dst_out ? a.out_keys : a.alt_keys;
-    uint32_t* dst_v = dst_out ? a.out_vals : a.alt_vals;
-    const K* src_k;
-    const uint32_t* src_v;
-    if (slot == 0) {
-        const bool from_alt = a.in_place && (act & 1);
-        src_k = from_alt ? a.alt_keys : a.in_keys;
-        src_v = from_alt ? a.alt_vals : a.in_vals;
-    } else {
-        const bool prev_out = ((act - slot) & 1) == 0;
-        src_k = prev_out ? a.out_keys : a.alt_keys;
-        src_v = prev_out ? a.out_vals : a.alt_vals;
-    }
-    const bool aligned = ((reinterpret_cast<uintptr_t>(src_k) | reinterpret_cast<uintptr_t>(src_v)) & 15) == 0;
-
-    extern __shared__ __align__(128) unsigned char smem[];
-    K* stage_k = reinterpret_cast<K*>(smem);
-    uint32_t* stage_v = reinterpret_cast<uint32_t*>(stage_k + TILE);
-    K* s_keys = reinterpret_cast<K*>(stage_v + (HAS_V ? TILE : 0));
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
-    uint32_t* warp_hist = s_vals + (HAS_V ? TILE : 0);
-    __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
-    __shared__ uint32_t s_scratch[8];
-    __shared__ uint32_t s_next;
-    __shared__ int s_abort;
-    __shared__ __align__(8) uint64_t s_bar;
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
-    uint32_t* ctr = &a.ctl->tile_ctr[slot];
-    const uint32_t n = a.n;
-    auto bulk_tile = [&](uint32_t t) { return aligned && (uint64_t)(t + 1) * TILE <= n; };
-    auto issue = [&](uint32_t t) {  // one thread
-        constexpr uint32_t KB = TILE * sizeof(K), VB = HAS_V ? TILE * 4 : 0;
-        dev::fence_proxy_async();
-        dev::mbar_arrive_expect_tx(&s_bar, KB + VB);
-        dev::bulk_g2s(stage_k, src_k + (size_t)t * TILE, KB, &s_bar);
-        if (HAS_V) dev::bulk_g2s(stage_v, src_v + (size_t)t * TILE, VB, &s_bar);
-    };
-    if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
-    if (tid == 0) {
-        s_abort = 0;
-        dev::mbar_init(&s_bar, 1);
-        dev::fence_mbar_init();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const uint32_t t = atomicAdd(ctr, 1u);
-        s_next = t;
-        if (t < a.num_tiles && bulk_tile(t)) issue(t);
-    }
-    uint32_t phase = 0;
-
-    for (;;) {
-        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
-        __syncthreads();
-        const uint32_t t = s_next;
-        if (t >= a.num_tiles) break;
-        const uint32_t tile_base = t * TILE;
-        const uint32_t valid = min((uint32_t)TILE, n - tile_base);
-        if (bulk_tile(t)) {
-            if (!dev::mbar_wait_bounded(&s_bar, phase)) {
-                dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                s_abort = 1;
-            }
-            phase ^= 1;
-        } else {
-            for (uint32_t i = tid; i < valid; i += THREADS) {
-                stage_k[i] = src_k[tile_base + i];
-                if (HAS_V) stage_v[i] = src_v[tile_base + i];
-            }
-            __syncthreads();
-        }
-
-        const uint32_t wlocal = warp * 32 * ITEMS + lane;
-        K key[ITEMS];
-        uint32_t rd[ITEMS];
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t li = wlocal + i * 32;
-            if (li < valid) {
-                key[i] = stage_k[li];
-                rd[i] = (uint32_t)(a.xf(key[i]) >> shift) & 0xFFu;
-            } else {
-                key[i] = 0;
-                rd[i] = 0xFFu;
-            }
-        }
-        uint32_t* wh = warp_hist + warp * RADIX;
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i];
-            uint32_t peers;
-            if (MATCH) {
-                peers = __match_any_sync(FULL_MASK, d);
-            } else {
-                peers = FULL_MASK;
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    const uint32_t bit = (d >> b) & 1u;
-                    const uint32_t vote = __ballot_sync(FULL_MASK, bit);
-                    peers &= bit ? vote : ~vote;
-                }
-            }
-            const int leader = 31 - __clz(peers);
-            uint32_t before = 0;
-            if (lane == leader) {
-                before = wh[d];
-                wh[d] = before + __popc(peers);
-            }
-            before = __shfl_sync(FULL_MASK, before, leader);
-            rd[i] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
-            __syncwarp();
-        }
-        __syncthreads();
-
-        uint32_t count = 0;
-        if (tid < RADIX) {
-#pragma unroll
-            for (int w = 0; w < WARPS; ++w) {
-                const uint32_t c = warp_hist[w * RADIX + tid];
-                warp_hist[w * RADIX + tid] = count;
-                count += c;
-            }
-        }
-        uint32_t agg = count;
-        if (tid == RADIX - 1) agg -= (uint32_t)TILE - valid;
-        uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
-        if (tid < RADIX)
-            dev::st_relaxed(&my_status[tid], pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
-        const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
-        if (tid < RADIX) s_local[tid] = local;
-        __syncthreads();
-
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i] & 0xFFu;
-            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
-            s_keys[pos] = key[i];
-            if (HAS_V) {
-                const uint32_t li = wlocal + i * 32;
-                s_vals[pos] = li < valid ? stage_v[li] : 0u;
-            }
-        }
-        __syncthreads();  // the stage is free: fetch the next tile behind the look-back
-        if (tid == 0) {
-            const uint32_t nt = atomicAdd(ctr, 1u);
-            s_next = nt;
-            if (nt < a.num_tiles && bulk_tile(nt)) issue(nt);
-        }
-
-        if (tid < RADIX) {
-            uint32_t excl = 0;
-            if (t > 0) {
-                uint64_t k = t - 1;
-                for (;;) {
-                    const uint64_t seq = seq0 + k;
-                    const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
-                    const uint64_t want = seq & TAG_MASK;
-                    uint64_t w = dev::ld_relaxed(p);
-                    bool gave_up = false;
-                    if ((w >> 62) == 0 || ((w >> 32) & TAG_MASK) != want) {
-                        const unsigned long long start = dev::globaltimer();
-                        for (uint32_t spin = 1;; ++spin) {
-                            w = dev::ld_relaxed(p);
-                            if ((w >> 62) != 0 && ((w >> 32) & TAG_MASK) == want) break;
-                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                gave_up = true;
-                                break;
-                            }
-                            if (spin > 32) __nanosleep(64);
-                        }
-                    }
-                    if (gave_up) {
-                        dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                        s_abort = 1;
-                        break;
-                    }
-                    excl += (uint32_t)w;
-                    if ((w >> 62) == FLAG_PRE || k == 0) break;
-                    --k;
-                }
-                dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + agg));
-            }
-            s_bin_off[tid] = s_bin_start[tid] + excl - s_local[tid];
-        }
-        __syncthreads();
-
-        const uint32_t limit = s_abort ? 0u : valid;
-        for (uint32_t j = tid; j < limit; j += THREADS) {
-            const K kk = s_keys[j];
-            const uint32_t d = (uint32_t)(a.xf(kk) >> shift) & 0xFFu;
-            const uint32_t o = s_bin_off[d] + j;
-            if (o < n) {
-                dst_k[o] = kk;
-                if (HAS_V) dst_v[o] = s_vals[j];
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// K2, early-publish form. The decoupled look-back's critical path is how soon
-// each tile publishes: here a tile counts its digits with shared-memory
-// atomics right after its keys arrive, publishes those counts, resolves its
-// look-back and publishes its inclusive prefix, and only then ranks its keys.
-// Successors therefore usually find an inclusive prefix one tile back. Each
-// look-back thread reads four predecessors per round trip.
-// ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) k_pass_early(SortArgs<K> a, int slot)
-{
-    constexpr int WARPS = THREADS / 32;
-    constexpr int TILE = THREADS * ITEMS;
-    static_assert(THREADS == RADIX, "one thread per bin, and bins == threads for the early counts");
+    static_assert(TILE < (1 << 24), "rank and digit share a word");
 
     const uint32_t act = a.ctl->plan.num_active;
     if (slot >= (int)act) return;
@@ -643,146 +433,175 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_early(SortArgs<K> a, int
     }
 
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256
-    K* s_keys = reinterpret_cast<K*>(warp_hist + WARPS * RADIX);
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256 running counts
+    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256 peer masks
+    K* s_keys = reinterpret_cast<K*>(warp_mask + WARPS * RADIX);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
-    __shared__ uint32_t s_count[RADIX], s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
+    __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
     __shared__ uint32_t s_scratch[8];
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_next;
     __shared__ int s_abort;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
-    if (tid == 0) s_abort = 0;
+    const uint32_t lt_mask = dev::lanemask_lt();
+    auto digit = [&](K k) -> uint32_t { return (uint32_t)((IDENT ? k : a.xf(k)) >> shift) & 0xFFu; };
+    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
+    if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
     uint32_t* ctr = &a.ctl->tile_ctr[slot];
     const uint32_t n = a.n;
+    if (tid == 0) s_abort = 0;
 
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(ctr, 1u);
-        s_count[tid] = 0;
+        if (tid == 0) s_next = atomicAdd(ctr, 1u);
         for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
-        const uint32_t t = s_tile;
+        const uint32_t t = s_next;
         if (t >= a.num_tiles) break;
         const uint32_t tile_base = t * TILE;
         const uint32_t valid = min((uint32_t)TILE, n - tile_base);
 
+        // Load: row i of warp w is keys tile_base + w*32*ITEMS + 32*i + lane.
+        // Past the end the digit is 255, so padding ranks last.
         const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
         K key[ITEMS];
         uint32_t rd[ITEMS];
+        uint32_t val[HAS_V ? ITEMS : 1];
+        if (valid == (uint32_t)TILE) {
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t idx = wbase + i * 32;
-            if (idx < n) {
-                key[i] = src_k[idx];
-                rd[i] = (uint32_t)(a.xf(key[i]) >> shift) & 0xFFu;
-                atomicAdd(&s_count[rd[i]], 1u);
-            } else {
-                key[i] = 0;
-                rd[i] = 0xFFu;  // padding ranks last, uncounted
+            for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * 32];
+            if (HAS_V) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) val[i] = src_v[wbase + i * 32];
             }
-        }
-        __syncthreads();
-
-        // Publish this tile's counts, then its inclusive prefix.
-        const uint32_t count = s_count[tid];
-        uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
-        dev::st_relaxed(&my_status[tid], pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, count));
-        uint32_t excl = 0;
-        if (t > 0) {
-            int64_t k = (int64_t)t - 1;
-            bool done = false;
-            while (!done) {
-                uint64_t w[4];
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    w[j] = k - j >= 0 ? dev::ld_relaxed(a.ring + ((seq0 + k - j) & (RING_TILES - 1)) * RADIX + tid) : 0;
-#pragma unroll
-                for (int j = 0; j < 4 && !done; ++j) {
-                    const uint64_t seq = seq0 + (uint64_t)(k - j);
-                    const uint64_t want = seq & TAG_MASK;
-                    uint64_t x = w[j];
-                    if ((x >> 62) == 0 || ((x >> 32) & TAG_MASK) != want) {
-                        const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
-                        const unsigned long long start = dev::globaltimer();
-                        for (uint32_t spin = 1;; ++spin) {
-                            x = dev::ld_relaxed(p);
-                            if ((x >> 62) != 0 && ((x >> 32) & TAG_MASK) == want) break;
-                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                                s_abort = 1;
-                                x = FLAG_PRE << 62;
-                                break;
-                            }
-                            if (spin > 16) __nanosleep(32);
-                        }
-                    }
-                    excl += (uint32_t)x;
-                    if ((x >> 62) == FLAG_PRE || k - j == 0) done = true;
-                }
-                k -= 4;
-            }
-            dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + count));
-        }
-        const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
-        s_local[tid] = local;
-        s_bin_off[tid] = s_bin_start[tid] + excl - local;
-
-        // Rank within each warp, row by row (= input order).
-        uint32_t* wh = warp_hist + warp * RADIX;
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i];
-            uint32_t peers = FULL_MASK;
-#pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const uint32_t bit = (d >> b) & 1u;
-                const uint32_t vote = __ballot_sync(FULL_MASK, bit);
-                peers &= bit ? vote : ~vote;
-            }
-            const int leader = 31 - __clz(peers);
-            uint32_t before = 0;
-            if (lane == leader) {
-                before = wh[d];
-                wh[d] = before + __popc(peers);
-            }
-            before = __shfl_sync(FULL_MASK, before, leader);
-            rd[i] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
-            __syncwarp();
-        }
-        __syncthreads();
-        {   // exclusive prefix over warps, plus the digit's local start
-            uint32_t run = s_local[tid];
-#pragma unroll
-            for (int w = 0; w < WARPS; ++w) {
-                const uint32_t c = warp_hist[w * RADIX + tid];
-                warp_hist[w * RADIX + tid] = run;
-                run += c;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i] & 0xFFu;
-            const uint32_t pos = warp_hist[warp * RADIX + d] + (rd[i] >> 8);
-            s_keys[pos] = key[i];
-            rd[i] = pos;
-        }
-        if (HAS_V) {
+            for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
+        } else {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const uint32_t idx = wbase + i * 32;
-                s_vals[rd[i]] = idx < n ? src_v[idx] : 0u;
+                const bool in = idx < n;
+                key[i] = in ? src_k[idx] : K(0);
+                if (HAS_V) val[i] = in ? src_v[idx] : 0u;
+                rd[i] = in ? digit(key[i]) : 0xFFu;
             }
+        }
+
+        // Rank within the warp, row by row (= input order).
+        uint32_t* wh = warp_hist + warp * RADIX;
+        uint32_t* wm = warp_mask + warp * RADIX;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i];
+            const bool by_ballot = (i & 3) < BALLOT_ROWS;
+            uint32_t peers;
+            if (by_ballot) {
+                peers = FULL_MASK;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t bit = (d >> b) & 1u;
+                    const uint32_t vote = __ballot_sync(FULL_MASK, bit);
+                    peers &= bit ? vote : ~vote;
+                }
+            } else {
+                atomicOr(&wm[d], 1u << lane);
+                __syncwarp();
+                peers = wm[d];
+            }
+            const uint32_t before = wh[d];
+            __syncwarp();
+            const uint32_t lower = peers & lt_mask;
+            if (lower == 0) {  // the lowest peer updates the digit's words
+                wh[d] = before + __popc(peers);
+                if (!by_ballot) wm[d] = 0;
+            }
+            __syncwarp();
+            rd[i] = ((before + __popc(lower)) << 8) | d;
         }
         __syncthreads();
 
+        // Per-digit tile counts; warp_hist becomes the exclusive prefix over warps.
+        uint32_t count = 0;
+        if (tid < RADIX) {
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t c = warp_hist[w * RADIX + tid];
+                warp_hist[w * RADIX + tid] = count;
+                count += c;
+            }
+        }
+        uint32_t agg = count;
+        if (tid == RADIX - 1) agg -= (uint32_t)TILE - valid;  // padding sits in bin 255
+        uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
+        if (tid < RADIX)
+            dev::st_relaxed(&my_status[tid], pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
+        const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
+        if (tid < RADIX) s_local[tid] = local;
+        __syncthreads();
+
+        // Local sort of the tile into shared memory.
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i] & 0xFFu;
+            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
+            s_keys[pos] = key[i];
+            if (HAS_V) s_vals[pos] = val[i];
+        }
+
+        // Decoupled look-back, one thread per digit, LBW status words per
+        // round trip.
+        if (tid < RADIX) {
+            uint32_t excl = 0;
+            if (t > 0) {
+                int64_t k = (int64_t)t - 1;
+                bool done = false;
+                while (!done) {
+                    uint64_t w[LBW];
+#pragma unroll
+                    for (int j = 0; j < LBW; ++j)
+                        if (k - j >= 0)
+                            w[j] = dev::ld_relaxed(a.ring + ((seq0 + (uint64_t)(k - j)) & (RING_TILES - 1)) * RADIX +
+                                                   tid);
+#pragma unroll
+                    for (int j = 0; j < LBW; ++j) {
+                        if (done || k - j < 0) break;
+                        const uint64_t seq = seq0 + (uint64_t)(k - j);
+                        const uint64_t want = seq & TAG_MASK;
+                        uint64_t x = w[j];
+                        if ((x >> 62) == 0 || ((x >> 32) & TAG_MASK) != want) {
+                            const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
+                            const unsigned long long start = dev::globaltimer();
+                            for (uint32_t spin = 1;; ++spin) {
+                                x = dev::ld_relaxed(p);
+                                if ((x >> 62) != 0 && ((x >> 32) & TAG_MASK) == want) break;
+                                if ((spin & 63) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                    dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                                    s_abort = 1;
+                                    x = FLAG_PRE << 62;  // stop walking
+                                    break;
+                                }
+                                __nanosleep(spin < 16 ? 32 : 128);
+                            }
+                        }
+                        excl += (uint32_t)x;
+                        if ((x >> 62) == FLAG_PRE) done = true;
+                    }
+                    k -= LBW;
+                    if (k < 0) done = true;
+                }
+                dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + agg));
+            }
+            s_bin_off[tid] = s_bin_start[tid] + excl - s_local[tid];
+        }
+        __syncthreads();
+
+        // Write the locally sorted tile (runs of equal digits go to
+        // consecutive addresses). After a timed-out wait the offsets are
+        // unknown: nothing is written.
         const uint32_t limit = s_abort ? 0u : valid;
         for (uint32_t j = tid; j < limit; j += THREADS) {
             const K kk = s_keys[j];
-            const uint32_t d = (uint32_t)(a.xf(kk) >> shift) & 0xFFu;
-            const uint32_t o = s_bin_off[d] + j;
+            const uint32_t o = s_bin_off[digit(kk)] + j;
             if (o < n) {
                 dst_k[o] = kk;
                 if (HAS_V) dst_v[o] = s_vals[j];
@@ -792,37 +611,45 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_early(SortArgs<K> a, int
     }
 }
 
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int BALLOT_ROWS, bool IDENT, int MINB, int LBW>
+__global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
+{
+    pass2_body<K, HAS_V, THREADS, ITEMS, BALLOT_ROWS, IDENT, LBW>(a, slot);
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 template <typename K> struct PassVariant {
     int threads, items;
-    bool match;  // __match_any_sync ranking (else 8 ballots)
-    bool tma;    // bulk-copy staged tiles (k_pass_tma)
-    void (*kernel)(SortArgs<K>, int);
+    bool masks;                              // the second form (peer-mask words in shared memory)
+    void (*kernel)(SortArgs<K>, int);        // any key transform
+    void (*kernel_ident)(SortArgs<K>, int);  // identity transform (unsigned ascending)
 };
 
 template <typename K, bool HAS_V> struct Variants;
 
 // Variant 0 is the default when the tuning table has no entry; the order
-// below puts the fastest measured shape first.
-#define GBC_PV(K, HV, T, I, M) PassVariant<K>{T, I, M, false, &k_pass<K, HV, T, I, M>}
-#define GBC_PT(K, HV, T, I, M, B) PassVariant<K>{T, I, M, true, &k_pass_tma<K, HV, T, I, M, B>}
-#define GBC_PE(K, HV, I, B) PassVariant<K>{256, I, false, false, &k_pass_early<K, HV, 256, I, B>}
-#define GBC_PM(K, HV, T, I, B) PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>}
+// below puts the fastest measured shape first (keys only and key-value
+// differ).
+#define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
+#define GBC_P1B(K, HV, T, I, B) \
+    PassVariant<K>{T, I, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
+#define GBC_P2(K, HV, T, I, BR, B, W) \
+    PassVariant<K>{T, I, true, &k_pass2<K, HV, T, I, BR, false, B, W>, &k_pass2<K, HV, T, I, BR, true, B, W>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
-            GBC_PV(uint32_t, HV, 256, 16, false),
-            GBC_PV(uint32_t, HV, 256, 16, true),
-            GBC_PM(uint32_t, HV, 256, 16, 3),
-            GBC_PM(uint32_t, HV, 256, 12, 4),
-            GBC_PM(uint32_t, HV, 256, 8, 5),
-            GBC_PE(uint32_t, HV, 12, 4),
-            GBC_PT(uint32_t, HV, 512, 12, false, 1),
-            GBC_PM(uint32_t, HV, 256, 20, 2),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 0, 2, 1) : GBC_P2(uint32_t, HV, 256, 24, 0, 2, 8),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 0, 2, 8) : GBC_P2(uint32_t, HV, 256, 24, 0, 2, 1),
+            GBC_P2(uint32_t, HV, 256, 16, 0, 3, 8),
+            GBC_P2(uint32_t, HV, 256, 16, 1, 3, 1),
+            GBC_P2(uint32_t, HV, 256, 32, 0, 2, 4),
+            GBC_P2(uint32_t, HV, 256, 20, 0, 2, 4),
+            GBC_P1(uint32_t, HV, 256, 16, false),
+            GBC_P1B(uint32_t, HV, 256, 16, 3),
         };
         return v[std::min(std::max(i, 0), count - 1)];
     }
@@ -832,25 +659,24 @@ template <bool HV> struct Variants<uint64_t, HV> {
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
-            GBC_PV(uint64_t, HV, 256, 12, false),
-            GBC_PV(uint64_t, HV, 256, 12, true),
-            GBC_PE(uint64_t, HV, 12, 2),
-            GBC_PE(uint64_t, HV, 8, 3),
-            GBC_PT(uint64_t, HV, 256, 12, false, 2),
+            GBC_P2(uint64_t, HV, 256, 12, 0, 2, 1),
+            GBC_P2(uint64_t, HV, 256, 12, 0, 2, 8),
+            GBC_P2(uint64_t, HV, 256, 8, 0, 3, 4),
+            GBC_P1(uint64_t, HV, 256, 12, false),
+            GBC_P1(uint64_t, HV, 256, 12, true),
         };
         return v[std::min(std::max(i, 0), count - 1)];
     }
 };
-#undef GBC_PV
-#undef GBC_PT
-#undef GBC_PE
-#undef GBC_PM
+#undef GBC_P1
+#undef GBC_P1B
+#undef GBC_P2
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {
     const std::size_t tile = (std::size_t)pv.threads * pv.items;
     const std::size_t one = tile * sizeof(K) + (has_v ? tile * 4 : 0);  // a tile of keys (+ values)
-    return (std::size_t)(pv.threads / 32) * RADIX * 4 + one * (pv.tma ? 2 : 1);
+    return (std::size_t)(pv.threads / 32) * RADIX * 4 * (pv.masks ? 2 : 1) + one;
 }
 
 struct KernelInfo {
@@ -936,11 +762,13 @@ static void run_sort(device_context& ctx, const K* in_k, K* out_k, const uint32_
 
     // K2 x P
     const std::size_t psmem = pass_smem<K>(pv, HAS_V);
-    const int pblocks = prepare_kernel(pv.kernel, pv.threads, psmem, g_occupancy, g_occupancy_mutex);
+    const bool ident = xf.a == 0 && xf.b == 0;
+    auto* pk = ident ? pv.kernel_ident : pv.kernel;
+    const int pblocks = prepare_kernel(pk, pv.threads, psmem, g_occupancy, g_occupancy_mutex);
     const int pgrid = (int)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * pblocks);
     for (int s = 0; s < P; ++s) {
         kernel_timer kt(ctx, "sort.digit_pass");
-        pv.kernel<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
+        pk<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
         check_cuda(cudaGetLastError(), "radix sort pass launch");
     }
 }

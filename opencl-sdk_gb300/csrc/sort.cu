@@ -394,10 +394,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 // by instruction issue (8 ballots per row of keys) and by its look-back,
 // which walks back one tile per round trip. Here:
 //   * rows are ranked by shared-memory peer masks: each lane ORs its bit into
-//     its digit's mask word, reads the word back (its peers), and the lowest
-//     peer bumps the warp's count for the digit and clears the word.
-//     BALLOT_ROWS of every 4 rows keep the ballot form, which loads the ALU
-//     pipe instead of the shared-memory pipe;
+//     its digit's mask word and reads the word back (its peers); GROUP rows
+//     use GROUP mask arrays, so their round trips overlap, and the running
+//     per-digit count is kept by one atomicAdd (with return) per peer set;
 //   * the look-back reads LBW predecessors' status words per round trip:
 //     tiles start a few tens of nanoseconds apart, so the nearest inclusive
 //     prefix is typically several tiles back. (Handing the whole look-back to
@@ -406,7 +405,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     taken before the CTA can work on it publishes its counts late);
 //   * IDENT: the key transform is the identity (unsigned ascending keys).
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int BALLOT_ROWS, bool IDENT, int LBW>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int GROUP, bool IDENT, int LBW, bool STAGED>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
@@ -434,32 +433,73 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256 running counts
-    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256 peer masks
-    K* s_keys = reinterpret_cast<K*>(warp_mask + WARPS * RADIX);
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // GROUP x WARPS x 256 peer masks
+    // One tile of keys (+ values); STAGED: two, the next tile's bulk copy
+    // landing in one while the current tile is worked on in the other.
+    unsigned char* tiles = reinterpret_cast<unsigned char*>(warp_mask + GROUP * WARPS * RADIX);
+    constexpr uint32_t KEY_BYTES = TILE * sizeof(K), VAL_BYTES = HAS_V ? TILE * 4 : 0;
+    constexpr uint32_t STAGE_BYTES = KEY_BYTES + VAL_BYTES;
     __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
     __shared__ uint32_t s_scratch[8];
-    __shared__ uint32_t s_next;
     __shared__ int s_abort;
+    __shared__ uint32_t s_stage_tile[2];
+    __shared__ int s_inflight[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lt_mask = dev::lanemask_lt();
     auto digit = [&](K k) -> uint32_t { return (uint32_t)((IDENT ? k : a.xf(k)) >> shift) & 0xFFu; };
-    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
+    for (int i = tid; i < GROUP * WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
     if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
     uint32_t* ctr = &a.ctl->tile_ctr[slot];
     const uint32_t n = a.n;
-    if (tid == 0) s_abort = 0;
+    // Bulk copies need 16-byte aligned sources; a partial last tile is loaded
+    // by plain loads.
+    const bool aligned =
+        STAGED && ((reinterpret_cast<uintptr_t>(src_k) | (HAS_V ? reinterpret_cast<uintptr_t>(src_v) : 0)) & 15) == 0;
+    auto bulk_ok = [&](uint32_t tt) { return aligned && tt < a.num_tiles && (uint64_t)(tt + 1) * TILE <= n; };
+    auto issue = [&](int st, uint32_t tt) {  // one thread
+        s_stage_tile[st] = tt;
+        if (!STAGED || s_abort || !bulk_ok(tt)) return;
+        unsigned char* dst = tiles + st * STAGE_BYTES;
+        dev::fence_proxy_async();
+        dev::mbar_arrive_expect_tx(&s_bar[st], STAGE_BYTES);
+        dev::bulk_g2s(dst, src_k + (size_t)tt * TILE, KEY_BYTES, &s_bar[st]);
+        if (HAS_V) dev::bulk_g2s(dst + KEY_BYTES, src_v + (size_t)tt * TILE, VAL_BYTES, &s_bar[st]);
+        s_inflight[st] = 1;
+    };
+    if (tid == 0) {
+        s_abort = 0;
+        s_inflight[0] = s_inflight[1] = 0;
+        if (STAGED) {
+            dev::mbar_init(&s_bar[0], 1);
+            dev::mbar_init(&s_bar[1], 1);
+            dev::fence_mbar_init();
+        }
+        issue(0, atomicAdd(ctr, 1u));
+    }
+    int st = 0;
+    uint32_t parity = 0;  // bit s: phase parity of stage s's barrier
 
     for (;;) {
-        if (tid == 0) s_next = atomicAdd(ctr, 1u);
+        if (STAGED && tid == 0) issue(st ^ 1, atomicAdd(ctr, 1u));  // the next tile's copy
         for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
-        const uint32_t t = s_next;
+        const uint32_t t = s_stage_tile[st];
         if (t >= a.num_tiles) break;
         const uint32_t tile_base = t * TILE;
         const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+        K* s_keys = reinterpret_cast<K*>(tiles + (STAGED ? st : 0) * STAGE_BYTES);
+        uint32_t* s_vals = reinterpret_cast<uint32_t*>(tiles + (STAGED ? st : 0) * STAGE_BYTES + KEY_BYTES);
+        const bool staged = s_inflight[st] != 0;
+        if (staged) {
+            if (!dev::mbar_wait_bounded(&s_bar[st], (parity >> st) & 1u)) {
+                dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                s_abort = 1;
+            }
+            parity ^= 1u << st;
+        }
 
         // Load: row i of warp w is keys tile_base + w*32*ITEMS + 32*i + lane.
         // Past the end the digit is 255, so padding ranks last.
@@ -467,7 +507,17 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         K key[ITEMS];
         uint32_t rd[ITEMS];
         uint32_t val[HAS_V ? ITEMS : 1];
-        if (valid == (uint32_t)TILE) {
+        if (staged) {
+            const uint32_t lb = warp * 32 * ITEMS + lane;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[lb + i * 32];
+            if (HAS_V) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[lb + i * 32];
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
+        } else if (valid == (uint32_t)TILE) {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * 32];
             if (HAS_V) {
@@ -487,36 +537,35 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             }
         }
 
-        // Rank within the warp, row by row (= input order).
+        // Rank within the warp (= input order), GROUP rows at a time: every
+        // row of a group ORs its lane bits into its own mask array, so the
+        // group's peer sets come back after one round trip; then the lowest
+        // peer of each row adds the row's count to the warp's running count
+        // for the digit and gets the count before it, rows in order.
         uint32_t* wh = warp_hist + warp * RADIX;
-        uint32_t* wm = warp_mask + warp * RADIX;
+        static_assert(ITEMS % GROUP == 0, "whole groups of rows");
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i];
-            const bool by_ballot = (i & 3) < BALLOT_ROWS;
-            uint32_t peers;
-            if (by_ballot) {
-                peers = FULL_MASK;
+        for (int i0 = 0; i0 < ITEMS; i0 += GROUP) {
+            uint32_t peers[GROUP];
 #pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    const uint32_t bit = (d >> b) & 1u;
-                    const uint32_t vote = __ballot_sync(FULL_MASK, bit);
-                    peers &= bit ? vote : ~vote;
+            for (int g = 0; g < GROUP; ++g) atomicOr(&warp_mask[(g * WARPS + warp) * RADIX + rd[i0 + g]], 1u << lane);
+            __syncwarp();
+#pragma unroll
+            for (int g = 0; g < GROUP; ++g) peers[g] = warp_mask[(g * WARPS + warp) * RADIX + rd[i0 + g]];
+            __syncwarp();
+#pragma unroll
+            for (int g = 0; g < GROUP; ++g) {
+                const uint32_t d = rd[i0 + g];
+                const uint32_t lower = peers[g] & lt_mask;
+                uint32_t before = 0;
+                if (lower == 0) {
+                    before = atomicAdd(&wh[d], (uint32_t)__popc(peers[g]));
+                    warp_mask[(g * WARPS + warp) * RADIX + d] = 0;
                 }
-            } else {
-                atomicOr(&wm[d], 1u << lane);
-                __syncwarp();
-                peers = wm[d];
+                __syncwarp();  // orders the rows' additions
+                before = __shfl_sync(FULL_MASK, before, __ffs(peers[g]) - 1);
+                rd[i0 + g] = ((before + __popc(lower)) << 8) | d;
             }
-            const uint32_t before = wh[d];
-            __syncwarp();
-            const uint32_t lower = peers & lt_mask;
-            if (lower == 0) {  // the lowest peer updates the digit's words
-                wh[d] = before + __popc(peers);
-                if (!by_ballot) wm[d] = 0;
-            }
-            __syncwarp();
-            rd[i] = ((before + __popc(lower)) << 8) | d;
         }
         __syncthreads();
 
@@ -596,25 +645,54 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         __syncthreads();
 
         // Write the locally sorted tile (runs of equal digits go to
-        // consecutive addresses). After a timed-out wait the offsets are
-        // unknown: nothing is written.
+        // consecutive addresses); unstaged, the next tile's index is fetched
+        // meanwhile. After a timed-out wait the offsets are unknown: nothing
+        // is written.
+        if (!STAGED && tid == 0) s_stage_tile[0] = atomicAdd(ctr, 1u);
         const uint32_t limit = s_abort ? 0u : valid;
-        for (uint32_t j = tid; j < limit; j += THREADS) {
-            const K kk = s_keys[j];
-            const uint32_t o = s_bin_off[digit(kk)] + j;
-            if (o < n) {
-                dst_k[o] = kk;
-                if (HAS_V) dst_v[o] = s_vals[j];
+        if (limit == (uint32_t)TILE) {
+            uint32_t o[ITEMS];
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[tid + i * THREADS];
+            if (HAS_V) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[tid + i * THREADS];
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) o[i] = s_bin_off[digit(key[i])] + tid + i * THREADS;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                if (o[i] < n) {
+                    dst_k[o[i]] = key[i];
+                    if (HAS_V) dst_v[o[i]] = val[i];
+                }
+            }
+        } else {
+            for (uint32_t j = tid; j < limit; j += THREADS) {
+                const K kk = s_keys[j];
+                const uint32_t o = s_bin_off[digit(kk)] + j;
+                if (o < n) {
+                    dst_k[o] = kk;
+                    if (HAS_V) dst_v[o] = s_vals[j];
+                }
             }
         }
+        if (tid == 0) s_inflight[st] = 0;
         __syncthreads();
+        if (STAGED) st ^= 1;
+    }
+    // A copy whose wait gave up may still be landing: let it finish (bounded)
+    // before the CTA's shared memory is released.
+    if (STAGED && tid == 0) {
+        for (int q = 0; q < 2; ++q)
+            if (s_inflight[q]) dev::mbar_wait_bounded(&s_bar[q], (parity >> q) & 1u);
     }
 }
 
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int BALLOT_ROWS, bool IDENT, int MINB, int LBW>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int GROUP, bool IDENT, int MINB, int LBW, bool STAGED>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, BALLOT_ROWS, IDENT, LBW>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, GROUP, IDENT, LBW, STAGED>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -622,7 +700,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot
 // ---------------------------------------------------------------------------
 template <typename K> struct PassVariant {
     int threads, items;
-    bool masks;                              // the second form (peer-mask words in shared memory)
+    int groups;                              // second form: mask arrays (rows ranked together); 0: first form
+    bool staged;                             // second form: next tile bulk-copied into a second stage
     void (*kernel)(SortArgs<K>, int);        // any key transform
     void (*kernel_ident)(SortArgs<K>, int);  // identity transform (unsigned ascending)
 };
@@ -632,22 +711,22 @@ template <typename K, bool HAS_V> struct Variants;
 // Variant 0 is the default when the tuning table has no entry; the order
 // below puts the fastest measured shape first (keys only and key-value
 // differ).
-#define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
+#define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, 0, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
 #define GBC_P1B(K, HV, T, I, B) \
-    PassVariant<K>{T, I, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
-#define GBC_P2(K, HV, T, I, BR, B, W) \
-    PassVariant<K>{T, I, true, &k_pass2<K, HV, T, I, BR, false, B, W>, &k_pass2<K, HV, T, I, BR, true, B, W>}
+    PassVariant<K>{T, I, 0, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
+#define GBC_P2(K, HV, T, I, G, B, W, S)                                                           \
+    PassVariant<K>{T, I, G, S, &k_pass2<K, HV, T, I, G, false, B, W, S>, &k_pass2<K, HV, T, I, G, true, B, W, S>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 0, 2, 1) : GBC_P2(uint32_t, HV, 256, 24, 0, 2, 8),
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 0, 2, 8) : GBC_P2(uint32_t, HV, 256, 24, 0, 2, 1),
-            GBC_P2(uint32_t, HV, 256, 16, 0, 3, 8),
-            GBC_P2(uint32_t, HV, 256, 16, 1, 3, 1),
-            GBC_P2(uint32_t, HV, 256, 32, 0, 2, 4),
-            GBC_P2(uint32_t, HV, 256, 20, 0, 2, 4),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, false) : GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, true),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, true) : GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, false),
+            GBC_P2(uint32_t, HV, 256, 24, 2, 2, 4, true),
+            GBC_P2(uint32_t, HV, 256, 16, 1, 3, 4, true),
+            GBC_P2(uint32_t, HV, 256, 24, 1, 2, 1, false),
+            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 1, 4, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 1, 4, true),
             GBC_P1(uint32_t, HV, 256, 16, false),
             GBC_P1B(uint32_t, HV, 256, 16, 3),
         };
@@ -659,9 +738,9 @@ template <bool HV> struct Variants<uint64_t, HV> {
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
-            GBC_P2(uint64_t, HV, 256, 12, 0, 2, 1),
-            GBC_P2(uint64_t, HV, 256, 12, 0, 2, 8),
-            GBC_P2(uint64_t, HV, 256, 8, 0, 3, 4),
+            GBC_P2(uint64_t, HV, 256, 12, 1, 2, 4, false),
+            GBC_P2(uint64_t, HV, 256, 12, 1, 2, 4, true),
+            GBC_P2(uint64_t, HV, 256, 8, 1, 3, 4, false),
             GBC_P1(uint64_t, HV, 256, 12, false),
             GBC_P1(uint64_t, HV, 256, 12, true),
         };
@@ -676,7 +755,7 @@ template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v
 {
     const std::size_t tile = (std::size_t)pv.threads * pv.items;
     const std::size_t one = tile * sizeof(K) + (has_v ? tile * 4 : 0);  // a tile of keys (+ values)
-    return (std::size_t)(pv.threads / 32) * RADIX * 4 * (pv.masks ? 2 : 1) + one;
+    return (std::size_t)(pv.threads / 32) * RADIX * 4 * (1 + pv.groups) + one * (pv.staged ? 2 : 1);
 }
 
 struct KernelInfo {
@@ -715,7 +794,8 @@ static void run_sort(device_context& ctx, const K* in_k, K* out_k, const uint32_
                      uint32_t* out_v, std::size_t n, dev::KeyXform<K> xf, int variant)
 {
     constexpr int P = Traits<K>::PASSES;
-    const PassVariant<K> pv = Variants<K, HAS_V>::get(variant);
+    PassVariant<K> pv = Variants<K, HAS_V>::get(variant);
+    if (pass_smem<K>(pv, HAS_V) + 8192 > ctx.smem_optin) pv = Variants<K, HAS_V>::get(0);
     const uint32_t tile = (uint32_t)(pv.threads * pv.items);
     const uint32_t num_tiles = (uint32_t)((n + tile - 1) / tile);
     const bool in_place = (const void*)in_k == (const void*)out_k;

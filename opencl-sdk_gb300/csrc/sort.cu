@@ -394,9 +394,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 // by instruction issue (8 ballots per row of keys) and by its look-back,
 // which walks back one tile per round trip. Here:
 //   * rows are ranked by shared-memory peer masks: each lane ORs its bit into
-//     its digit's mask word and reads the word back (its peers); GROUP rows
-//     use GROUP mask arrays, so their round trips overlap, and the running
-//     per-digit count is kept by one atomicAdd (with return) per peer set;
+//     its digit's mask word and reads the word back (its peers); the lowest
+//     peer bumps the warp's count and clears the word (keeping the rows of a
+//     group in separate mask arrays to overlap their round trips measured no
+//     faster, and packing mask and count into one 64-bit word slower);
+//   * each warp's place offset per digit already includes the digit's start
+//     in the tile, so placing a key costs one shared-memory lookup;
 //   * the look-back reads LBW predecessors' status words per round trip:
 //     tiles start a few tens of nanoseconds apart, so the nearest inclusive
 //     prefix is typically several tiles back. (Handing the whole look-back to
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     taken before the CTA can work on it publishes its counts late);
 //   * IDENT: the key transform is the identity (unsigned ascending keys).
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int GROUP, bool IDENT, int LBW, bool STAGED>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
@@ -432,11 +435,13 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256 running counts
-    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // GROUP x WARPS x 256 peer masks
+    // Per warp and digit: the running count (then the place offset) and the
+    // current row's peer mask.
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256
+    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256
     // One tile of keys (+ values); STAGED: two, the next tile's bulk copy
     // landing in one while the current tile is worked on in the other.
-    unsigned char* tiles = reinterpret_cast<unsigned char*>(warp_mask + GROUP * WARPS * RADIX);
+    unsigned char* tiles = reinterpret_cast<unsigned char*>(warp_mask + WARPS * RADIX);
     constexpr uint32_t KEY_BYTES = TILE * sizeof(K), VAL_BYTES = HAS_V ? TILE * 4 : 0;
     constexpr uint32_t STAGE_BYTES = KEY_BYTES + VAL_BYTES;
     __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
@@ -449,7 +454,7 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lt_mask = dev::lanemask_lt();
     auto digit = [&](K k) -> uint32_t { return (uint32_t)((IDENT ? k : a.xf(k)) >> shift) & 0xFFu; };
-    for (int i = tid; i < GROUP * WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
+    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
     if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
     uint32_t* ctr = &a.ctl->tile_ctr[slot];
@@ -537,39 +542,32 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             }
         }
 
-        // Rank within the warp (= input order), GROUP rows at a time: every
-        // row of a group ORs its lane bits into its own mask array, so the
-        // group's peer sets come back after one round trip; then the lowest
-        // peer of each row adds the row's count to the warp's running count
-        // for the digit and gets the count before it, rows in order.
+        // Rank within the warp, row by row (= input order): every lane ORs its
+        // bit into its digit's mask word and reads the word back (its peers)
+        // and the warp's count of the digit in earlier rows; the lowest peer
+        // stores the new count and clears the mask.
         uint32_t* wh = warp_hist + warp * RADIX;
-        static_assert(ITEMS % GROUP == 0, "whole groups of rows");
+        uint32_t* wm = warp_mask + warp * RADIX;
 #pragma unroll
-        for (int i0 = 0; i0 < ITEMS; i0 += GROUP) {
-            uint32_t peers[GROUP];
-#pragma unroll
-            for (int g = 0; g < GROUP; ++g) atomicOr(&warp_mask[(g * WARPS + warp) * RADIX + rd[i0 + g]], 1u << lane);
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = rd[i];
+            atomicOr(&wm[d], 1u << lane);
             __syncwarp();
-#pragma unroll
-            for (int g = 0; g < GROUP; ++g) peers[g] = warp_mask[(g * WARPS + warp) * RADIX + rd[i0 + g]];
+            const uint32_t peers = wm[d];
+            const uint32_t before = wh[d];
             __syncwarp();
-#pragma unroll
-            for (int g = 0; g < GROUP; ++g) {
-                const uint32_t d = rd[i0 + g];
-                const uint32_t lower = peers[g] & lt_mask;
-                uint32_t before = 0;
-                if (lower == 0) {
-                    before = atomicAdd(&wh[d], (uint32_t)__popc(peers[g]));
-                    warp_mask[(g * WARPS + warp) * RADIX + d] = 0;
-                }
-                __syncwarp();  // orders the rows' additions
-                before = __shfl_sync(FULL_MASK, before, __ffs(peers[g]) - 1);
-                rd[i0 + g] = ((before + __popc(lower)) << 8) | d;
+            const uint32_t lower = peers & lt_mask;
+            if (lower == 0) {
+                wh[d] = before + __popc(peers);
+                wm[d] = 0;
             }
+            __syncwarp();
+            rd[i] = ((before + __popc(lower)) << 8) | d;
         }
         __syncthreads();
 
-        // Per-digit tile counts; warp_hist becomes the exclusive prefix over warps.
+        // Per-digit tile counts; warp_hist becomes each warp's place offsets
+        // (exclusive over warps, plus the digit's start within the tile).
         uint32_t count = 0;
         if (tid < RADIX) {
 #pragma unroll
@@ -585,14 +583,17 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         if (tid < RADIX)
             dev::st_relaxed(&my_status[tid], pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
         const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
-        if (tid < RADIX) s_local[tid] = local;
+        if (tid < RADIX) {
+            s_local[tid] = local;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) warp_hist[w * RADIX + tid] += local;
+        }
         __syncthreads();
 
         // Local sort of the tile into shared memory.
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i] & 0xFFu;
-            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
+            const uint32_t pos = warp_hist[warp * RADIX + (rd[i] & 0xFFu)] + (rd[i] >> 8);
             s_keys[pos] = key[i];
             if (HAS_V) s_vals[pos] = val[i];
         }
@@ -689,10 +690,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 }
 
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int GROUP, bool IDENT, int MINB, int LBW, bool STAGED>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, GROUP, IDENT, LBW, STAGED>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -700,7 +701,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot
 // ---------------------------------------------------------------------------
 template <typename K> struct PassVariant {
     int threads, items;
-    int groups;                              // second form: mask arrays (rows ranked together); 0: first form
+    bool second;                             // second form (k_pass2)
     bool staged;                             // second form: next tile bulk-copied into a second stage
     void (*kernel)(SortArgs<K>, int);        // any key transform
     void (*kernel_ident)(SortArgs<K>, int);  // identity transform (unsigned ascending)
@@ -711,22 +712,22 @@ template <typename K, bool HAS_V> struct Variants;
 // Variant 0 is the default when the tuning table has no entry; the order
 // below puts the fastest measured shape first (keys only and key-value
 // differ).
-#define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, 0, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
+#define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
 #define GBC_P1B(K, HV, T, I, B) \
-    PassVariant<K>{T, I, 0, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
-#define GBC_P2(K, HV, T, I, G, B, W, S)                                                           \
-    PassVariant<K>{T, I, G, S, &k_pass2<K, HV, T, I, G, false, B, W, S>, &k_pass2<K, HV, T, I, G, true, B, W, S>}
+    PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
+#define GBC_P2(K, HV, T, I, B, W, S) \
+    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S>, &k_pass2<K, HV, T, I, true, B, W, S>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, false) : GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, true),
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, true) : GBC_P2(uint32_t, HV, 256, 24, 1, 2, 4, false),
-            GBC_P2(uint32_t, HV, 256, 24, 2, 2, 4, true),
-            GBC_P2(uint32_t, HV, 256, 16, 1, 3, 4, true),
-            GBC_P2(uint32_t, HV, 256, 24, 1, 2, 1, false),
-            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 1, 4, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 1, 4, true),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, false),
+            GBC_P2(uint32_t, HV, 256, 16, 3, 4, true),
+            GBC_P2(uint32_t, HV, 256, 20, 2, 4, false),
+            GBC_P2(uint32_t, HV, 256, 24, 2, 1, false),
+            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 4, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 4, true),
             GBC_P1(uint32_t, HV, 256, 16, false),
             GBC_P1B(uint32_t, HV, 256, 16, 3),
         };
@@ -738,9 +739,9 @@ template <bool HV> struct Variants<uint64_t, HV> {
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
-            GBC_P2(uint64_t, HV, 256, 12, 1, 2, 4, false),
-            GBC_P2(uint64_t, HV, 256, 12, 1, 2, 4, true),
-            GBC_P2(uint64_t, HV, 256, 8, 1, 3, 4, false),
+            GBC_P2(uint64_t, HV, 256, 12, 2, 4, false),
+            GBC_P2(uint64_t, HV, 256, 12, 2, 4, true),
+            GBC_P2(uint64_t, HV, 256, 8, 3, 4, false),
             GBC_P1(uint64_t, HV, 256, 12, false),
             GBC_P1(uint64_t, HV, 256, 12, true),
         };
@@ -755,7 +756,8 @@ template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v
 {
     const std::size_t tile = (std::size_t)pv.threads * pv.items;
     const std::size_t one = tile * sizeof(K) + (has_v ? tile * 4 : 0);  // a tile of keys (+ values)
-    return (std::size_t)(pv.threads / 32) * RADIX * 4 * (1 + pv.groups) + one * (pv.staged ? 2 : 1);
+    const std::size_t per_warp = pv.second ? RADIX * 8 : RADIX * 4;  // counts and peer masks, or counts
+    return (std::size_t)(pv.threads / 32) * per_warp + one * (pv.staged ? 2 : 1);
 }
 
 struct KernelInfo {

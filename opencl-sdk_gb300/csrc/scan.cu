@@ -34,6 +34,8 @@ namespace {
 using dev::FULL_MASK;
 
 constexpr int THREADS = 256;
+constexpr int LB_PER_LANE = 4;     // look-back window: 32 x 4 tiles per round trip
+constexpr int PREFETCH_GRIDS = 1;  // L2 prefetch distance, in grids of tiles (2 measured slower)
 constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
 constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
 
@@ -124,7 +126,7 @@ template <typename T> __device__ __forceinline__ void store_wide(void* dst, T v)
 
 template <typename T> struct ScanShape {
     static constexpr int VEC = 16 / sizeof(T);
-    static constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
+    static constexpr int ROWS = 8;
     static constexpr int TILE = THREADS * VEC * ROWS;
     static constexpr int RW = ROWS * (THREADS / 32);
     static constexpr int PER = RW / 32;
@@ -136,7 +138,8 @@ template <typename T> struct ScanShape {
 // barriers: every thread of the CTA calls it.
 template <typename T, typename Op, bool WIDE_SUM>
 __device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape<T>::ROWS][ScanShape<T>::VEC],
-                                          uint32_t t, uint32_t base, bool full, T* s_rw, T& s_prefix)
+                                          uint32_t t, uint32_t base, bool full, T* s_rw, T& s_prefix,
+                                          unsigned long long& wide)
 {
     constexpr int VEC = ScanShape<T>::VEC;
     constexpr int ROWS = ScanShape<T>::ROWS;
@@ -146,21 +149,18 @@ __device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape
     const T identity = a.identity;
 
     if (WIDE_SUM) {
-        // Exact sum of the valid elements, widened, one atomic per warp.
-        unsigned long long s = 0;
+        // Exact sum of the valid elements, widened (mod 2^64), accumulated by
+        // the thread over all its tiles and added once at the kernel's end.
 #pragma unroll
         for (int r = 0; r < ROWS; ++r)
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
                 const uint32_t idx = base + (r * THREADS + tid) * VEC + j;
                 if (idx < a.n) {
-                    if (std::is_signed<T>::value) s += (unsigned long long)(long long)x[r][j];
-                    else s += (unsigned long long)x[r][j];
+                    if (std::is_signed<T>::value) wide += (unsigned long long)(long long)x[r][j];
+                    else wide += (unsigned long long)x[r][j];
                 }
             }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o);
-        if (lane == 0) atomicAdd(a.wide_sum, s);
     }
 
     // Per-row warp scans of the thread totals.
@@ -195,44 +195,63 @@ __device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape
         const uint64_t my_seq = a.seq0 + t;
         if (lane == 0) Status<T>::publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
 
-        // Warp-cooperative look-back: lane l inspects tile w_end-32+l;
-        // the nearest tile holding an inclusive prefix ends the walk.
+        // Warp-cooperative look-back over windows of 32 * LB_PER_LANE
+        // preceding tiles (lane l inspects LB_PER_LANE consecutive ones); the
+        // nearest tile holding an inclusive prefix ends the walk. Tiles start
+        // a few nanoseconds apart, so that prefix is typically a hundred or
+        // more tiles back: a wide window finds it in one or two round trips.
         T excl = identity;
         if (t > 0) {
             bool have = false;
             int64_t w_end = t;
+            bool gave_up = false;
             for (;;) {
-                const int64_t k = w_end - 32 + lane;
-                uint64_t flag = FLAG_PRE;
-                T val = identity;
-                bool gave_up = false;
-                if (k >= 0) {
-                    if (!Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) {
+                uint64_t flag[LB_PER_LANE];
+                T val[LB_PER_LANE];
+#pragma unroll
+                for (int q = 0; q < LB_PER_LANE; ++q) {
+                    const int64_t k = w_end - 32 * LB_PER_LANE + lane * LB_PER_LANE + q;
+                    flag[q] = FLAG_PRE;  // before tile 0: an empty inclusive prefix
+                    val[q] = identity;
+                    if (k >= 0 && !Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag[q], val[q])) {
                         const unsigned long long start = dev::globaltimer();
                         for (uint32_t spin = 1;; ++spin) {
-                            if (Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag, val)) break;
+                            if (Status<T>::read(a.ring, a.seq0 + (uint64_t)k, flag[q], val[q])) break;
                             if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
                                 gave_up = true;
-                                flag = FLAG_PRE;
-                                val = identity;
+                                flag[q] = FLAG_PRE;
+                                val[q] = identity;
                                 break;
                             }
                             if (spin > 32) __nanosleep(64);
                         }
                     }
                 }
-                if (__any_sync(FULL_MASK, gave_up)) {
-                    if (lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                int hi = -1;  // this lane's nearest inclusive prefix
+#pragma unroll
+                for (int q = 0; q < LB_PER_LANE; ++q)
+                    if (flag[q] == FLAG_PRE) hi = q;
+                const uint32_t pre = __ballot_sync(FULL_MASK, hi >= 0);
+                const int L = pre ? 31 - __clz(pre) : -1;
+                // This lane's part of the window, in sequence order.
+                T contrib = identity;
+                bool any = false;
+                if (lane >= L) {
+                    const int q0 = lane == L ? hi : 0;
+#pragma unroll
+                    for (int q = 0; q < LB_PER_LANE; ++q) {
+                        if (q < q0) continue;
+                        contrib = any ? op(contrib, val[q]) : val[q];
+                        any = true;
+                    }
                 }
-                const uint32_t pre = __ballot_sync(FULL_MASK, flag == FLAG_PRE);
-                const int L = pre ? 31 - __clz(pre) : 0;
-                const T contrib = lane >= L ? val : identity;
                 const T wsum = dev::warp_reduce(contrib, op);
                 excl = have ? op(wsum, excl) : wsum;
                 have = true;
                 if (pre) break;
-                w_end -= 32;
+                w_end -= 32 * LB_PER_LANE;
             }
+            if (__any_sync(FULL_MASK, gave_up) && lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
             if (lane == 0) Status<T>::publish(a.ring, my_seq, FLAG_PRE, op(excl, agg));
         }
         if (lane == 0) s_prefix = excl;
@@ -271,16 +290,28 @@ __device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape
     }
 }
 
+// Latency-bound: each SM needs several tiles in flight, so the register
+// budget is capped for 4 CTAs per SM (2 for 8-byte elements).
 template <typename T, typename Op, bool WIDE_SUM>
-__global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
+__global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 4 : 2) k_scan(ScanArgs<T> a)
 {
     using S = ScanShape<T>;
     __shared__ T s_rw[S::RW];
     __shared__ T s_prefix;
     __shared__ uint32_t s_tile;
     const int tid = threadIdx.x;
+    unsigned long long wide = 0;
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(a.tile_ctr, 1u);
+        // The tile index is taken only when the CTA can start on it (taking
+        // it earlier delays its status, measured slower). The tile
+        // PREFETCH_GRIDS grids further on, which a CTA will take about that
+        // many tile-times from now, is prefetched into L2.
+        if (tid == 0) {
+            s_tile = atomicAdd(a.tile_ctr, 1u);
+            const uint64_t ahead = (uint64_t)s_tile + PREFETCH_GRIDS * gridDim.x;
+            if (a.aligned && (ahead + 1) * S::TILE <= a.n)
+                dev::prefetch_l2(a.in + ahead * S::TILE, S::TILE * sizeof(T));
+        }
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= a.num_tiles) break;
@@ -302,74 +333,13 @@ __global__ void __launch_bounds__(THREADS) k_scan(ScanArgs<T> a)
                     x[r][j] = idx < a.n ? a.in[idx] : a.identity;
                 }
         }
-        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix);
+        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix, wide);
         __syncthreads();
     }
-}
-
-// The same scan with bulk-copy staging: while a CTA finishes tile t, the TMA
-// engine already copies its next tile into a shared-memory stage, so the
-// loads overlap the look-back and the stores.
-template <typename T, typename Op, bool WIDE_SUM>
-__global__ void __launch_bounds__(THREADS) k_scan_staged(ScanArgs<T> a)
-{
-    using S = ScanShape<T>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    T* stage = reinterpret_cast<T*>(smem_raw);
-    __shared__ T s_rw[S::RW];
-    __shared__ T s_prefix;
-    __shared__ uint32_t s_next;
-    __shared__ __align__(8) uint64_t s_bar;
-    const int tid = threadIdx.x;
-    auto bulk_tile = [&](uint32_t t) { return a.aligned && (uint64_t)(t + 1) * S::TILE <= a.n; };
-    auto issue = [&](uint32_t t) {
-        dev::fence_proxy_async();
-        dev::mbar_arrive_expect_tx(&s_bar, S::TILE * sizeof(T));
-        dev::bulk_g2s(stage, a.in + (size_t)t * S::TILE, S::TILE * sizeof(T), &s_bar);
-    };
-    if (tid == 0) {
-        dev::mbar_init(&s_bar, 1);
-        dev::fence_mbar_init();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const uint32_t t = atomicAdd(a.tile_ctr, 1u);
-        s_next = t;
-        if (t < a.num_tiles && bulk_tile(t)) issue(t);
-    }
-    __syncthreads();
-    uint32_t phase = 0;
-    for (;;) {
-        const uint32_t t = s_next;
-        if (t >= a.num_tiles) break;
-        const uint32_t base = t * S::TILE;
-        const bool full = base + S::TILE <= a.n;
-        T x[S::ROWS][S::VEC];
-        if (bulk_tile(t)) {
-            if (!dev::mbar_wait_bounded(&s_bar, phase)) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-            phase ^= 1;
+    if (WIDE_SUM) {
 #pragma unroll
-            for (int r = 0; r < S::ROWS; ++r) {
-                const uint4 w = *reinterpret_cast<const uint4*>(stage + (r * THREADS + tid) * S::VEC);
-                memcpy(x[r], &w, 16);
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < S::ROWS; ++r)
-#pragma unroll
-                for (int j = 0; j < S::VEC; ++j) {
-                    const uint32_t idx = base + (r * THREADS + tid) * S::VEC + j;
-                    x[r][j] = idx < a.n ? a.in[idx] : a.identity;
-                }
-        }
-        __syncthreads();  // stage consumed: fetch the next tile behind this one
-        if (tid == 0) {
-            const uint32_t nt = atomicAdd(a.tile_ctr, 1u);
-            s_next = nt;
-            if (nt < a.num_tiles && bulk_tile(nt)) issue(nt);
-        }
-        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix);
-        __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(FULL_MASK, wide, o);
+        if ((tid & 31) == 0 && wide != 0) atomicAdd(a.wide_sum, wide);
     }
 }
 
@@ -405,8 +375,7 @@ struct ScanLaunch {
     template <typename T, typename Op> void run()
     {
         constexpr int VEC = 16 / sizeof(T);
-        constexpr int ROWS = sizeof(T) == 4 ? 4 : 8;
-        constexpr uint32_t TILE = THREADS * VEC * ROWS;
+        constexpr uint32_t TILE = ScanShape<T>::TILE;
         constexpr bool can_wide = std::is_integral<T>::value && sizeof(T) == 4 &&
                                   std::is_same<Op, ops::Plus>::value;
         ScanArgs<T> a;
@@ -429,10 +398,9 @@ struct ScanLaunch {
         a.total = use_wide ? nullptr : total_dev;
         if (!use_wide) a.wide_sum = nullptr;
 
-        // The bulk-copy staged kernel (k_scan_staged) measured slower: a CTA
-        // that takes its next tile early publishes that tile's status late,
-        // which stalls every successor's look-back. The direct-load kernel is
-        // the default.
+        // A bulk-copy staged form of this kernel measured slower: a CTA that
+        // takes its next tile early publishes that tile's status late, which
+        // stalls every successor's look-back.
         auto kernel = use_wide ? &k_scan<T, Op, can_wide> : &k_scan<T, Op, false>;
         const std::size_t smem = 0;
         const int grid =
@@ -457,7 +425,7 @@ void selftest_lookback_timeout(device_context& ctx)
     // up, record ERR_LOOKBACK_TIMEOUT and let the kernel finish. Every access
     // stays inside the two-tile buffer.
     ctx.activate();
-    constexpr uint32_t TILE = THREADS * 16;
+    constexpr uint32_t TILE = ScanShape<int32_t>::TILE;
     temp_buffer buf(ctx.resource, 2 * TILE * sizeof(int32_t));
     check_cuda(cudaMemsetAsync(buf.get(), 0, 2 * TILE * sizeof(int32_t), ctx.stream), "cudaMemsetAsync");
     unsigned char* ctl = ctx.d_small;
@@ -515,9 +483,9 @@ void scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t,
 // ---------------------------------------------------------------------------
 namespace noalloc {
 
-constexpr uint32_t TILE = THREADS * 16;  // the int32 tile of k_scan
-constexpr uint32_t MAX_TILES = 1u << 16;
-constexpr std::size_t MAX_ELEMENTS = (std::size_t)TILE * MAX_TILES;  // 2^28
+constexpr uint32_t TILE = ScanShape<int32_t>::TILE;  // the int32 tile of k_scan
+constexpr std::size_t MAX_ELEMENTS = std::size_t(1) << 28;
+constexpr uint32_t MAX_TILES = (uint32_t)(MAX_ELEMENTS / TILE);
 
 // [0, MAX_TILES): status word of each tile; [MAX_TILES]: the tile counter.
 static __device__ __align__(256) uint64_t scan_scratch[MAX_TILES + 32];

@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     taken before the CTA can work on it publishes its counts late);
 //   * IDENT: the key transform is the identity (unsigned ascending keys).
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
@@ -461,8 +461,9 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     const uint32_t n = a.n;
     // Bulk copies need 16-byte aligned sources; a partial last tile is loaded
     // by plain loads.
-    const bool aligned =
-        STAGED && ((reinterpret_cast<uintptr_t>(src_k) | (HAS_V ? reinterpret_cast<uintptr_t>(src_v) : 0)) & 15) == 0;
+    const bool aligned_src =
+        ((reinterpret_cast<uintptr_t>(src_k) | (HAS_V ? reinterpret_cast<uintptr_t>(src_v) : 0)) & 15) == 0;
+    const bool aligned = STAGED && aligned_src;
     auto bulk_ok = [&](uint32_t tt) { return aligned && tt < a.num_tiles && (uint64_t)(tt + 1) * TILE <= n; };
     auto issue = [&](int st, uint32_t tt) {  // one thread
         s_stage_tile[st] = tt;
@@ -489,6 +490,15 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 
     for (;;) {
         if (STAGED && tid == 0) issue(st ^ 1, atomicAdd(ctr, 1u));  // the next tile's copy
+        if (PREFETCH && tid == 0) {
+            // The tile a grid further on, which some CTA takes about one
+            // tile-time from now, is prefetched into L2.
+            const uint64_t ahead = (uint64_t)s_stage_tile[STAGED ? st ^ 1 : 0] + gridDim.x;
+            if (ahead < a.num_tiles && (ahead + 1) * TILE <= n && aligned_src) {
+                dev::prefetch_l2(src_k + ahead * TILE, TILE * sizeof(K));
+                if (HAS_V) dev::prefetch_l2(src_v + ahead * TILE, TILE * 4);
+            }
+        }
         for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
         const uint32_t t = s_stage_tile[st];
@@ -690,10 +700,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 }
 
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -715,19 +725,19 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
 #define GBC_P1B(K, HV, T, I, B) \
     PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
-#define GBC_P2(K, HV, T, I, B, W, S) \
-    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S>, &k_pass2<K, HV, T, I, true, B, W, S>}
+#define GBC_P2(K, HV, T, I, B, W, S, PF) \
+    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF>, &k_pass2<K, HV, T, I, true, B, W, S, PF>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true),
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, false),
-            GBC_P2(uint32_t, HV, 256, 16, 3, 4, true),
-            GBC_P2(uint32_t, HV, 256, 20, 2, 4, false),
-            GBC_P2(uint32_t, HV, 256, 24, 2, 1, false),
-            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 4, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 4, true),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, true),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, false) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, false),
+            GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true),
+            GBC_P2(uint32_t, HV, 256, 16, 3, 4, false, true),
+            GBC_P2(uint32_t, HV, 256, 20, 2, 4, false, true),
+            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 4, true, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 4, true, true),
             GBC_P1(uint32_t, HV, 256, 16, false),
             GBC_P1B(uint32_t, HV, 256, 16, 3),
         };
@@ -739,9 +749,9 @@ template <bool HV> struct Variants<uint64_t, HV> {
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
-            GBC_P2(uint64_t, HV, 256, 12, 2, 4, false),
-            GBC_P2(uint64_t, HV, 256, 12, 2, 4, true),
-            GBC_P2(uint64_t, HV, 256, 8, 3, 4, false),
+            GBC_P2(uint64_t, HV, 256, 12, 2, 4, false, true),
+            GBC_P2(uint64_t, HV, 256, 12, 2, 4, false, false),
+            GBC_P2(uint64_t, HV, 256, 8, 3, 4, false, true),
             GBC_P1(uint64_t, HV, 256, 12, false),
             GBC_P1(uint64_t, HV, 256, 12, true),
         };

@@ -281,6 +281,11 @@ def main() -> None:
         gbc.sort_raw(ctx, keys_in.data_ptr(), keys_out.data_ptr(), np.uint32, n, vals_in.data_ptr(),
                      vals_out.data_ptr())
 
+    # The project's autotuner picks the digit-pass launch shape for this
+    # workload (stored in the context's tuning table; untimed).
+    tuned_variant, _ = gbc.autotune_sort(ctx, keys_in.data_ptr(), keys_out.data_ptr(), np.uint32, n,
+                                         vals_in.data_ptr(), vals_out.data_ptr(), repetitions=2)
+
     clocks = ClockSampler(local)
     clocks.start()
     ms, prof = timed(kv_sort, args.steps, args.warmup, ("sort.",), soak_s=3.0)
@@ -349,6 +354,7 @@ def main() -> None:
         "vs_baseline": None, "dtype": "u32",
         "data": "synthetic: seeded uniform uint32 keys (torch generator on the device), uint32 values = index",
         "config": {"workload": "kv_sort_u32_uniform_n2^28", "n": n, "key": "u32", "value": "u32 (index)",
+                   "autotuned_variant": tuned_variant,
                    "step": "out-of-place stable sort_by_key through clc_sort_keys_raw",
                    "l2": "inputs (2 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
         "bitexact": bitexact,
@@ -393,6 +399,27 @@ def learned_mixture_keys(torch, n: int, seed: int):
     del a, b, c, comp
     perm = torch.randperm(n, device="cuda", generator=g)
     return keys[perm].contiguous()
+
+
+def zipf_splitmix_keys(torch, n: int, s: float, distinct: int, seed: int):
+    """n u64 keys: Zipf(s) ranks over `distinct` values (inverse CDF on the
+    device), mapped by splitmix64; u32 values uniform in [0, 2^16)."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    w = torch.arange(1, distinct + 1, device="cuda", dtype=torch.float64).pow(-s)
+    cdf = torch.cumsum(w, 0)
+    cdf /= cdf[-1].clone()
+    keys = torch.empty(n, dtype=torch.int64, device="cuda")
+    chunk = 1 << 26
+    for i in range(0, n, chunk):
+        u = torch.rand(min(chunk, n - i), device="cuda", generator=g, dtype=torch.float64)
+        r = torch.searchsorted(cdf, u).clamp_(max=distinct - 1)
+        x = r + (-7046029254386353131)  # + 0x9E3779B97F4A7C15 (wrapping)
+        x = (x ^ ((x >> 30) & ((1 << 34) - 1))) * (-4658895280553007687)  # 0xBF58476D1CE4E5B9
+        x = (x ^ ((x >> 27) & ((1 << 37) - 1))) * (-7723592293110705685)  # 0x94D049BB133111EB
+        keys[i:i + r.numel()] = x ^ ((x >> 31) & ((1 << 33) - 1))
+    vals = torch.randint(0, 1 << 16, (n,), dtype=torch.int32, device="cuda", generator=g)
+    return keys, vals
 
 
 def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, warmup) -> dict:
@@ -501,6 +528,9 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
         gbc.segmented_scan_raw(ctx, sx.data_ptr(), sy.data_ptr(), total, np.int32, off_d.data_ptr(), lens.size,
                                exclusive=True)
 
+    # the autotuner picks the one-CTA capacity for this size / segment-length class
+    seg_cap, _ = gbc.autotune_segmented_sort(ctx, sk.data_ptr(), sko.data_ptr(), np.uint64, total, off_d.data_ptr(),
+                                             lens.size, sv.data_ptr(), svo.data_ptr(), repetitions=1)
     batch()
     ctx.finish()
     graph = gbc.capture(ctx, batch)
@@ -527,12 +557,50 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ok = ok and bool(torch.equal(sy.to(torch.int64), csum - sx.to(torch.int64) - base))
     graph.release()
     entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, 32 * total, ok, prof_s,
-          {"segments": int(lens.size), "total_keys": total, "graph": True,
+          {"segments": int(lens.size), "total_keys": total, "graph": True, "autotuned_cta_capacity": seg_cap,
            "includes": "segmented sort (u64 keys + u32 values) and segmented exclusive int32 scan",
            "plain_per_array_estimate_ms": per_array_est_ms,
            "speedup_vs_per_array": per_array_est_ms / ms_seg,
            "note": "bytes: 24 B/pair (one read + one write) + 8 B/elem scan; large segments move more"})
     del sk, sv, sko, svo, sx, sy, seg_id, order, csum, base
+    torch.cuda.empty_cache()
+
+    # sort -> reduce_by_key -> 65,536-bin histogram: 2^29 u64 keys, Zipf(1.1)
+    # ranks over 2^24 distinct values mapped by splitmix64 (a bijection, so
+    # every digit varies), u32 values uniform in [0, 2^16)
+    np_ = 1 << 29
+    zk, zv = zipf_splitmix_keys(torch, np_, 1.1, 1 << 24, 6)
+    zko, zvo = torch.empty_like(zk), torch.empty_like(zv)
+    uk = torch.empty_like(zk)
+    sums = torch.empty(np_, dtype=torch.int64, device="cuda")
+    cnts = torch.empty(np_, dtype=torch.int32, device="cuda")
+    h16 = torch.empty(65536, dtype=torch.int32, device="cuda")
+    runs = []
+
+    def pipeline():
+        gbc.sort_raw(ctx, zk.data_ptr(), zko.data_ptr(), np.uint64, np_, zv.data_ptr(), zvo.data_ptr())
+        runs.append(gbc.reduce_by_key_raw(ctx, zko.data_ptr(), np.uint64, zvo.data_ptr(), np_, uk.data_ptr(),
+                                          sums.data_ptr(), cnts.data_ptr(), h16.data_ptr()))
+
+    ms_pipe, prof_pipe = timed(pipeline, max(3, steps // 5), warmup, ("sort.", "reduce_by_key"))
+    # independent check: torch's stable sort in unsigned order, run lengths, sums, bincount
+    zu = zk ^ (-2**63)
+    order = torch.sort(zu, stable=True).indices
+    sk_ref = zk[order]
+    ok = bool(torch.equal(zko, sk_ref)) and bool(torch.equal(zvo, zv[order]))
+    uniq, counts = torch.unique_consecutive(sk_ref, return_counts=True)
+    r = runs[-1]
+    ok = ok and r == uniq.numel() and bool(torch.equal(uk[:r], uniq)) and bool(torch.equal(cnts[:r].long(), counts))
+    seg = torch.repeat_interleave(torch.arange(r, device="cuda"), counts)
+    ref_sums = torch.zeros(r, dtype=torch.int64, device="cuda").index_add_(0, seg, zvo.long())
+    ok = ok and bool(torch.equal(sums[:r], ref_sums))
+    ok = ok and bool(torch.equal(torch.bincount(zk & 0xFFFF, minlength=65536).to(torch.int32), h16))
+    entry("pipeline_sort_rbk_hist_u64_zipf_n2^29", np_, "Gkeys/s", ms_pipe, 212 * np_, ok,
+          prof_pipe, {"runs": int(r), "key": "splitmix64(Zipf(1.1) rank over 2^24 values)",
+                      "values": "u32 uniform [0, 2^16)",
+                      "note": "bytes: 8 B upfront histogram + 8 digit passes x 24 B + 12 B reduce_by_key read = 212 B/key; "
+                              "the learned-CDF form is 32-bit only"})
+    del zk, zv, zko, zvo, uk, sums, cnts, zu, order, sk_ref, uniq, counts, seg, ref_sums
     torch.cuda.empty_cache()
 
     # 256-bin histogram of 2^30 uniform bytes

@@ -375,14 +375,31 @@ GBC_EXPORT clc_status clc_profile_entry(clc_context ctx, size_t index, char* nam
                                         unsigned long long* launches, double* total_ms);
 
 /* Tuning: entries of the context's table and how many compiled variants a
- * sort family has; the autotuner times them (bench-side) and stores the
- * fastest with clc_tuning_set, clc_tuning_save writes the table. */
+ * sort family has; clc_autotune_* time them and store the fastest (or set an
+ * entry with clc_tuning_set); clc_tuning_save writes the table. */
 GBC_EXPORT int clc_tuning_sort_variants(int key_bytes, int has_values);
 GBC_EXPORT clc_status clc_tuning_sort_key(int key_bytes, int has_values, size_t n, char* out,
                                           size_t out_bytes);
 GBC_EXPORT clc_status clc_tuning_set(clc_context ctx, const char* key, int variant);
 GBC_EXPORT clc_status clc_tuning_get(clc_context ctx, const char* key, int* variant);
 GBC_EXPORT clc_status clc_tuning_save(clc_context ctx, const char* path);
+
+/* Autotuner: times every compiled launch shape of the plain sort (the
+ * variants differ in threads per CTA, keys per thread, CTAs per SM, look-back
+ * window and bulk-copy staging; digits are 8 bits throughout) on the
+ * caller's device data, stores the fastest in the context's tuning table
+ * under the workload's key (element type and size class) and returns it with
+ * its time per call. keys_in must differ from keys_out, which receives the
+ * sorted keys. Blocks. */
+GBC_EXPORT clc_status clc_autotune_sort(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                        const uint32_t* vals_in, uint32_t* vals_out, size_t n, int repetitions,
+                                        int* best_variant, double* best_ms);
+/* The same for the segmented sort: the candidates are capacities of its
+ * one-CTA size class; the key adds the class of the average segment length. */
+GBC_EXPORT clc_status clc_autotune_segmented_sort(clc_context ctx, const void* keys_in, void* keys_out,
+                                                  clc_type key_type, const uint32_t* vals_in, uint32_t* vals_out,
+                                                  size_t n, const uint32_t* offsets, size_t num_segments,
+                                                  int repetitions, int* best_cta_cap, double* best_ms);
 
 #ifdef __cplusplus
 }

@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "runtime.cpp",
     "capi.cpp",
+    "autotune.cpp",
     "elementwise.cu",
     "sort.cu",
     "scan.cu",

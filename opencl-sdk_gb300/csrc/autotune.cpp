@@ -1,0 +1,123 @@
+// Autotuner (see autotune.hpp). Candidates run back to back on the context's
+// stream; each is warmed up once, then timed over `repetitions` calls with
+// CUDA events on that stream.
+#include "autotune.hpp"
+
+#include <algorithm>
+#include <stdexcept>
+
+#include "segmented.hpp"
+#include "sort_internal.hpp"
+
+namespace gbc {
+namespace {
+
+class event_pair {
+public:
+    event_pair()
+    {
+        check_cuda(cudaEventCreate(&a_), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&b_), "cudaEventCreate");
+    }
+    ~event_pair()
+    {
+        cudaEventDestroy(a_);
+        cudaEventDestroy(b_);
+    }
+    template <typename F> double time(device_context& ctx, int reps, F&& f)
+    {
+        f();  // warm-up (first-use allocations, kernel attributes)
+        check_cuda(cudaEventRecord(a_, ctx.stream), "cudaEventRecord");
+        for (int i = 0; i < reps; ++i) f();
+        check_cuda(cudaEventRecord(b_, ctx.stream), "cudaEventRecord");
+        check_cuda(cudaEventSynchronize(b_), "cudaEventSynchronize");
+        float ms = 0.f;
+        check_cuda(cudaEventElapsedTime(&ms, a_, b_), "cudaEventElapsedTime");
+        const int err = ctx.take_device_error();
+        if (err != 0) throw device_error("autotune: a candidate reported a device error", err);
+        return (double)ms / reps;
+    }
+
+private:
+    cudaEvent_t a_ = nullptr, b_ = nullptr;
+};
+
+void check_args(const void* in, const void* out, int reps)
+{
+    if (in == nullptr || out == nullptr) throw std::invalid_argument("autotune: null keys");
+    if (in == out) throw std::invalid_argument("autotune: keys_in and keys_out must differ");
+    if (reps < 1 || reps > 1000) throw std::invalid_argument("autotune: repetitions must be in [1, 1000]");
+}
+
+void pick(autotune_result& r, device_context& ctx)
+{
+    const auto it = std::min_element(r.ms.begin(), r.ms.end());
+    r.best = r.candidates[it - r.ms.begin()];
+    r.best_ms = *it;
+    launch_shape s;
+    s.variant = r.best;
+    ctx.tuning.store(r.key, s);
+}
+
+}  // namespace
+
+autotune_result autotune_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
+                              const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, int repetitions)
+{
+    check_args(keys_in, keys_out, repetitions);
+    if (key_bytes != 4 && key_bytes != 8) throw std::invalid_argument("autotune: keys must be 32 or 64 bits");
+    ctx.activate();
+    const bool kv = vals_in != nullptr;
+    autotune_result r;
+    r.key = sort_tuning_key(key_bytes, kv, n);
+    launch_shape before;
+    const bool had = ctx.tuning.lookup(r.key, before);
+    event_pair ev;
+    try {
+        for (int v = 0; v < sort_variant_count(key_bytes, kv); ++v) {
+            launch_shape s;
+            s.variant = v;
+            ctx.tuning.store(r.key, s);
+            r.candidates.push_back(v);
+            r.ms.push_back(ev.time(ctx, repetitions, [&] {
+                radix_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, false);
+            }));
+        }
+    } catch (...) {
+        if (had) ctx.tuning.store(r.key, before);
+        throw;
+    }
+    pick(r, ctx);
+    return r;
+}
+
+autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes,
+                                        int key_kind, const uint32_t* vals_in, uint32_t* vals_out, std::size_t n,
+                                        const uint32_t* offsets, std::size_t num_segments, int repetitions)
+{
+    check_args(keys_in, keys_out, repetitions);
+    if (key_bytes != 4 && key_bytes != 8) throw std::invalid_argument("autotune: keys must be 32 or 64 bits");
+    ctx.activate();
+    const bool kv = vals_in != nullptr;
+    autotune_result r;
+    r.key = segsort_tuning_key(key_bytes, kv, n, num_segments);
+    // The one-CTA class's capacity: from a quarter of the shared-memory
+    // maximum up to the maximum, in steps of 1024 keys.
+    const int cap = (int)segsort_cta_cap(key_bytes, kv);
+    for (int c = std::max(1024, cap / 4 / 1024 * 1024); c < cap; c += std::max(1024, cap / 4 / 1024 * 1024))
+        r.candidates.push_back(c);
+    r.candidates.push_back(cap);
+    event_pair ev;
+    for (int c : r.candidates) {
+        seg_options o;
+        o.cta_cap = c;
+        r.ms.push_back(ev.time(ctx, repetitions, [&] {
+            segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
+                           false, o);
+        }));
+    }
+    pick(r, ctx);
+    return r;
+}
+
+}  // namespace gbc

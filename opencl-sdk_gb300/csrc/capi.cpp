@@ -25,6 +25,7 @@
 #include <new>
 #include <string>
 
+#include "autotune.hpp"
 #include "learned.hpp"
 #include "runtime.hpp"
 #include "segmented.hpp"
@@ -987,6 +988,36 @@ clc_status clc_tuning_get(clc_context ctx, const char* key, int* variant)
         require(ctx != nullptr && key != nullptr && variant != nullptr, "clc: null argument");
         gbc::launch_shape s;
         *variant = ctx->ctx->tuning.lookup(key, s) ? s.variant : -1;
+    });
+}
+
+clc_status clc_autotune_sort(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                             const uint32_t* vals_in, uint32_t* vals_out, size_t n, int repetitions, int* best_variant,
+                             double* best_ms)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        int bytes, kind;
+        key_kind_of(key_type, bytes, kind);
+        const gbc::autotune_result r =
+            gbc::autotune_sort(*ctx->ctx, keys_in, keys_out, bytes, kind, vals_in, vals_out, n, repetitions);
+        if (best_variant != nullptr) *best_variant = r.best;
+        if (best_ms != nullptr) *best_ms = r.best_ms;
+    });
+}
+
+clc_status clc_autotune_segmented_sort(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                       const uint32_t* vals_in, uint32_t* vals_out, size_t n, const uint32_t* offsets,
+                                       size_t num_segments, int repetitions, int* best_cta_cap, double* best_ms)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        int bytes, kind;
+        key_kind_of(key_type, bytes, kind);
+        const gbc::autotune_result r = gbc::autotune_segmented_sort(
+            *ctx->ctx, keys_in, keys_out, bytes, kind, vals_in, vals_out, n, offsets, num_segments, repetitions);
+        if (best_cta_cap != nullptr) *best_cta_cap = r.best;
+        if (best_ms != nullptr) *best_ms = r.best_ms;
     });
 }
 

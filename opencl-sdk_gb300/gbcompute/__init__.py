@@ -176,6 +176,8 @@ _PROTOS = {
     "clc_learned_default_options": (None, [_vp]),
     "clc_sort_learned": (_i, [_vp, _vp, _vp, _i, _sz, _vp, _vp]),
     "clc_learned_param_count": (_i, []),
+    "clc_autotune_sort": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _i, _vp, _vp]),
+    "clc_autotune_segmented_sort": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _vp, _sz, _i, _vp, _vp]),
     "clc_learned_mlp_gradients": (_i, [_vp, _vp, _vp, C.c_float, _vp, _vp, _sz, _vp, _vp]),
     "clc_graph_begin": (_i, [_vp]),
     "clc_graph_end": (_i, [_vp, C.POINTER(_vp)]),
@@ -630,6 +632,29 @@ def sort_learned(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int,
     _raise_for(lib.clc_sort_learned(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype), n,
                                     C.byref(options) if options is not None else None, C.byref(st)))
     return st
+
+
+def autotune_sort(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int, vals_in: int = 0, vals_out: int = 0,
+                  repetitions: int = 3):
+    """Times every compiled sort variant on the given device data, stores the
+    fastest in the context's tuning table; returns (variant, ms per call)."""
+    best, ms = C.c_int(-1), C.c_double(0)
+    _raise_for(lib.clc_autotune_sort(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype),
+                                     C.c_void_p(vals_in or None), C.c_void_p(vals_out or None), n, repetitions,
+                                     C.byref(best), C.byref(ms)))
+    return best.value, ms.value
+
+
+def autotune_segmented_sort(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int, offsets: int,
+                            num_segments: int, vals_in: int = 0, vals_out: int = 0, repetitions: int = 3):
+    """Times the segmented sort's one-CTA capacities on the given device data,
+    stores the fastest; returns (capacity, ms per call)."""
+    best, ms = C.c_int(-1), C.c_double(0)
+    _raise_for(lib.clc_autotune_segmented_sort(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out),
+                                               clc_type(key_dtype), C.c_void_p(vals_in or None),
+                                               C.c_void_p(vals_out or None), n, C.c_void_p(offsets), num_segments,
+                                               repetitions, C.byref(best), C.byref(ms)))
+    return best.value, ms.value
 
 
 def learned_param_count() -> int:

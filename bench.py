@@ -54,6 +54,34 @@ def load_traffic() -> dict:
         return {}
 
 
+class ReplicaGroup:
+    """One process per GPU, each an independent replica of the workload (the
+    path does not shard: no collective on the data path). A barrier brackets
+    the timed region and the job's time is the slowest rank's."""
+
+    def __init__(self, dist, device):
+        self.dist = dist
+        self.device = device
+        self.world = dist.get_world_size() if dist is not None else 1
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max_over_ranks(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def job_rate(self, units_per_rank: float, seconds: float) -> float:
+        """Whole-job throughput: every rank's units over the slowest rank's time."""
+        return units_per_rank * self.world / seconds
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling while the workload runs."""
 
@@ -223,16 +251,9 @@ def main() -> None:
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     peak, peak_src = load_peak_gbs()
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    replicas = ReplicaGroup(dist, torch.device("cuda", local))
+    barrier = replicas.barrier
+    max_over_ranks = replicas.max_over_ranks
 
     n = args.n
     gen = torch.Generator(device="cuda")

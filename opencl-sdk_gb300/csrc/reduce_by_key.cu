@@ -26,8 +26,9 @@ namespace {
 
 using dev::FULL_MASK;
 constexpr int THREADS = 256;
-constexpr int ITEMS = 8;
+constexpr int ITEMS = 16;
 constexpr int TILE = THREADS * ITEMS;
+constexpr int LB_PER_LANE = 4;  // look-back window: 32 x 4 tiles per round trip
 constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
 constexpr uint64_t TAG_MASK = (1ull << 29) - 1;
 constexpr uint64_t HEAD_BIT = 1ull << 61;
@@ -120,15 +121,25 @@ template <typename K> struct RbkArgs {
     int* err;
 };
 
-template <typename K> __global__ void __launch_bounds__(THREADS) k_reduce_by_key(RbkArgs<K> a)
+template <typename K> __global__ void __launch_bounds__(THREADS, 2) k_reduce_by_key(RbkArgs<K> a)
 {
     __shared__ State s_warp[THREADS / 32];
     __shared__ State s_prefix;
     __shared__ uint32_t s_tile;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a.keys) | reinterpret_cast<uintptr_t>(a.vals)) & 15) == 0;
 
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(a.tile_ctr, 1u);
+        // The tile index is taken only when the CTA can start on it; the
+        // tile a grid further on is prefetched into L2 (cf. the scan).
+        if (tid == 0) {
+            s_tile = atomicAdd(a.tile_ctr, 1u);
+            const uint64_t ahead = (uint64_t)s_tile + gridDim.x;
+            if (aligned && (ahead + 1) * TILE <= a.n) {
+                dev::prefetch_l2(a.keys + ahead * TILE, TILE * sizeof(K));
+                dev::prefetch_l2(a.vals + ahead * TILE, TILE * 4);
+            }
+        }
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= a.num_tiles) break;
@@ -137,16 +148,33 @@ template <typename K> __global__ void __launch_bounds__(THREADS) k_reduce_by_key
         K key[ITEMS];
         uint32_t val[ITEMS];
         uint32_t head = 0, valid_mask = 0;
+        if (aligned && first + ITEMS <= a.n) {
+            // 128-bit loads of the thread's consecutive items
+            const uint4* kp = reinterpret_cast<const uint4*>(a.keys + first);
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t idx = first + i;
-            if (idx < a.n) {
-                key[i] = a.keys[idx];
-                val[i] = a.vals[idx];
-                valid_mask |= 1u << i;
-            } else {
-                key[i] = 0;
-                val[i] = 0;
+            for (int j = 0; j < ITEMS * (int)sizeof(K) / 16; ++j) {
+                const uint4 w = kp[j];
+                memcpy(reinterpret_cast<unsigned char*>(key) + 16 * j, &w, 16);
+            }
+            const uint4* vp = reinterpret_cast<const uint4*>(a.vals + first);
+#pragma unroll
+            for (int j = 0; j < ITEMS / 4; ++j) {
+                const uint4 w = vp[j];
+                memcpy(&val[4 * j], &w, 16);
+            }
+            valid_mask = (ITEMS == 32) ? 0xFFFFFFFFu : ((1u << ITEMS) - 1);
+        } else {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t idx = first + i;
+                if (idx < a.n) {
+                    key[i] = a.keys[idx];
+                    val[i] = a.vals[idx];
+                    valid_mask |= 1u << i;
+                } else {
+                    key[i] = 0;
+                    val[i] = 0;
+                }
             }
         }
         const K before = (first > 0 && first - 1 < a.n) ? a.keys[first - 1] : K(0);
@@ -185,34 +213,53 @@ template <typename K> __global__ void __launch_bounds__(THREADS) k_reduce_by_key
             if (lane == 0) publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
             State excl{0, 0, 0, 0};
             if (t > 0) {
-                bool have = false;
+                // Look back over windows of 32 x LB_PER_LANE tiles (lane l
+                // inspects LB_PER_LANE consecutive ones); the nearest tile with
+                // an inclusive state ends the walk.
+                bool have = false, gave_up = false;
                 int64_t w_end = t;
                 for (;;) {
-                    const int64_t k = w_end - 32 + lane;
-                    uint64_t flag = FLAG_PRE;
-                    State v{0, 0, 0, 0};
-                    if (k >= 0 && !read(a.ring, a.seq0 + (uint64_t)k, flag, v)) {
-                        const unsigned long long start = dev::globaltimer();
-                        for (uint32_t spin = 1;; ++spin) {
-                            if (read(a.ring, a.seq0 + (uint64_t)k, flag, v)) break;
-                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                                flag = FLAG_PRE;
-                                v = State{0, 0, 0, 0};
-                                break;
+                    uint64_t flag[LB_PER_LANE];
+                    State v[LB_PER_LANE];
+#pragma unroll
+                    for (int q = 0; q < LB_PER_LANE; ++q) {
+                        const int64_t k = w_end - 32 * LB_PER_LANE + lane * LB_PER_LANE + q;
+                        flag[q] = FLAG_PRE;  // before tile 0: the empty state
+                        v[q] = State{0, 0, 0, 0};
+                        if (k >= 0 && !read(a.ring, a.seq0 + (uint64_t)k, flag[q], v[q])) {
+                            const unsigned long long start = dev::globaltimer();
+                            for (uint32_t spin = 1;; ++spin) {
+                                if (read(a.ring, a.seq0 + (uint64_t)k, flag[q], v[q])) break;
+                                if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                    gave_up = true;
+                                    flag[q] = FLAG_PRE;
+                                    v[q] = State{0, 0, 0, 0};
+                                    break;
+                                }
+                                if (spin > 32) __nanosleep(64);
                             }
-                            if (spin > 32) __nanosleep(64);
                         }
                     }
-                    const uint32_t pre = __ballot_sync(FULL_MASK, flag == FLAG_PRE);
-                    const int L = pre ? 31 - __clz(pre) : 0;
-                    const State contrib = lane >= L ? v : State{0, 0, 0, 0};
+                    int hi = -1;
+#pragma unroll
+                    for (int q = 0; q < LB_PER_LANE; ++q)
+                        if (flag[q] == FLAG_PRE) hi = q;
+                    const uint32_t pre = __ballot_sync(FULL_MASK, hi >= 0);
+                    const int L = pre ? 31 - __clz(pre) : -1;
+                    State contrib{0, 0, 0, 0};
+                    if (lane >= L) {
+                        const int q0 = lane == L ? hi : 0;
+#pragma unroll
+                        for (int q = 0; q < LB_PER_LANE; ++q)
+                            if (q >= q0) contrib = combine(contrib, v[q]);
+                    }
                     const State ws = shfl(warp_incl(contrib), 31);
                     excl = have ? combine(ws, excl) : ws;
                     have = true;
                     if (pre) break;
-                    w_end -= 32;
+                    w_end -= 32 * LB_PER_LANE;
                 }
+                if (__any_sync(FULL_MASK, gave_up) && lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
                 if (lane == 0) publish(a.ring, my_seq, FLAG_PRE, combine(excl, agg));
             }
             if (lane == 0) {

@@ -745,13 +745,15 @@ template <bool HV> struct Variants<uint32_t, HV> {
     }
 };
 template <bool HV> struct Variants<uint64_t, HV> {
-    static constexpr int count = 5;
+    static constexpr int count = 7;
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
+            HV ? GBC_P2(uint64_t, HV, 256, 20, 2, 4, false, true) : GBC_P2(uint64_t, HV, 256, 24, 2, 4, false, true),
+            HV ? GBC_P2(uint64_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint64_t, HV, 256, 20, 2, 4, false, true),
+            GBC_P2(uint64_t, HV, 256, 16, 2, 4, false, true),
             GBC_P2(uint64_t, HV, 256, 12, 2, 4, false, true),
-            GBC_P2(uint64_t, HV, 256, 12, 2, 4, false, false),
-            GBC_P2(uint64_t, HV, 256, 8, 3, 4, false, true),
+            GBC_P2(uint64_t, HV, 256, 16, 2, 1, false, true),
             GBC_P1(uint64_t, HV, 256, 12, false),
             GBC_P1(uint64_t, HV, 256, 12, true),
         };

@@ -380,9 +380,13 @@ template <typename K> __global__ void __launch_bounds__(256) k_seg_large_hist(Se
     }
 }
 
-// One digit pass over every large segment's tiles (cf. onesweep::k_pass).
-template <typename K, bool HAS_V, int THREADS, int ITEMS>
-__global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int slot)
+// One digit pass over every large segment's tiles (cf. onesweep::k_pass2:
+// shared-memory peer-mask ranking, place offsets folded into the per-warp
+// counts, a look-back reading LBW predecessors per round trip, which stops at
+// the segment's first tile (it publishes an inclusive count), an L2 prefetch
+// of the tile a grid ahead and an unrolled write-out of full tiles).
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int MINB, int LBW>
+__global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, int slot)
 {
     constexpr int P = Traits<K>::PASSES;
     constexpr int WARPS = THREADS / 32;
@@ -396,21 +400,40 @@ __global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int sl
     uint32_t* dst_v = dst_out ? a.out_v : a.alt_v;
     const K* src_k = slot == 0 ? a.in_k : (dst_out ? a.alt_k : a.out_k);
     const uint32_t* src_v = slot == 0 ? a.in_v : (dst_out ? a.alt_v : a.out_v);
+    const bool aligned_src =
+        ((reinterpret_cast<uintptr_t>(src_k) | (HAS_V ? reinterpret_cast<uintptr_t>(src_v) : 0)) & 15) == 0;
 
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);
-    K* s_keys = reinterpret_cast<K*>(warp_hist + WARPS * RADIX);
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256: counts, then place offsets
+    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256 peer masks
+    K* s_keys = reinterpret_cast<K*>(warp_mask + WARPS * RADIX);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
     __shared__ uint32_t s_bin_off[RADIX], s_local[RADIX];
     __shared__ uint32_t s_scratch[8];
     __shared__ uint32_t s_tile;
     __shared__ int s_abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lt_mask = dev::lanemask_lt();
+    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
     if (tid == 0) s_abort = 0;
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.max_tiles;
+    auto digit = [&](K k) -> uint32_t { return (uint32_t)(a.xf(k) >> shift) & 0xFFu; };
 
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(&a.ctl->tile_ctr[slot], 1u);
+        if (tid == 0) {
+            s_tile = atomicAdd(&a.ctl->tile_ctr[slot], 1u);
+            // L2 prefetch of the tile a grid further on in the tile sequence
+            const uint32_t ahead = s_tile + gridDim.x;
+            if (aligned_src && ahead < num_tiles) {
+                const uint32_t ja = a.tile_seg[ahead];
+                const uint32_t sa = a.large_list[ja];
+                const uint32_t ba = a.off[sa] + (ahead - a.tile_begin[ja]) * TILE;
+                if (ba + TILE <= a.off[sa + 1] && (ba % (16 / sizeof(K))) == 0) {
+                    dev::prefetch_l2(src_k + ba, TILE * sizeof(K));
+                    if (HAS_V && (ba & 3) == 0) dev::prefetch_l2(src_v + ba, TILE * 4);
+                }
+            }
+        }
         for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
         const uint32_t t = s_tile;
@@ -426,33 +449,47 @@ __global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int sl
         const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
         K key[ITEMS];
         uint32_t rd[ITEMS];
+        uint32_t val[HAS_V ? ITEMS : 1];
+        if (valid == (uint32_t)TILE) {
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t idx = wbase + i * 32;
-            if (idx < sege) {
-                key[i] = src_k[idx];
-                rd[i] = (uint32_t)(a.xf(key[i]) >> shift) & 0xFFu;
-            } else {
-                key[i] = 0;
-                rd[i] = 0xFFu;
+            for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * 32];
+            if (HAS_V) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) val[i] = src_v[wbase + i * 32];
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t idx = wbase + i * 32;
+                const bool in = idx < sege;
+                key[i] = in ? src_k[idx] : K(0);
+                if (HAS_V) val[i] = in ? src_v[idx] : 0u;
+                rd[i] = in ? digit(key[i]) : 0xFFu;  // padding ranks last
             }
         }
+
         uint32_t* wh = warp_hist + warp * RADIX;
+        uint32_t* wm = warp_mask + warp * RADIX;
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t d = rd[i];
-            const uint32_t peers = __match_any_sync(FULL_MASK, d);
-            const int leader = 31 - __clz(peers);
-            uint32_t before = 0;
-            if (lane == leader) {
-                before = wh[d];
-                wh[d] = before + __popc(peers);
-            }
-            before = __shfl_sync(FULL_MASK, before, leader);
-            rd[i] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
+            atomicOr(&wm[d], 1u << lane);
             __syncwarp();
+            const uint32_t peers = wm[d];
+            const uint32_t before = wh[d];
+            __syncwarp();
+            const uint32_t lower = peers & lt_mask;
+            if (lower == 0) {
+                wh[d] = before + __popc(peers);
+                wm[d] = 0;
+            }
+            __syncwarp();
+            rd[i] = ((before + __popc(lower)) << 8) | d;
         }
         __syncthreads();
+
         uint32_t count = 0;
         if (tid < RADIX) {
 #pragma unroll
@@ -467,52 +504,56 @@ __global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int sl
         uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
         if (tid < RADIX) dev::st_relaxed(&my_status[tid], pack_status(first ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
         const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
-        if (tid < RADIX) s_local[tid] = local;
+        if (tid < RADIX) {
+            s_local[tid] = local;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) warp_hist[w * RADIX + tid] += local;
+        }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = rd[i] & 0xFFu;
-            const uint32_t pos = s_local[d] + warp_hist[warp * RADIX + d] + (rd[i] >> 8);
+            const uint32_t pos = warp_hist[warp * RADIX + (rd[i] & 0xFFu)] + (rd[i] >> 8);
             s_keys[pos] = key[i];
-            rd[i] = pos;
-        }
-        if (HAS_V) {
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t idx = wbase + i * 32;
-                s_vals[rd[i]] = idx < sege ? src_v[idx] : 0u;
-            }
+            if (HAS_V) s_vals[pos] = val[i];
         }
         if (tid < RADIX) {
             uint32_t excl = 0;
             if (!first) {
-                uint64_t k = t - 1;
-                for (;;) {
-                    const uint64_t seq = seq0 + k;
-                    const uint64_t* p = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
-                    const uint64_t want = seq & TAG_MASK;
-                    uint64_t w = dev::ld_relaxed(p);
-                    bool gave_up = false;
-                    if ((w >> 62) == 0 || ((w >> 32) & TAG_MASK) != want) {
-                        const unsigned long long start = dev::globaltimer();
-                        for (uint32_t spin = 1;; ++spin) {
-                            w = dev::ld_relaxed(p);
-                            if ((w >> 62) != 0 && ((w >> 32) & TAG_MASK) == want) break;
-                            if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                gave_up = true;
-                                break;
+                int64_t k = (int64_t)t - 1;
+                bool done = false;
+                while (!done) {
+                    uint64_t w[LBW];
+#pragma unroll
+                    for (int q = 0; q < LBW; ++q)
+                        if (k - q >= 0)
+                            w[q] = dev::ld_relaxed(a.ring + ((seq0 + (uint64_t)(k - q)) & (RING_TILES - 1)) * RADIX +
+                                                   tid);
+#pragma unroll
+                    for (int q = 0; q < LBW; ++q) {
+                        if (done || k - q < 0) break;
+                        const uint64_t seq = seq0 + (uint64_t)(k - q);
+                        const uint64_t want = seq & TAG_MASK;
+                        uint64_t x = w[q];
+                        if ((x >> 62) == 0 || ((x >> 32) & TAG_MASK) != want) {
+                            const uint64_t* pw = a.ring + (seq & (RING_TILES - 1)) * RADIX + tid;
+                            const unsigned long long start = dev::globaltimer();
+                            for (uint32_t spin = 1;; ++spin) {
+                                x = dev::ld_relaxed(pw);
+                                if ((x >> 62) != 0 && ((x >> 32) & TAG_MASK) == want) break;
+                                if ((spin & 63) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
+                                    dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
+                                    s_abort = 1;
+                                    x = FLAG_PRE << 62;  // stop walking
+                                    break;
+                                }
+                                __nanosleep(spin < 16 ? 32 : 128);
                             }
-                            if (spin > 32) __nanosleep(64);
                         }
+                        excl += (uint32_t)x;
+                        if ((x >> 62) == FLAG_PRE) done = true;
                     }
-                    if (gave_up) {
-                        dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                        s_abort = 1;
-                        break;
-                    }
-                    excl += (uint32_t)w;
-                    if ((w >> 62) == FLAG_PRE || k == 0) break;
-                    --k;
+                    k -= LBW;
+                    if (k < 0) done = true;
                 }
                 dev::st_relaxed(&my_status[tid], pack_status(FLAG_PRE, seq0 + t, excl + agg));
             }
@@ -520,13 +561,31 @@ __global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int sl
         }
         __syncthreads();
         const uint32_t limit = s_abort ? 0u : valid;
-        for (uint32_t q = tid; q < limit; q += THREADS) {
-            const K kk = s_keys[q];
-            const uint32_t d = (uint32_t)(a.xf(kk) >> shift) & 0xFFu;
-            const uint32_t o = s_bin_off[d] + q;
-            if (o >= segb && o < sege) {
-                dst_k[o] = kk;
-                if (HAS_V) dst_v[o] = s_vals[q];
+        if (limit == (uint32_t)TILE) {
+            uint32_t o[ITEMS];
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[tid + i * THREADS];
+            if (HAS_V) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[tid + i * THREADS];
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) o[i] = s_bin_off[digit(key[i])] + tid + i * THREADS;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                if (o[i] >= segb && o[i] < sege) {
+                    dst_k[o[i]] = key[i];
+                    if (HAS_V) dst_v[o[i]] = val[i];
+                }
+            }
+        } else {
+            for (uint32_t q = tid; q < limit; q += THREADS) {
+                const K kk = s_keys[q];
+                const uint32_t o = s_bin_off[digit(kk)] + q;
+                if (o >= segb && o < sege) {
+                    dst_k[o] = kk;
+                    if (HAS_V) dst_v[o] = s_vals[q];
+                }
             }
         }
         __syncthreads();
@@ -538,10 +597,10 @@ __global__ void __launch_bounds__(THREADS) k_seg_large_pass(SegArgs<K> a, int sl
 // ---------------------------------------------------------------------------
 template <typename K, bool HAS_V> struct LargeShape;
 template <bool HV> struct LargeShape<uint32_t, HV> {
-    static constexpr int THREADS = 256, ITEMS = 16;
+    static constexpr int THREADS = 256, ITEMS = 24, MINB = 2, LBW = HV ? 1 : 4;
 };
 template <bool HV> struct LargeShape<uint64_t, HV> {
-    static constexpr int THREADS = 256, ITEMS = 12;
+    static constexpr int THREADS = 256, ITEMS = HV ? 20 : 24, MINB = 2, LBW = 4;
 };
 
 template <typename F> static void set_smem(F* kernel, std::size_t bytes)
@@ -646,8 +705,8 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
         auto hk = &k_seg_large_hist<K>;
         k_seg_large_hist<K><<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
         check_cuda(cudaGetLastError(), "segmented sort histogram launch");
-        auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS>;
-        const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 4 + (std::size_t)TILE * sizeof(K) +
+        auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS, LS::MINB, LS::LBW>;
+        const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +
                                   (HAS_V ? (std::size_t)TILE * 4 : 0);
         set_smem(pk, psmem);
         const int pgrid = ctx.sm_count * occupancy(pk, LS::THREADS, psmem);

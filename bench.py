@@ -262,6 +262,28 @@ def main() -> None:
     def uniform_u32(count: int) -> torch.Tensor:
         return torch.randint(0, 2**32, (count,), dtype=torch.int64, device="cuda", generator=gen).to(torch.int32)
 
+    l2_flush = []
+
+    def timed_flushed(fn, steps: int, warmup: int) -> float:
+        """For inputs smaller than L2: every step is preceded by a write of a
+        buffer larger than L2 and timed alone (CUDA events around the call);
+        returns the median ms per step."""
+        if not l2_flush:
+            l2_flush.append(torch.empty(1 << 28, dtype=torch.int32, device="cuda"))  # 1 GiB > 129 MB of L2
+        for _ in range(warmup):
+            fn()
+        times = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                l2_flush[0].fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return max_over_ranks(statistics.median(times))
+
     def timed(fn, steps: int, warmup: int, families: tuple[str, ...], soak_s: float = 0.0):
         """Runs fn warmup times (plus a soak), then `steps` timed calls between
         CUDA events on the library stream. Returns (ms per step, per-family
@@ -363,7 +385,7 @@ def main() -> None:
     workloads = {}
     if not args.no_extras:
         workloads = run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, max(5, args.steps // 5),
-                               args.warmup)
+                               args.warmup, timed_flushed)
     del keys_in, vals_in, keys_out, vals_out
     torch.cuda.empty_cache()
 
@@ -422,9 +444,10 @@ def learned_mixture_keys(torch, n: int, seed: int):
     return keys[perm].contiguous()
 
 
-def zipf_splitmix_keys(torch, n: int, s: float, distinct: int, seed: int):
+def zipf_splitmix_keys(torch, n: int, s: float, distinct: int, seed: int, raw_rank: bool = False):
     """n u64 keys: Zipf(s) ranks over `distinct` values (inverse CDF on the
-    device), mapped by splitmix64; u32 values uniform in [0, 2^16)."""
+    device), mapped by splitmix64 (or left as ranks); u32 values uniform in
+    [0, 2^16)."""
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     w = torch.arange(1, distinct + 1, device="cuda", dtype=torch.float64).pow(-s)
@@ -435,6 +458,9 @@ def zipf_splitmix_keys(torch, n: int, s: float, distinct: int, seed: int):
     for i in range(0, n, chunk):
         u = torch.rand(min(chunk, n - i), device="cuda", generator=g, dtype=torch.float64)
         r = torch.searchsorted(cdf, u).clamp_(max=distinct - 1)
+        if raw_rank:
+            keys[i:i + r.numel()] = r
+            continue
         x = r + (-7046029254386353131)  # + 0x9E3779B97F4A7C15 (wrapping)
         x = (x ^ ((x >> 30) & ((1 << 34) - 1))) * (-4658895280553007687)  # 0xBF58476D1CE4E5B9
         x = (x ^ ((x >> 27) & ((1 << 37) - 1))) * (-7723592293110705685)  # 0x94D049BB133111EB
@@ -443,7 +469,7 @@ def zipf_splitmix_keys(torch, n: int, s: float, distinct: int, seed: int):
     return keys, vals
 
 
-def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, warmup) -> dict:
+def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, warmup, timed_flushed) -> dict:
     """The other configuration workloads, each timed the same way."""
     out = {}
 
@@ -463,6 +489,17 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     entry("keys_sort_u32_uniform_n2^28", n, "Gkeys/s", ms, 36 * n,
           bool(torch.equal(ref, kout.to(torch.int64) & 0xFFFFFFFF)), prof)
     del ref, kout
+
+    # configuration 1's own size: keys-only u32 sort of 2^24 (inputs fit in L2:
+    # each step follows an L2 flush and is timed alone; median)
+    small = keys[: 1 << 24].clone()
+    sout = torch.empty_like(small)
+    ms = timed_flushed(lambda: gbc.sort_raw(ctx, small.data_ptr(), sout.data_ptr(), np.uint32, small.numel()), steps,
+                       warmup)
+    ok = bool(torch.equal(torch.sort(small.to(torch.int64) & 0xFFFFFFFF).values, sout.to(torch.int64) & 0xFFFFFFFF))
+    entry("keys_sort_u32_uniform_n2^24", small.numel(), "Gkeys/s", ms, 36 * small.numel(), ok, {},
+          {"l2": "flushed before every step (1 GiB write), median of the steps"})
+    del small, sout
 
     # entropy sweep: keys = AND of k uniform words, values = index
     vals = torch.arange(n, dtype=torch.int32, device="cuda")
@@ -621,7 +658,27 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                       "values": "u32 uniform [0, 2^16)",
                       "note": "bytes: 8 B upfront histogram + 8 digit passes x 24 B + 12 B reduce_by_key read = 212 B/key; "
                               "the learned-CDF form is 32-bit only"})
-    del zk, zv, zko, zvo, uk, sums, cnts, zu, order, sk_ref, uniq, counts, seg, ref_sums
+    # the same pipeline on the raw Zipf ranks as keys (< 2^24: the pass plan
+    # runs 3 of the 8 digit passes)
+    rk, _ = zipf_splitmix_keys(torch, np_, 1.1, 1 << 24, 6, raw_rank=True)
+    runs.clear()
+
+    def pipeline_raw():
+        gbc.sort_raw(ctx, rk.data_ptr(), zko.data_ptr(), np.uint64, np_, zv.data_ptr(), zvo.data_ptr())
+        runs.append(gbc.reduce_by_key_raw(ctx, zko.data_ptr(), np.uint64, zvo.data_ptr(), np_, uk.data_ptr(),
+                                          sums.data_ptr(), cnts.data_ptr(), h16.data_ptr()))
+
+    ms_raw, prof_raw = timed(pipeline_raw, max(3, steps // 5), warmup, ("sort.", "reduce_by_key"))
+    order = torch.sort(rk, stable=True).indices
+    ok = bool(torch.equal(zko, rk[order])) and bool(torch.equal(zvo, zv[order]))
+    uniq, counts = torch.unique_consecutive(rk[order], return_counts=True)
+    r = runs[-1]
+    ok = ok and r == uniq.numel() and bool(torch.equal(uk[:r], uniq)) and bool(torch.equal(cnts[:r].long(), counts))
+    ok = ok and bool(torch.equal(torch.bincount(rk & 0xFFFF, minlength=65536).to(torch.int32), h16))
+    entry("pipeline_sort_rbk_hist_u64_zipf_rawrank_n2^29", np_, "Gkeys/s", ms_raw, (8 + 24 * 3 + 12) * np_, ok,
+          prof_raw, {"runs": int(r), "key": "Zipf(1.1) rank over 2^24 values, unmapped",
+                     "note": "3 active digit passes: bytes = 8 + 3 x 24 + 12 = 92 B/key"})
+    del zk, zv, zko, zvo, uk, sums, cnts, zu, order, sk_ref, uniq, counts, seg, ref_sums, rk
     torch.cuda.empty_cache()
 
     # 256-bin histogram of 2^30 uniform bytes

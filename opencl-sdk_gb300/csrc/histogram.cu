@@ -63,8 +63,23 @@ __global__ void __launch_bounds__(THREADS)
     uint32_t head = 0;
     if ((reinterpret_cast<uintptr_t>(in) & 15) == 0) {
         const uint32_t nv = n / VEC;
-        for (uint32_t v = gtid; v < nv; v += stride) {
-            const uint4 w = dev::ld_stream(reinterpret_cast<const uint4*>(in) + v);
+        const uint4* vin = reinterpret_cast<const uint4*>(in);
+        uint32_t v = gtid;
+        // four 128-bit loads in flight per thread before they are counted
+        for (; (uint64_t)v + 3ull * stride < nv; v += 4 * stride) {
+            uint4 w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = dev::ld_stream(vin + v + q * stride);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                T e[VEC];
+                memcpy(e, &w[q], 16);
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) count(e[j]);
+            }
+        }
+        for (; v < nv; v += stride) {
+            const uint4 w = dev::ld_stream(vin + v);
             T e[VEC];
             memcpy(e, &w, 16);
 #pragma unroll

@@ -102,7 +102,21 @@ __global__ void __launch_bounds__(THREADS) k_upfront(SortArgs<K> a)
     if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
         const size_t nv = n / PER_VEC;
         const uint4* kv = reinterpret_cast<const uint4*>(keys);
-        for (size_t v = gtid; v < nv; v += stride) {
+        size_t v = gtid;
+        // four 128-bit loads in flight per thread before they are counted
+        for (; v + 3 * stride < nv; v += 4 * stride) {
+            uint4 w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = dev::ld_stream(kv + v + q * stride);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                K ks[PER_VEC];
+                memcpy(ks, &w[q], 16);
+#pragma unroll
+                for (int j = 0; j < PER_VEC; ++j) count(ks[j]);
+            }
+        }
+        for (; v < nv; v += stride) {
             const uint4 w = dev::ld_stream(kv + v);
             K ks[PER_VEC];
             memcpy(ks, &w, 16);

@@ -33,6 +33,7 @@ SOURCES = [
     "segscan.cu",
     "learned.cu",
     "reduce_by_key.cu",
+    "select.cu",
 ]
 
 COMMON = [

@@ -26,6 +26,7 @@
 #include <string>
 
 #include "autotune.hpp"
+#include "select.hpp"
 #include "learned.hpp"
 #include "runtime.hpp"
 #include "segmented.hpp"
@@ -490,10 +491,19 @@ clc_status clc_transform2(clc_context, clc_buffer, clc_type, clc_buffer, clc_typ
 {
     GBC_UNSUPPORTED("transform with a run-time expression");
 }
-clc_status clc_copy_if(clc_context, clc_buffer, clc_buffer, size_t, clc_type, const char*, size_t* count)
+// copy_if (CApi.cpp:533-545): the predicate comes from a fixed grammar
+// (select.hpp); anything else is CLC_ERROR_UNSUPPORTED.
+clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n, clc_type type, const char* predicate,
+                       size_t* count)
 {
-    if (count) *count = 0;
-    GBC_UNSUPPORTED("copy_if with a run-time predicate");
+    return guarded([&] {
+        require(ctx != nullptr && predicate != nullptr && count != nullptr, "clc: null argument");
+        *count = 0;
+        require_fits(in, n, type);
+        require_fits(out, n, type);
+        const gbc::predicate p = gbc::parse_predicate(predicate, elem_of(type));
+        *count = gbc::copy_if(*ctx->ctx, in->ptr, out->ptr, n, elem_of(type), p);
+    });
 }
 clc_status clc_add_header(clc_context, const char*, const char*) { GBC_UNSUPPORTED("run-time kernel source"); }
 clc_status clc_kernel_create(clc_context, const char*, const char*, const char*, const char* const*,

@@ -442,6 +442,19 @@ def reduce(ctx: Context, inp: DeviceBuffer, op: binary_op | None = None, init=0)
     return r[0]
 
 
+def copy_if(ctx: Context, inp: DeviceBuffer, out: DeviceBuffer, predicate: str) -> int:
+    """Stable compaction (reference Algorithm.hpp:229-237): out[0:count] = the
+    elements x of inp with predicate(x); returns count. The predicate is an
+    OpenCL C expression over x from a fixed grammar (comparisons of x,
+    (x % c) or (x & c) with a constant, joined by && or ||)."""
+    if out.size < inp.size:
+        raise ValueError("copy_if: output too small")
+    count = C.c_size_t(0)
+    _raise_for(lib.clc_copy_if(ctx.handle, inp.handle, out.handle, inp.size, clc_type(inp.dtype),
+                               predicate.encode(), C.byref(count)))
+    return count.value
+
+
 def _scan(ctx, inp, out, op, exclusive, want_total):
     if out.size < inp.size:
         raise ValueError(("exclusive" if exclusive else "inclusive") + "_scan: output too small")

@@ -534,13 +534,22 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ok = int(total.item()) == int(cs[-1].item())
     ok = ok and bool(torch.equal(y[1:], cs[:-1].to(torch.int32))) and int(y[0].item()) == 0
     entry("exclusive_scan_i32_n2^30", m, "Gelem/s", ms, 8 * m, ok, prof)
-    del cs, y
+    del cs
 
     # reduce (plus) of the same data
-    ms, prof = timed(lambda: gbc.reduce(ctx, gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), m, np.int32)), steps, warmup,
-                     ("reduce.",))
+    xb = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), m, np.int32)
+    ms, prof = timed(lambda: gbc.reduce(ctx, xb), steps, warmup, ("reduce.",))
     entry("reduce_i32_n2^30", m, "Gelem/s", ms, 4 * m, True, prof, {"note": "includes the blocking result read"})
-    del x
+
+    # copy_if ("x > 0") of the same data: stable compaction, count read back
+    yb = gbc.DeviceBuffer.wrap(ctx, y.data_ptr(), m, np.int32)
+    kept = []
+    ms, prof = timed(lambda: kept.append(gbc.copy_if(ctx, xb, yb, "x > 0")), steps, warmup, ("select.",))
+    want = x[x > 0]
+    ok = kept[-1] == want.numel() and bool(torch.equal(y[: kept[-1]], want))
+    entry("copy_if_i32_n2^30", m, "Gelem/s", ms, 4 * m + 4 * kept[-1], ok, prof,
+          {"predicate": "x > 0", "kept": int(kept[-1]), "note": "includes the blocking count read"})
+    del x, y, want
 
     # learned-CDF sort of the 2^28-key float mixture vs the plain sort of the same keys
     torch.cuda.empty_cache()

@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     taken before the CTA can work on it publishes its counts late);
 //   * IDENT: the key transform is the identity (unsigned ascending keys).
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH, int BR>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
@@ -575,15 +575,29 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t d = rd[i];
-            atomicOr(&wm[d], 1u << lane);
-            __syncwarp();
-            const uint32_t peers = wm[d];
+            // BR of every 4 rows find their peers with 8 ballots (ALU pipe)
+            // instead of the mask word (shared-memory pipe)
+            const bool by_ballot = (i & 3) < BR;
+            uint32_t peers;
+            if (by_ballot) {
+                peers = FULL_MASK;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t bit = (d >> b) & 1u;
+                    const uint32_t vote = __ballot_sync(FULL_MASK, bit);
+                    peers &= bit ? vote : ~vote;
+                }
+            } else {
+                atomicOr(&wm[d], 1u << lane);
+                __syncwarp();
+                peers = wm[d];
+            }
             const uint32_t before = wh[d];
             __syncwarp();
             const uint32_t lower = peers & lt_mask;
             if (lower == 0) {
                 wh[d] = before + __popc(peers);
-                wm[d] = 0;
+                if (!by_ballot) wm[d] = 0;
             }
             __syncwarp();
             rd[i] = ((before + __popc(lower)) << 8) | d;
@@ -714,10 +728,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 }
 
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF, int BR>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -739,19 +753,21 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
 #define GBC_P1B(K, HV, T, I, B) \
     PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
-#define GBC_P2(K, HV, T, I, B, W, S, PF) \
-    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF>, &k_pass2<K, HV, T, I, true, B, W, S, PF>}
+#define GBC_P2(K, HV, T, I, B, W, S, PF) GBC_P2R(K, HV, T, I, B, W, S, PF, 0)
+#define GBC_P2R(K, HV, T, I, B, W, S, PF, BR)                                                  \
+    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR>,              \
+                   &k_pass2<K, HV, T, I, true, B, W, S, PF, BR>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 8;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
             HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, true),
-            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, false) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, false),
-            GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true),
-            GBC_P2(uint32_t, HV, 256, 16, 3, 4, false, true),
-            GBC_P2(uint32_t, HV, 256, 20, 2, 4, false, true),
-            HV ? GBC_P2(uint32_t, HV, 512, 16, 1, 4, true, true) : GBC_P2(uint32_t, HV, 512, 24, 1, 4, true, true),
+            HV ? GBC_P2R(uint32_t, HV, 256, 24, 2, 4, false, true, 1) : GBC_P2R(uint32_t, HV, 256, 24, 2, 4, true, true, 1),
+            HV ? GBC_P2R(uint32_t, HV, 256, 24, 2, 4, false, true, 2) : GBC_P2R(uint32_t, HV, 256, 24, 2, 4, true, true, 2),
+            HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true),
+            GBC_P2(uint32_t, HV, 512, 12, 2, 4, false, true),
+            GBC_P2(uint32_t, HV, 384, 16, 2, 4, false, true),
             GBC_P1(uint32_t, HV, 256, 16, false),
             GBC_P1B(uint32_t, HV, 256, 16, 3),
         };
@@ -777,6 +793,7 @@ template <bool HV> struct Variants<uint64_t, HV> {
 #undef GBC_P1
 #undef GBC_P1B
 #undef GBC_P2
+#undef GBC_P2R
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {

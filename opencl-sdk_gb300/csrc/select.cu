@@ -200,44 +200,56 @@ constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
 constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
 constexpr uint64_t SLOTS = onesweep::RING_BYTES / 8;
 
-template <typename C> __device__ __forceinline__ bool compare(C a, C b, int cmp)
+// A clause flattened for the device: the operand path (0 int32, 1 uint32,
+// 2 int64, 3 uint64, 4 double, which is exact for float operands and
+// literals), the left side, and the result for each ordering of lhs against
+// the constant (less, equal, greater, unordered: NaN), so that no switch on
+// the comparison is needed.
+struct dclause {
+    int kind;
+    int lhs;  // 0: x, 1: x % m, 2: x & m
+    int64_t m, c;
+    double cf;
+    bool lt, eq, gt, un;
+};
+struct dpredicate {
+    int count, join;
+    dclause c[4];
+};
+
+template <typename I, typename T> __device__ __forceinline__ int order_int(T x, const dclause& c)
 {
-    switch (cmp) {
-    case 0: return a < b;
-    case 1: return a <= b;
-    case 2: return a > b;
-    case 3: return a >= b;
-    case 4: return a == b;
-    default: return a != b;
+    I v = (I)x;
+    if (c.lhs == 1) v = (I)(v % (I)c.m);
+    else if (c.lhs == 2) v = (I)(v & (I)c.m);
+    const I k = (I)c.c;
+    return v < k ? 0 : (v == k ? 1 : 2);
+}
+
+// (if-else rather than switch: a jump table costs an indirect branch per
+// element and stalls instruction fetch)
+template <typename T> __device__ __forceinline__ bool clause_eval(T x, const dclause& c)
+{
+    int o;
+    if (c.kind == 0) o = order_int<int32_t>(x, c);
+    else if (c.kind == 1) o = order_int<uint32_t>(x, c);
+    else if (c.kind == 2) o = order_int<int64_t>(x, c);
+    else if (c.kind == 3) o = order_int<uint64_t>(x, c);
+    else {
+        const double v = (double)x;
+        o = v < c.cf ? 0 : (v == c.cf ? 1 : (v > c.cf ? 2 : 3));
     }
+    return o == 0 ? c.lt : (o == 1 ? c.eq : (o == 2 ? c.gt : c.un));
 }
 
-template <typename C, typename T> __device__ __forceinline__ bool eval_in(T x, const pred_clause& c)
+template <typename T> __device__ __forceinline__ bool eval(T x, const dpredicate& p)
 {
-    C v = (C)x;
-    if (c.lhs == 1) v = (C)(v % (C)c.m_i);
-    else if (c.lhs == 2) v = (C)(v & (C)c.m_i);
-    return compare<C>(v, (C)c.c_i, c.cmp);
-}
-
-template <typename T> __device__ __forceinline__ bool eval_clause(T x, const pred_clause& c)
-{
-    switch (c.ctype) {
-    case 0: return eval_in<int32_t>(x, c);
-    case 1: return eval_in<uint32_t>(x, c);
-    case 2: return eval_in<int64_t>(x, c);
-    case 3: return eval_in<uint64_t>(x, c);
-    case 4: return compare<float>((float)x, (float)c.c_f, c.cmp);
-    default: return compare<double>((double)x, c.c_f, c.cmp);
-    }
-}
-
-template <typename T> __device__ __forceinline__ bool eval(T x, const predicate& p)
-{
-    bool r = eval_clause(x, p.c[0]);
+    bool r = clause_eval(x, p.c[0]);
+    // unrolled with guards: constant indices keep the clauses in the
+    // parameter space (a run-time index would copy them to local memory)
 #pragma unroll
     for (int k = 1; k < 4; ++k)
-        if (k < p.count) r = p.join ? (r || eval_clause(x, p.c[k])) : (r && eval_clause(x, p.c[k]));
+        if (k < p.count) r = p.join ? (r || clause_eval(x, p.c[k])) : (r && clause_eval(x, p.c[k]));
     return r;
 }
 
@@ -245,7 +257,7 @@ template <typename T> struct SelArgs {
     const T* in;
     T* out;
     uint32_t n;
-    predicate p;
+    dpredicate p;
     uint32_t num_tiles;
     uint64_t* ring;
     uint64_t seq0;
@@ -267,49 +279,71 @@ __device__ __forceinline__ bool read_status(const uint64_t* ring, uint64_t seq, 
     return true;
 }
 
-// Tile: THREADS x ITEMS elements, each thread ITEMS consecutive ones (read as
-// 128-bit vectors when aligned), kept in order.
+// Tile: THREADS x ITEMS elements; warp w owns ROWS = ITEMS / V rows of 32 x V
+// consecutive elements (V = 16 / sizeof(T): one 128-bit load per lane and
+// row), row r at tile_base + (w * ROWS + r) * 32 V, lane l holding elements
+// l V .. l V + V - 1 of the row. A ballot per element slot gives the row's
+// keep masks; an element's place among the row's kept ones is the number of
+// kept elements in lower lanes (sum over the slots of popc(mask & lower
+// lanes)) plus the lane's own kept elements before it. The rows are visited
+// by loops that are not unrolled, so the predicate's evaluator appears once
+// in the code (unrolled, its copies overflowed the instruction cache).
 template <typename T, int ITEMS> __global__ void __launch_bounds__(THREADS) k_copy_if(SelArgs<T> a)
 {
+    constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
-    __shared__ uint32_t s_warp[THREADS / 32];
+    constexpr int V = 16 / sizeof(T);
+    constexpr int ROWS = ITEMS / V;
+    static_assert(ITEMS % V == 0, "whole 128-bit rows");
+    __shared__ __align__(16) T s_in[TILE];
+    __shared__ uint32_t s_mask[WARPS * ROWS * V];
+    __shared__ uint32_t s_warp[WARPS];
     __shared__ uint32_t s_prefix;
     __shared__ uint32_t s_tile;
+    __shared__ dpredicate s_p;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool aligned = ((reinterpret_cast<uintptr_t>(a.in)) & 15) == 0;
+    if (tid == 0) s_p = a.p;
+    const uint32_t lt_mask = dev::lanemask_lt();
+    const bool aligned = (reinterpret_cast<uintptr_t>(a.in) & 15) == 0;
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(a.tile_ctr, 1u);
+        if (tid == 0) {
+            // taken only when the CTA can start on it; the tile a grid ahead
+            // is prefetched into L2 (cf. the scan)
+            s_tile = atomicAdd(a.tile_ctr, 1u);
+            const uint64_t ahead = (uint64_t)s_tile + gridDim.x;
+            if (aligned && (ahead + 1) * TILE <= a.n) dev::prefetch_l2(a.in + ahead * TILE, TILE * sizeof(T));
+        }
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= a.num_tiles) break;
-        const uint32_t first = t * TILE + tid * ITEMS;
-        T x[ITEMS];
-        uint32_t keep = 0;
-        if (aligned && first + ITEMS <= a.n) {
-            const uint4* p = reinterpret_cast<const uint4*>(a.in + first);
+        const uint32_t wbase = t * TILE + warp * ROWS * 32 * V;
+        T* srow = s_in + warp * ROWS * 32 * V;
+        uint32_t count = 0;
+#pragma unroll 1
+        for (int r = 0; r < ROWS; ++r) {
+            const uint32_t first = wbase + (r * 32 + lane) * V;
+            T x[V];
+            if (aligned && first + V <= a.n) {
+                const uint4 w = *reinterpret_cast<const uint4*>(a.in + first);
+                memcpy(x, &w, 16);
+            } else {
 #pragma unroll
-            for (int j = 0; j < ITEMS * (int)sizeof(T) / 16; ++j) {
-                const uint4 w = p[j];
-                memcpy(reinterpret_cast<unsigned char*>(x) + 16 * j, &w, 16);
+                for (int q = 0; q < V; ++q) x[q] = first + q < a.n ? a.in[first + q] : T(0);
             }
+            *reinterpret_cast<uint4*>(srow + (r * 32 + lane) * V) = *reinterpret_cast<const uint4*>(x);
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) keep |= (eval(x[i], a.p) ? 1u : 0u) << i;
-        } else {
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t idx = first + i;
-                x[i] = idx < a.n ? a.in[idx] : T(0);
-                keep |= (idx < a.n && eval(x[i], a.p) ? 1u : 0u) << i;
+            for (int q = 0; q < V; ++q) {
+                const uint32_t m = __ballot_sync(FULL_MASK, first + q < a.n && eval(x[q], s_p));
+                if (lane == 0) s_mask[(warp * ROWS + r) * V + q] = m;
+                count += __popc(m);
             }
         }
-        const uint32_t mine = __popc(keep);
-        const uint32_t winc = dev::warp_inclusive_scan(mine, [](uint32_t p, uint32_t q) { return p + q; });
-        if (lane == 31) s_warp[warp] = winc;
+        if (lane == 0) s_warp[warp] = count;
         __syncthreads();
         if (warp == 0) {
-            const uint32_t wv = lane < THREADS / 32 ? s_warp[lane] : 0u;
+            const uint32_t wv = lane < WARPS ? s_warp[lane] : 0u;
             const uint32_t wi = dev::warp_inclusive_scan(wv, [](uint32_t p, uint32_t q) { return p + q; });
-            if (lane < THREADS / 32) s_warp[lane] = wi - wv;
+            if (lane < WARPS) s_warp[lane] = wi - wv;
             const uint32_t agg = __shfl_sync(FULL_MASK, wi, 31);
             const uint64_t my_seq = a.seq0 + t;
             if (lane == 0) publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
@@ -365,13 +399,26 @@ template <typename T, int ITEMS> __global__ void __launch_bounds__(THREADS) k_co
             }
         }
         __syncthreads();
-        uint32_t pos = s_prefix + s_warp[warp] + winc - mine;
+        uint32_t pos = s_prefix + s_warp[warp];
+#pragma unroll 1
+        for (int r = 0; r < ROWS; ++r) {
+            uint32_t m[V], below = 0, row_total = 0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i)
-            if ((keep >> i) & 1u) {
-                if (pos < a.n) a.out[pos] = x[i];
-                ++pos;
+            for (int q = 0; q < V; ++q) {
+                m[q] = s_mask[(warp * ROWS + r) * V + q];
+                below += __popc(m[q] & lt_mask);
+                row_total += __popc(m[q]);
             }
+            uint32_t o = pos + below;
+            const T* src = srow + (r * 32 + lane) * V;
+#pragma unroll
+            for (int q = 0; q < V; ++q)
+                if ((m[q] >> lane) & 1u) {
+                    if (o < a.n) a.out[o] = src[q];
+                    ++o;
+                }
+            pos += row_total;
+        }
         __syncthreads();
     }
 }
@@ -379,13 +426,27 @@ template <typename T, int ITEMS> __global__ void __launch_bounds__(THREADS) k_co
 template <typename T>
 void launch_select(device_context& ctx, const void* in, void* out, uint32_t n, const predicate& p, uint32_t* total)
 {
-    constexpr int ITEMS = sizeof(T) <= 4 ? 16 : 8;
+    constexpr int ITEMS = sizeof(T) <= 4 ? 32 : 16;
     constexpr uint32_t TILE = THREADS * ITEMS;
     SelArgs<T> a;
     a.in = static_cast<const T*>(in);
     a.out = static_cast<T*>(out);
     a.n = n;
-    a.p = p;
+    a.p.count = p.count;
+    a.p.join = p.join;
+    for (int k = 0; k < p.count; ++k) {
+        const pred_clause& q = p.c[k];
+        dclause& d = a.p.c[k];
+        d.kind = q.ctype >= 4 ? 4 : q.ctype;
+        d.lhs = q.lhs;
+        d.m = q.m_i;
+        d.c = q.c_i;
+        d.cf = q.ctype == 4 ? (double)(float)q.c_f : q.c_f;  // float compare: the constant in float
+        d.lt = q.cmp == 0 || q.cmp == 1 || q.cmp == 5;
+        d.eq = q.cmp == 1 || q.cmp == 3 || q.cmp == 4;
+        d.gt = q.cmp == 2 || q.cmp == 3 || q.cmp == 5;
+        d.un = q.cmp == 5;  // only != holds for NaN
+    }
     a.num_tiles = (n + TILE - 1) / TILE;
     a.ring = ctx.lookback_ring;
     a.seq0 = ctx.reserve_seq(a.num_tiles);

@@ -5,8 +5,11 @@ an ncu capture has a short, deterministic launch sequence.
 
 Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
 (u64 keys + u32 values), scan-i32 (exclusive, int64 total), reduce-i32,
-hist-u8 (256 bins). Inputs are seeded uniform data generated on the device;
-every call goes through the C ABI on the library's stream.
+hist-u8 (256 bins), segsort-u64kv (lognormal segments, median 256, sigma 2,
+n = total keys), rbk-u64 (reduce_by_key over sorted keys with runs, fused
+65,536-bin histogram), copy-if-i32 ("x > 0"). Inputs are seeded synthetic
+data generated on the device; every call goes through the C ABI on the
+library's stream.
 """
 from __future__ import annotations
 
@@ -72,6 +75,44 @@ def main() -> None:
 
         def step():
             gbc.histogram_even_raw(ctx, x.data_ptr(), n, np.uint8, h.data_ptr(), 256, 0.0, 256.0)
+    elif args.case == "segsort-u64kv":
+        rng = np.random.default_rng(4)
+        lens = []
+        total = 0
+        while total < n:
+            ln = int(min(max(round(rng.lognormal(np.log(256), 2.0)), 1), 1 << 20))
+            ln = min(ln, n - total)
+            lens.append(ln)
+            total += ln
+        offs = np.zeros(len(lens) + 1, dtype=np.int64)
+        np.cumsum(lens, out=offs[1:])
+        off = torch.from_numpy(offs.astype(np.int32)).cuda()
+        k = torch.randint(-2**63, 2**63 - 1, (n,), dtype=torch.int64, device="cuda", generator=g)
+        ko = torch.empty_like(k)
+        v, vo = torch.arange(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")
+
+        def step():
+            gbc.segmented_sort_raw(ctx, k.data_ptr(), ko.data_ptr(), np.uint64, n, off.data_ptr(), len(lens),
+                                   v.data_ptr(), vo.data_ptr())
+    elif args.case == "rbk-u64":
+        # sorted keys with runs of geometric length (mean 40), values < 2^16
+        runs = torch.rand(n, device="cuda", generator=g) < 1.0 / 40
+        k = torch.cumsum(runs.to(torch.int64), 0) * 2654435761
+        v = torch.randint(0, 1 << 16, (n,), dtype=torch.int32, device="cuda", generator=g)
+        uk, sums = torch.empty_like(k), torch.empty(n, dtype=torch.int64, device="cuda")
+        cnt, h = torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(65536, dtype=torch.int32, device="cuda")
+
+        def step():
+            gbc.reduce_by_key_raw(ctx, k.data_ptr(), np.uint64, v.data_ptr(), n, uk.data_ptr(), sums.data_ptr(),
+                                  cnt.data_ptr(), h.data_ptr(), want_count=False)
+    elif args.case == "copy-if-i32":
+        x = torch.randint(-1000, 1001, (n,), dtype=torch.int32, device="cuda", generator=g)
+        y = torch.empty_like(x)
+        xb = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), n, np.int32)
+        yb = gbc.DeviceBuffer.wrap(ctx, y.data_ptr(), n, np.int32)
+
+        def step():
+            gbc.copy_if(ctx, xb, yb, "x > 0")
     else:
         raise SystemExit(f"unknown case {args.case}")
 

@@ -515,7 +515,7 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
         sk, si = torch.sort(ki, stable=True)
         ok = bool(torch.equal(sk, kout.to(torch.int64) & 0xFFFFFFFF)) and bool(torch.equal(si.to(torch.int32), vout))
         passes = int(sum(1 for b in range(4) if int(((ki >> (8 * b)) & 255).unique().numel()) > 1))
-        moved = 4 * n + 16 * n * passes + (8 * n if passes == 0 else 0)
+        moved = 4 * n + 16 * n * passes + (16 * n if passes == 0 else 0)  # no active pass: one copy of keys + values
         entry(f"kv_sort_u32_and{k}_n2^28", n, "Gkeys/s", ms, moved, ok, prof, {"active_passes": passes})
         del kk, ki, sk, si
     del keys, vals, vout, kout

@@ -549,7 +549,27 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ok = kept[-1] == want.numel() and bool(torch.equal(y[: kept[-1]], want))
     entry("copy_if_i32_n2^30", m, "Gelem/s", ms, 4 * m + 4 * kept[-1], ok, prof,
           {"predicate": "x > 0", "kept": int(kept[-1]), "note": "includes the blocking count read"})
-    del x, y, want
+    del want
+
+    # transform: the Fahrenheit conversion of the reference's compute-pipeline
+    # sample ("x * 0.18f + 32.0f", uint -> float) and its binary calibration
+    # ("x + y", uint), over the same 2^30 words read as uint32
+    f = torch.empty(m, dtype=torch.float32, device="cuda")
+    fb = gbc.DeviceBuffer.wrap(ctx, f.data_ptr(), m, np.float32)
+    xu = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), m, np.uint32)
+    ms, prof = timed(lambda: gbc.transform(ctx, xu, fb, "x * 0.18f + 32.0f"), steps, warmup, ("transform",))
+    chk = 1 << 26
+    ref = (x[:chk].to(torch.int64) & 0xFFFFFFFF).to(torch.float32) * 0.18 + 32.0
+    ok = bool(torch.equal(ref.view(torch.int32), f[:chk].view(torch.int32)))
+    entry("transform_u32_to_f32_n2^30", m, "Gelem/s", ms, 8 * m, ok, prof,
+          {"expression": "x * 0.18f + 32.0f", "checked": f"first {chk} elements against torch"})
+    yu = gbc.DeviceBuffer.wrap(ctx, y.data_ptr(), m, np.uint32)
+    fu = gbc.DeviceBuffer.wrap(ctx, f.data_ptr(), m, np.uint32)
+    ms, prof = timed(lambda: gbc.transform(ctx, xu, yu, fu, "x + y"), steps, warmup, ("transform",))
+    ok = bool(torch.equal((x[:chk].to(torch.int64) + y[:chk].to(torch.int64)).to(torch.int32), f[:chk].view(torch.int32)))
+    entry("transform2_u32_add_n2^30", m, "Gelem/s", ms, 12 * m, ok, prof,
+          {"expression": "x + y", "checked": f"first {chk} elements against torch"})
+    del x, y, f, ref
 
     # learned-CDF sort of the 2^28-key float mixture vs the plain sort of the same keys
     torch.cuda.empty_cache()

@@ -144,7 +144,12 @@ GBC_EXPORT clc_status clc_fill(clc_context ctx, clc_buffer out, size_t n, clc_ty
                                const void* value);
 GBC_EXPORT clc_status clc_sequence(clc_context ctx, clc_buffer out, size_t n, clc_type type,
                                    const void* start, const void* step);
-/* Run-time expressions need an OpenCL C compiler: CLC_ERROR_UNSUPPORTED. */
+/* out[i] = (out_type)(expression) with x = in[i] (and y = in2[i]); out may
+ * alias an input of the same type. Replaces compute_c.h:147-154. The
+ * expression is OpenCL C from a subset (operators, casts, literals, min/max/
+ * clamp/abs/fabs/as_T/convert_T) compiled for an ahead-of-time interpreter:
+ * malformed text is CLC_ERROR_BUILD with "build log" in clc_last_error(),
+ * OpenCL C outside the subset CLC_ERROR_UNSUPPORTED. Asynchronous. */
 GBC_EXPORT clc_status clc_transform(clc_context ctx, clc_buffer in, clc_type in_type,
                                     clc_buffer out, clc_type out_type, size_t n,
                                     const char* expression);
@@ -164,6 +169,13 @@ GBC_EXPORT clc_status clc_scan(clc_context ctx, clc_buffer in, clc_buffer out, s
  * CLC_ERROR_INVALID_ARGUMENT as in the reference (CApi.cpp:517-531). */
 GBC_EXPORT clc_status clc_sort(clc_context ctx, clc_buffer keys, clc_type key_type,
                                clc_buffer values, size_t n, int descending);
+/* Extension (no reference counterpart): compiles a transform expression
+ * without a device and writes the program listing (one operation per line)
+ * into listing[capacity] when listing is not NULL. Same statuses as
+ * clc_transform. */
+GBC_EXPORT clc_status clc_transform_compile(const char* expression, clc_type in_type, int has_in2,
+                                            clc_type in2_type, clc_type out_type, char* listing,
+                                            size_t capacity);
 GBC_EXPORT clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
                                   clc_type type, const char* predicate, size_t* count);
 

@@ -34,6 +34,7 @@ SOURCES = [
     "learned.cu",
     "reduce_by_key.cu",
     "select.cu",
+    "transform.cu",
 ]
 
 COMMON = [

@@ -26,6 +26,7 @@
 #include <string>
 
 #include "autotune.hpp"
+#include "expr.hpp"
 #include "select.hpp"
 #include "learned.hpp"
 #include "runtime.hpp"
@@ -55,9 +56,7 @@ struct clc_graph_s {
 
 namespace {
 
-struct build_error : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
+using gbc::build_error;
 
 thread_local std::string last_error;
 thread_local int last_native_error = 0;
@@ -482,14 +481,49 @@ clc_status clc_file_write(clc_context, const char*, int, size_t, clc_buffer, siz
     if (done) *done = 0;
     GBC_UNSUPPORTED("file I/O");
 }
-clc_status clc_transform(clc_context, clc_buffer, clc_type, clc_buffer, clc_type, size_t, const char*)
+// transform / transform2 (CApi.cpp:455-486): the expression is compiled on
+// the host into a program for the ahead-of-time interpreter kernel (expr.hpp);
+// a malformed expression is CLC_ERROR_BUILD with "build log" in the message,
+// OpenCL C outside the supported subset CLC_ERROR_UNSUPPORTED.
+clc_status clc_transform(clc_context ctx, clc_buffer in, clc_type in_type, clc_buffer out, clc_type out_type,
+                         size_t n, const char* expression)
 {
-    GBC_UNSUPPORTED("transform with a run-time expression");
+    return guarded([&] {
+        require(ctx != nullptr && expression != nullptr, "clc: null argument");
+        require_fits(in, n, in_type);
+        require_fits(out, n, out_type);
+        const gbc::xp::program p =
+            gbc::xp::compile(expression, elem_of(in_type), false, elem_of(in_type), elem_of(out_type));
+        gbc::transform(*ctx->ctx, p, in->ptr, nullptr, out->ptr, n);
+    });
 }
-clc_status clc_transform2(clc_context, clc_buffer, clc_type, clc_buffer, clc_type, clc_buffer, clc_type,
-                          size_t, const char*)
+clc_status clc_transform2(clc_context ctx, clc_buffer in1, clc_type type1, clc_buffer in2, clc_type type2,
+                          clc_buffer out, clc_type out_type, size_t n, const char* expression)
 {
-    GBC_UNSUPPORTED("transform with a run-time expression");
+    return guarded([&] {
+        require(ctx != nullptr && expression != nullptr, "clc: null argument");
+        require_fits(in1, n, type1);
+        require_fits(in2, n, type2);
+        require_fits(out, n, out_type);
+        const gbc::xp::program p =
+            gbc::xp::compile(expression, elem_of(type1), true, elem_of(type2), elem_of(out_type));
+        gbc::transform(*ctx->ctx, p, in1->ptr, in2->ptr, out->ptr, n);
+    });
+}
+clc_status clc_transform_compile(const char* expression, clc_type in_type, int has_in2, clc_type in2_type,
+                                 clc_type out_type, char* listing, size_t capacity)
+{
+    return guarded([&] {
+        require(expression != nullptr, "clc: null argument");
+        const gbc::xp::program p = gbc::xp::compile(expression, elem_of(in_type), has_in2 != 0,
+                                                    elem_of(has_in2 ? in2_type : in_type), elem_of(out_type));
+        if (listing != nullptr && capacity > 0) {
+            const std::string text = gbc::xp::listing(p);
+            const std::size_t k = std::min(capacity - 1, text.size());
+            std::memcpy(listing, text.data(), k);
+            listing[k] = '\0';
+        }
+    });
 }
 // copy_if (CApi.cpp:533-545): the predicate comes from a fixed grammar
 // (select.hpp); anything else is CLC_ERROR_UNSUPPORTED.

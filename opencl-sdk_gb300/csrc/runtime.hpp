@@ -39,6 +39,11 @@ struct unsupported_error : std::runtime_error {
 struct no_device_error : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
+//! An expression that OpenCL C would reject (the reference's build_error,
+//! ProgramCache.hpp:28); the message carries a "build log" line.
+struct build_error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
 
 //! Throws out_of_memory for allocation failures and device_error otherwise.
 void check_cuda(cudaError_t e, const char* what);

@@ -181,10 +181,23 @@ template <typename K> __global__ void k_precopy(SortArgs<K> a)
         return;
     }
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-        d[i] = s[i];
-        if (sv != nullptr) dv[i] = sv[i];
-    }
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    auto copy = [&](const void* src, void* dst, size_t bytes) {
+        // 128-bit copies when both sides are aligned, then the tail
+        size_t head = 0;
+        if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+            const uint4* s4 = static_cast<const uint4*>(src);
+            uint4* d4 = static_cast<uint4*>(dst);
+            const size_t nv = bytes / 16;
+            for (size_t v = gtid; v < nv; v += stride) d4[v] = dev::ld_stream(s4 + v);
+            head = nv * 16;
+        }
+        const unsigned char* sb = static_cast<const unsigned char*>(src);
+        unsigned char* db = static_cast<unsigned char*>(dst);
+        for (size_t i = head + gtid; i < bytes; i += stride) db[i] = sb[i];
+    };
+    copy(s, d, (size_t)a.n * sizeof(K));
+    if (sv != nullptr) copy(sv, dv, (size_t)a.n * 4);
 }
 
 // ---------------------------------------------------------------------------

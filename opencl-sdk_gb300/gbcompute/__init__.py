@@ -91,6 +91,10 @@ class OutOfMemoryError(ClcError, MemoryError):
     pass
 
 
+class BuildError(ClcError):
+    """A malformed expression (the reference's build_error); the message holds a build log."""
+
+
 def _raise_for(status: int) -> None:
     if status == SUCCESS:
         return
@@ -101,6 +105,7 @@ def _raise_for(status: int) -> None:
         ERROR_UNSUPPORTED: UnsupportedError,
         ERROR_NO_DEVICE: NoDeviceError,
         ERROR_OUT_OF_MEMORY: OutOfMemoryError,
+        ERROR_BUILD: BuildError,
     }.get(status, ClcError)
     raise cls(status, msg, native)
 
@@ -157,6 +162,7 @@ _PROTOS = {
     "clc_scan": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i]),
     "clc_sort": (_i, [_vp, _vp, _i, _vp, _sz, _i]),
     "clc_copy_if": (_i, [_vp, _vp, _vp, _sz, _i, _cp, C.POINTER(_sz)]),
+    "clc_transform_compile": (_i, [_cp, _i, _i, _i, _i, _cp, _sz]),
     "clc_add_header": (_i, [_vp, _cp, _cp]),
     "clc_kernel_create": (_i, [_vp, _cp, _cp, _cp, _vp, _vp, _sz, C.POINTER(_vp)]),
     "clc_kernel_release": (None, [_vp]),
@@ -431,6 +437,40 @@ def sequence(ctx: Context, out: DeviceBuffer, start=0, step=1) -> None:
     s, d = _scalar(out.dtype, start), _scalar(out.dtype, step)
     _raise_for(lib.clc_sequence(ctx.handle, out.handle, out.size, clc_type(out.dtype),
                                 s.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p)))
+
+
+def transform(ctx: Context, a: DeviceBuffer, b: DeviceBuffer, c, d: str | None = None) -> None:
+    """Element-wise transform (reference Algorithm.hpp:135-157), both overloads:
+    ``transform(ctx, inp, out, expression)`` computes out[i] = expression(x =
+    inp[i]); ``transform(ctx, in1, in2, out, expression)`` computes out[i] =
+    expression(x = in1[i], y = in2[i]), and out may alias an input. The
+    expression is OpenCL C from the subset the library compiles (operators,
+    casts, literals, min/max/clamp/abs/fabs/as_T/convert_T); a malformed one
+    raises BuildError, one outside the subset UnsupportedError."""
+    if d is None:
+        inp, out, expression = a, b, c
+        if out.size < inp.size:
+            raise ValueError("transform: output too small")
+        _raise_for(lib.clc_transform(ctx.handle, inp.handle, clc_type(inp.dtype), out.handle, clc_type(out.dtype),
+                                     inp.size, expression.encode()))
+        return
+    in1, in2, out, expression = a, b, c, d
+    if in2.size < in1.size or out.size < in1.size:
+        raise ValueError("transform: size mismatch")
+    _raise_for(lib.clc_transform2(ctx.handle, in1.handle, clc_type(in1.dtype), in2.handle, clc_type(in2.dtype),
+                                  out.handle, clc_type(out.dtype), in1.size, expression.encode()))
+
+
+def transform_compile(expression: str, in_dtype, out_dtype, in2_dtype=None) -> str:
+    """Compiles a transform expression without a device; returns the program
+    listing (one operation per line). Raises BuildError / UnsupportedError as
+    transform does."""
+    buf = C.create_string_buffer(8192)
+    has2 = in2_dtype is not None
+    _raise_for(lib.clc_transform_compile(expression.encode(), clc_type(in_dtype), int(has2),
+                                         clc_type(in2_dtype if has2 else in_dtype), clc_type(out_dtype),
+                                         buf, len(buf)))
+    return buf.value.decode()
 
 
 def reduce(ctx: Context, inp: DeviceBuffer, op: binary_op | None = None, init=0):

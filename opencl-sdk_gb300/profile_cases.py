@@ -7,7 +7,8 @@ Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
 (u64 keys + u32 values), scan-i32 (exclusive, int64 total), reduce-i32,
 hist-u8 (256 bins), segsort-u64kv (lognormal segments, median 256, sigma 2,
 n = total keys), rbk-u64 (reduce_by_key over sorted keys with runs, fused
-65,536-bin histogram), copy-if-i32 ("x > 0"). Inputs are seeded synthetic
+65,536-bin histogram), copy-if-i32 ("x > 0"), transform-u32f32 ("x * 0.18f +
+32.0f", uint -> float), transform2-u32 ("x + y"). Inputs are seeded synthetic
 data generated on the device; every call goes through the C ABI on the
 library's stream.
 """
@@ -113,6 +114,18 @@ def main() -> None:
 
         def step():
             gbc.copy_if(ctx, xb, yb, "x > 0")
+    elif args.case in ("transform-u32f32", "transform2-u32"):
+        x, y = u32(n), u32(n)
+        o = torch.empty(n, dtype=torch.int32, device="cuda")
+        xb = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), n, np.uint32)
+        yb = gbc.DeviceBuffer.wrap(ctx, y.data_ptr(), n, np.uint32)
+        ob = gbc.DeviceBuffer.wrap(ctx, o.data_ptr(), n, np.float32 if args.case == "transform-u32f32" else np.uint32)
+
+        def step():
+            if args.case == "transform-u32f32":
+                gbc.transform(ctx, xb, ob, "x * 0.18f + 32.0f")
+            else:
+                gbc.transform(ctx, xb, yb, ob, "x + y")
     else:
         raise SystemExit(f"unknown case {args.case}")
 

@@ -5,7 +5,8 @@ import os
 
 import numpy as np
 
-GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_recipes.json")))
+with open(os.path.join(os.path.dirname(__file__), "golden", "reference_recipes.json")) as _f:
+    GOLDEN = json.load(_f)
 SIZES = GOLDEN["sizes"]  # lib/test/Compute/main.cpp:54
 
 

@@ -69,8 +69,9 @@ def test_null_arguments_and_stubs(gbc):
     L.clc_buffer_release(None)  # no-op
     L.clc_context_release(None)
     assert L.clc_buffer_size(None) == 0
+    assert L.clc_transform(None, None, 4, None, 8, 10, b"(float)x") == gbc.ERROR_INVALID_ARGUMENT
+    assert L.clc_transform2(None, None, 4, None, 4, None, 4, 10, b"x + y") == gbc.ERROR_INVALID_ARGUMENT
     # out-of-scope entry points link and report UNSUPPORTED
-    assert L.clc_transform(None, None, 4, None, 8, 10, b"(float)x") == gbc.ERROR_UNSUPPORTED
     done = C.c_size_t(7)
     assert L.clc_file_read(None, b"x", 0, None, 0, 0, C.byref(done)) == gbc.ERROR_UNSUPPORTED and done.value == 0
     k = C.c_void_p(1)

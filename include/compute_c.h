@@ -352,7 +352,7 @@ GBC_EXPORT clc_status clc_reduce_raw(clc_context ctx, const void* in, size_t n, 
  * allocator, a fixed arena on a shared GPU) and code that cannot afford the
  * device-wide synchronisation of cudaFree. The call allocates nothing and
  * needs no clc_context: its scratch (one look-back status word per tile of
- * 4,096 elements, and a tile counter) is a fixed 512 KiB array inside the
+ * 16,384 elements, and a tile counter) is a fixed 128 KiB array inside the
  * library, so n is limited to 2^28 elements; larger n returns
  * CLC_ERROR_INVALID_ARGUMENT without launching anything.
  *

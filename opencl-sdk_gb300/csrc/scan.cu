@@ -124,9 +124,9 @@ template <typename T> __device__ __forceinline__ void store_wide(void* dst, T v)
     }
 }
 
-template <typename T> struct ScanShape {
+template <typename T, int ROWS_ = 8> struct ScanShape {
     static constexpr int VEC = 16 / sizeof(T);
-    static constexpr int ROWS = 8;
+    static constexpr int ROWS = ROWS_;
     static constexpr int TILE = THREADS * VEC * ROWS;
     static constexpr int RW = ROWS * (THREADS / 32);
     static constexpr int PER = RW / 32;
@@ -136,14 +136,14 @@ template <typename T> struct ScanShape {
 // One tile after its elements x are in registers: wide sum, warp scans, the
 // row-warp scan and look-back (warp 0), then the outputs. Contains CTA
 // barriers: every thread of the CTA calls it.
-template <typename T, typename Op, bool WIDE_SUM>
-__device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape<T>::ROWS][ScanShape<T>::VEC],
+template <typename T, typename Op, bool WIDE_SUM, int ROWS_>
+__device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ROWS_][ScanShape<T, ROWS_>::VEC],
                                           uint32_t t, uint32_t base, bool full, T* s_rw, T& s_prefix,
                                           unsigned long long& wide)
 {
-    constexpr int VEC = ScanShape<T>::VEC;
-    constexpr int ROWS = ScanShape<T>::ROWS;
-    constexpr int PER = ScanShape<T>::PER;
+    constexpr int VEC = ScanShape<T, ROWS_>::VEC;
+    constexpr int ROWS = ROWS_;
+    constexpr int PER = ScanShape<T, ROWS_>::PER;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const Op op;
     const T identity = a.identity;
@@ -291,11 +291,13 @@ __device__ __forceinline__ void scan_tile(const ScanArgs<T>& a, T (&x)[ScanShape
 }
 
 // Latency-bound: each SM needs several tiles in flight, so the register
-// budget is capped for 4 CTAs per SM (2 for 8-byte elements).
-template <typename T, typename Op, bool WIDE_SUM>
-__global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 4 : 2) k_scan(ScanArgs<T> a)
+// budget is capped for MINB CTAs per SM (by default 4, 2 for 8-byte
+// elements). PF: L2 prefetch distance in grids of tiles (0: none).
+template <typename T, typename Op, bool WIDE_SUM, int ROWS_ = 8, int MINB = (sizeof(T) == 4 ? 4 : 2),
+          int PF = PREFETCH_GRIDS>
+__global__ void __launch_bounds__(THREADS, MINB) k_scan(ScanArgs<T> a)
 {
-    using S = ScanShape<T>;
+    using S = ScanShape<T, ROWS_>;
     __shared__ T s_rw[S::RW];
     __shared__ T s_prefix;
     __shared__ uint32_t s_tile;
@@ -308,8 +310,8 @@ __global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 4 : 2) k_scan(ScanAr
         // many tile-times from now, is prefetched into L2.
         if (tid == 0) {
             s_tile = atomicAdd(a.tile_ctr, 1u);
-            const uint64_t ahead = (uint64_t)s_tile + PREFETCH_GRIDS * gridDim.x;
-            if (a.aligned && (ahead + 1) * S::TILE <= a.n)
+            const uint64_t ahead = (uint64_t)s_tile + PF * gridDim.x;
+            if (PF > 0 && a.aligned && (ahead + 1) * S::TILE <= a.n)
                 dev::prefetch_l2(a.in + ahead * S::TILE, S::TILE * sizeof(T));
         }
         __syncthreads();
@@ -333,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 4 : 2) k_scan(ScanAr
                     x[r][j] = idx < a.n ? a.in[idx] : a.identity;
                 }
         }
-        scan_tile<T, Op, WIDE_SUM>(a, x, t, base, full, s_rw, s_prefix, wide);
+        scan_tile<T, Op, WIDE_SUM, ROWS_>(a, x, t, base, full, s_rw, s_prefix, wide);
         __syncthreads();
     }
     if (WIDE_SUM) {
@@ -372,10 +374,32 @@ struct ScanLaunch {
     void* total_dev;
     bool wide_plus;
 
+    // Tile shape: 16 rows and 2 CTAs per SM for 4-byte elements, 8 rows for
+    // 8-byte ones, L2 prefetch one grid ahead. Measured on GB300 (exclusive
+    // int32 plus-scan of 2^30 with its int64 total, ms): 16 rows x 2 CTAs
+    // 2.03; 8 x 4 (spills) 2.22; 12 x 3 2.33; 20 x 2 (spills) 2.36; 32 x 1
+    // 2.28; 24 x 1 2.48; 4 x 6 2.77; 4 x 8 3.91; prefetch off 2.38, two grids
+    // ahead 2.23. For int32 plus-scans the tuning table entry "scan:32"
+    // selects 1: 8 rows x 4, 2: 32 rows x 1, 3: 16 rows x 2 without prefetch.
     template <typename T, typename Op> void run()
     {
+        if constexpr (std::is_same<T, int32_t>::value && std::is_same<Op, ops::Plus>::value) {
+            launch_shape sh;
+            switch (ctx.tuning.lookup("scan:32", sh) ? sh.variant : 0) {
+            case 1: run_shape<T, Op, 8, 4, 1>(); return;
+            case 2: run_shape<T, Op, 32, 1, 1>(); return;
+            case 3: run_shape<T, Op, 16, 2, 0>(); return;
+            default: break;
+            }
+        }
+        if constexpr (sizeof(T) == 4) run_shape<T, Op, 16, 2, PREFETCH_GRIDS>();
+        else run_shape<T, Op, 8, 2, PREFETCH_GRIDS>();
+    }
+
+    template <typename T, typename Op, int ROWS_, int MINB, int PF> void run_shape()
+    {
         constexpr int VEC = 16 / sizeof(T);
-        constexpr uint32_t TILE = ScanShape<T>::TILE;
+        constexpr uint32_t TILE = ScanShape<T, ROWS_>::TILE;
         constexpr bool can_wide = std::is_integral<T>::value && sizeof(T) == 4 &&
                                   std::is_same<Op, ops::Plus>::value;
         ScanArgs<T> a;
@@ -401,7 +425,7 @@ struct ScanLaunch {
         // A bulk-copy staged form of this kernel measured slower: a CTA that
         // takes its next tile early publishes that tile's status late, which
         // stalls every successor's look-back.
-        auto kernel = use_wide ? &k_scan<T, Op, can_wide> : &k_scan<T, Op, false>;
+        auto kernel = use_wide ? &k_scan<T, Op, can_wide, ROWS_, MINB, PF> : &k_scan<T, Op, false, ROWS_, MINB, PF>;
         const std::size_t smem = 0;
         const int grid =
             (int)std::min<std::size_t>(a.num_tiles, (std::size_t)ctx.sm_count * blocks_per_sm(kernel, smem));
@@ -474,16 +498,17 @@ void scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t,
 // it needs no clc_context (creating one allocates). The caller passes the
 // input, the output and the stream.
 //
-// The array holds 65,536 tiles of 4,096 elements: at most 2^28 elements per
-// call (512 KiB of status words, held by every GPU that loads the library
-// until the process exits). Every call shares it and it keeps the last call's
+// The array holds 16,384 tiles of 16,384 elements (the int32 tile shape of
+// the pooled scan): at most 2^28 elements per call (128 KiB of status words,
+// held by every GPU that loads the library until the process exits). Every call shares it and it keeps the last call's
 // contents, so each call first clears the words it will read; calls whose
 // work overlaps on the GPU (different streams, or different host threads)
 // race on it and must be serialised by the caller.
 // ---------------------------------------------------------------------------
 namespace noalloc {
 
-constexpr uint32_t TILE = ScanShape<int32_t>::TILE;  // the int32 tile of k_scan
+constexpr int ROWS = 16, MINB = 2;  // the int32 shape of the pooled scan
+constexpr uint32_t TILE = ScanShape<int32_t, ROWS>::TILE;
 constexpr std::size_t MAX_ELEMENTS = std::size_t(1) << 28;
 constexpr uint32_t MAX_TILES = (uint32_t)(MAX_ELEMENTS / TILE);
 
@@ -511,7 +536,8 @@ device_setup setup_current_device(int dev)
     s.scratch = static_cast<uint64_t*>(p);
     int sms = 0, blocks = 0;
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, &k_scan<int32_t, ops::Plus, false>, THREADS, 0),
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &blocks, &k_scan<int32_t, ops::Plus, false, ROWS, MINB, PREFETCH_GRIDS>, THREADS, 0),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     s.grid_cap = sms * std::max(blocks, 1);
     g_setup[dev] = s;
@@ -560,7 +586,7 @@ extern "C" clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size
         a.total = nullptr;
         a.err = nullptr;  // a wait that runs out ends the kernel; there is no context to report to
         const int grid = (int)std::min<uint32_t>(num_tiles, (uint32_t)s.grid_cap);
-        k_scan<int32_t, ops::Plus, false><<<grid, THREADS, 0, st>>>(a);
+        k_scan<int32_t, ops::Plus, false, noalloc::ROWS, noalloc::MINB, PREFETCH_GRIDS><<<grid, THREADS, 0, st>>>(a);
         check_cuda(cudaGetLastError(), "clc_scan_i32_noalloc launch");
         return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
     } catch (const device_error& e) {

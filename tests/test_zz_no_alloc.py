@@ -42,7 +42,7 @@ def test_noalloc_scan_matches_regular_scan_twice(gbc, ctx):
 
 
 def test_noalloc_scan_in_place_and_limits(gbc, ctx):
-    x = (np.arange(4096 * 3 + 17, dtype=np.int64) % 13 - 6).astype(np.int32)
+    x = (np.arange(16384 * 3 + 17, dtype=np.int64) % 13 - 6).astype(np.int32)  # 3 tiles and a partial one
     xb = gbc.DeviceBuffer.from_host(ctx, x)
     expected = _regular_scan(gbc, ctx, xb, x.size, False)
     p = C.c_void_p(xb.device_pointer)

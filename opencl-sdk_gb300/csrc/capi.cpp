@@ -525,8 +525,9 @@ clc_status clc_transform_compile(const char* expression, clc_type in_type, int h
         }
     });
 }
-// copy_if (CApi.cpp:533-545): the predicate comes from a fixed grammar
-// (select.hpp); anything else is CLC_ERROR_UNSUPPORTED.
+// copy_if (CApi.cpp:533-545): the predicate is compiled from the expression
+// subset transform uses (expr.hpp); a malformed one is CLC_ERROR_BUILD, one
+// outside the subset CLC_ERROR_UNSUPPORTED.
 clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n, clc_type type, const char* predicate,
                        size_t* count)
 {
@@ -535,7 +536,7 @@ clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
         *count = 0;
         require_fits(in, n, type);
         require_fits(out, n, type);
-        const gbc::predicate p = gbc::parse_predicate(predicate, elem_of(type));
+        const gbc::xp::program p = gbc::xp::compile_predicate(predicate, elem_of(type));
         *count = gbc::copy_if(*ctx->ctx, in->ptr, out->ptr, n, elem_of(type), p);
     });
 }

@@ -107,6 +107,11 @@ struct program {
 //! output of type tout. Throws build_error or unsupported_error.
 program compile(const std::string& text, elem tx, bool has_y, elem ty2, elem tout);
 
+//! Compiles a copy_if predicate over x of element type tx: the program leaves
+//! an int 1 where the expression is nonzero in its own type (the reference's
+//! `(PRED) ? 1u : 0u`), else 0.
+program compile_predicate(const std::string& text, elem tx);
+
 //! Human-readable listing of a compiled program (tests and diagnostics).
 std::string listing(const program& p);
 

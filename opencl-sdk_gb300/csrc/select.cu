@@ -3,495 +3,311 @@
 //
 // Reference path replaced: detail::copy_if (lib/src/Compute/Algorithm.cpp:
 // 529-567) with its kernels clc_select_flags / clc_select_scatter (216-237):
-// a flag pass, an exclusive scan of the flags into positions and a scatter
-// pass, then a blocking read of the last position and flag. The reference
-// compiles the predicate as an OpenCL C expression over x; here it is parsed
-// from a fixed grammar (comparisons of x, (x % c) or (x & c) with a constant,
-// joined by && or ||) and evaluated with OpenCL C's usual arithmetic
-// conversions. One single-pass kernel: each tile counts its kept elements,
-// finds the count of all earlier tiles by a decoupled look-back and writes
-// its kept elements in order.
-#include <cctype>
-#include <cmath>
+// `flags[i] = (PRED) ? 1u : 0u`, an exclusive scan of the flags into
+// positions, a scatter pass, then a blocking read of the last position and
+// flag. The reference compiles the predicate as OpenCL C over `x`; here it is
+// compiled on the host from the expression subset that transform uses
+// (xp::compile_predicate: the expression's truth value in its own type) and
+// run by the shared interpreter (interp.cuh).
+//
+// Three streaming passes, each warp working alone on its part of a tile (no
+// CTA barrier): evaluate the predicate, store the warp's keep masks (one bit
+// per element) and its count of kept elements; the library's scan turns the
+// counts into offsets and their exact total; read the part and its masks
+// again, compact the kept elements in the warp's shared memory and write
+// them as one run at the warp's offset.
+// Each thread runs the program over RUN elements at a time, so an
+// operation's dispatch is shared by RUN elements. (Measured on
+// GB300, 2^30 int32 "x > 0": a single-pass form with a decoupled look-back
+// and a per-element evaluator of a fixed grammar took 3.25 ms; the evaluator,
+// not the look-back, was the cost.)
 #include <cstring>
 
 #include "device_common.cuh"
+#include "interp.cuh"
 #include "select.hpp"
-#include "sort_internal.hpp"
 
 namespace gbc {
-
-// ---- predicate grammar ------------------------------------------------------
 namespace {
 
-struct lexer {
-    const std::string& s;
-    std::size_t i = 0;
-    void skip()
-    {
-        while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
-    }
-    bool eat(const char* tok)
-    {
-        skip();
-        const std::size_t k = std::strlen(tok);
-        if (s.compare(i, k, tok) == 0) {
-            i += k;
-            return true;
-        }
-        return false;
-    }
-    bool done()
-    {
-        skip();
-        return i == s.size();
-    }
-};
-
-[[noreturn]] void bad(const std::string& text)
-{
-    throw unsupported_error("copy_if: predicate \"" + text +
-                            "\" is outside the supported grammar (comparisons of x, (x % c) or (x & c) with a "
-                            "constant, joined by && or ||)");
-}
-
-// literal type: 0 int, 1 uint, 2 long, 3 ulong, 4 float, 5 double
-struct literal {
-    int type = 0;
-    int64_t i = 0;
-    double f = 0;
-};
-
-literal parse_literal(lexer& lx, const std::string& text)
-{
-    lx.skip();
-    const char* b = lx.s.c_str() + lx.i;
-    bool neg = false;
-    if (*b == '-' || *b == '+') {
-        neg = *b == '-';
-        ++b;
-    }
-    const char* p = b;
-    literal L;
-    bool is_float = false;
-    while (std::isdigit((unsigned char)*p) || *p == '.' || *p == 'e' || *p == 'E' ||
-           ((*p == '-' || *p == '+') && (p[-1] == 'e' || p[-1] == 'E')) || (*p == 'x' || *p == 'X') ||
-           (std::isxdigit((unsigned char)*p) && (b[0] == '0' && (b[1] == 'x' || b[1] == 'X')))) {
-        if (*p == '.' || ((*p == 'e' || *p == 'E') && !(b[0] == '0' && (b[1] == 'x' || b[1] == 'X')))) is_float = true;
-        ++p;
-    }
-    if (p == b) bad(text);
-    const std::string digits(b, p);
-    bool u = false, l = false, f = false;
-    while (*p == 'u' || *p == 'U' || *p == 'l' || *p == 'L' || *p == 'f' || *p == 'F') {
-        if (*p == 'u' || *p == 'U') u = true;
-        else if (*p == 'l' || *p == 'L') l = true;
-        else f = true;
-        ++p;
-    }
-    if (std::isalnum((unsigned char)*p) || *p == '_') bad(text);
-    lx.i = (std::size_t)(p - lx.s.c_str());
-    if (is_float || f) {
-        if (u || l) bad(text);
-        L.type = f ? 4 : 5;
-        L.f = std::strtod(digits.c_str(), nullptr);
-        if (f) L.f = (double)(float)L.f;
-        if (neg) L.f = -L.f;
-        return L;
-    }
-    errno = 0;
-    const unsigned long long v = std::strtoull(digits.c_str(), nullptr, 0);
-    if (errno != 0) bad(text);
-    // the type of an integer constant: the first of int, uint, long, ulong
-    // (decimal without u: int, long) that holds it, as in C
-    const bool decimal = !(digits.size() > 1 && digits[0] == '0');
-    if (!u && !l && v <= 0x7FFFFFFFull) L.type = 0;
-    else if (!l && (u || !decimal) && v <= 0xFFFFFFFFull) L.type = 1;
-    else if (!u && v <= 0x7FFFFFFFFFFFFFFFull) L.type = 2;
-    else L.type = 3;
-    L.i = (int64_t)v;
-    if (neg) L.i = -L.i;  // unary minus applies in the literal's type below
-    return L;
-}
-
-// element type -> operand type after integer promotion
-int promoted(elem t)
-{
-    switch (t) {
-    case elem::i8: case elem::u8: case elem::i16: case elem::u16: case elem::i32: return 0;
-    case elem::u32: return 1;
-    case elem::i64: return 2;
-    case elem::u64: return 3;
-    case elem::f32: return 4;
-    default: return 5;
-    }
-}
-
-// usual arithmetic conversions for the type codes above
-int common(int a, int b)
-{
-    if (a >= 4 || b >= 4) return std::max(a, b);
-    const int ra = a >> 1, rb = b >> 1;  // rank: 0 (32-bit), 1 (64-bit)
-    const bool ua = a & 1, ub = b & 1;
-    if (ra == rb) return (ra << 1) | (ua || ub);
-    const int hi = ra > rb ? a : b, lo = ra > rb ? b : a;
-    // the 64-bit type holds every 32-bit value, so signedness follows it
-    (void)lo;
-    return hi;
-}
-
-pred_clause parse_clause(lexer& lx, elem t, const std::string& text)
-{
-    pred_clause c;
-    int lhs_type = promoted(t);
-    if (lx.eat("(")) {
-        if (!lx.eat("x")) bad(text);
-        if (lx.eat("%")) c.lhs = 1;
-        else if (lx.eat("&")) c.lhs = 2;
-        else bad(text);
-        const literal m = parse_literal(lx, text);
-        if (!lx.eat(")")) bad(text);
-        if (lhs_type >= 4 || m.type >= 4) bad(text);  // % and & need integers
-        lhs_type = common(lhs_type, m.type);
-        c.m_i = m.i;
-        if (c.lhs == 1 && m.i == 0) bad(text);
-    } else if (!lx.eat("x")) {
-        bad(text);
-    }
-    if (lx.eat("<=")) c.cmp = 1;
-    else if (lx.eat(">=")) c.cmp = 3;
-    else if (lx.eat("==")) c.cmp = 4;
-    else if (lx.eat("!=")) c.cmp = 5;
-    else if (lx.eat("<")) c.cmp = 0;
-    else if (lx.eat(">")) c.cmp = 2;
-    else bad(text);
-    const literal k = parse_literal(lx, text);
-    c.ctype = common(lhs_type, k.type);
-    c.c_i = k.type >= 4 ? (int64_t)k.f : k.i;
-    c.c_f = k.type >= 4 ? k.f : (double)k.i;
-    if (k.type < 4 && (k.type & 1) && k.i < 0) c.c_f = (double)(uint64_t)k.i;
-    return c;
-}
-
-}  // namespace
-
-predicate parse_predicate(const std::string& text, elem t)
-{
-    lexer lx{text};
-    predicate p;
-    for (;;) {
-        if (p.count == 4) bad(text);
-        p.c[p.count++] = parse_clause(lx, t, text);
-        if (lx.done()) break;
-        const int join = lx.eat("&&") ? 0 : lx.eat("||") ? 1 : -1;
-        if (join < 0 || (p.count > 1 && join != p.join)) bad(text);
-        p.join = join;
-    }
-    return p;
-}
-
-// ---- device -------------------------------------------------------------------
-namespace {
-
+using namespace xp;
+using namespace xp::interp;
 using dev::FULL_MASK;
+
 constexpr int THREADS = 256;
-constexpr int LB_PER_LANE = 4;
-constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
-constexpr uint64_t TAG_MASK = (1ull << 30) - 1;
-constexpr uint64_t SLOTS = onesweep::RING_BYTES / 8;
+constexpr int WARPS = THREADS / 32;
 
-// A clause flattened for the device: the operand path (0 int32, 1 uint32,
-// 2 int64, 3 uint64, 4 double, which is exact for float operands and
-// literals), the left side, and the result for each ordering of lhs against
-// the constant (less, equal, greater, unordered: NaN), so that no switch on
-// the comparison is needed.
-struct dclause {
-    int kind;
-    int lhs;  // 0: x, 1: x % m, 2: x & m
-    int64_t m, c;
-    double cf;
-    bool lt, eq, gt, un;
-};
-struct dpredicate {
-    int count, join;
-    dclause c[4];
+// Elements of SZ bytes; each thread holds ITEMS of them as ROWS rows of V =
+// 16 / SZ (one 128-bit access per row). Row r of warp w covers tile elements
+// (w * ROWS + r) * 32 V + lane V + q, q < V; the thread's element j = r V + q.
+// All of a thread's loads are issued first; the predicate then runs over
+// RUN elements at a time (fewer registers than all ITEMS at once).
+template <int SZ> struct SelShape {
+    static constexpr int ITEMS = SZ == 8 ? 8 : 16;
+    static constexpr int RUN = 8;
+    static constexpr int V = 16 / SZ;
+    static constexpr int ROWS = ITEMS / V;
+    static constexpr int TILE = THREADS * ITEMS;
+    static constexpr int WARP_ELEMS = ROWS * 32 * V;
+    static constexpr int WORDS = ITEMS * SZ / 4;  // 32-bit words per thread
+    static_assert(ITEMS % RUN == 0 && ITEMS <= 32, "whole runs; one mask word per lane");
 };
 
-template <typename I, typename T> __device__ __forceinline__ int order_int(T x, const dclause& c)
-{
-    I v = (I)x;
-    if (c.lhs == 1) v = (I)(v % (I)c.m);
-    else if (c.lhs == 2) v = (I)(v & (I)c.m);
-    const I k = (I)c.c;
-    return v < k ? 0 : (v == k ? 1 : 2);
-}
-
-// (if-else rather than switch: a jump table costs an indirect branch per
-// element and stalls instruction fetch)
-template <typename T> __device__ __forceinline__ bool clause_eval(T x, const dclause& c)
-{
-    int o;
-    if (c.kind == 0) o = order_int<int32_t>(x, c);
-    else if (c.kind == 1) o = order_int<uint32_t>(x, c);
-    else if (c.kind == 2) o = order_int<int64_t>(x, c);
-    else if (c.kind == 3) o = order_int<uint64_t>(x, c);
-    else {
-        const double v = (double)x;
-        o = v < c.cf ? 0 : (v == c.cf ? 1 : (v > c.cf ? 2 : 3));
-    }
-    return o == 0 ? c.lt : (o == 1 ? c.eq : (o == 2 ? c.gt : c.un));
-}
-
-template <typename T> __device__ __forceinline__ bool eval(T x, const dpredicate& p)
-{
-    bool r = clause_eval(x, p.c[0]);
-    // unrolled with guards: constant indices keep the clauses in the
-    // parameter space (a run-time index would copy them to local memory)
-#pragma unroll
-    for (int k = 1; k < 4; ++k)
-        if (k < p.count) r = p.join ? (r || clause_eval(x, p.c[k])) : (r && clause_eval(x, p.c[k]));
-    return r;
-}
-
-template <typename T> struct SelArgs {
-    const T* in;
-    T* out;
+struct SelArgs {
+    const unsigned char* in;
+    unsigned char* out;
     uint32_t n;
-    dpredicate p;
-    uint32_t num_tiles;
-    uint64_t* ring;
-    uint64_t seq0;
-    uint32_t* tile_ctr;
-    uint32_t* total;  // written by the last tile
-    int* err;
+    uint32_t* tiles;  // per tile and warp: kept elements (count pass), then their exclusive offsets
+    uint32_t* masks;  // per tile and warp: ITEMS keep masks (count pass), read by the scatter pass
 };
 
-__device__ __forceinline__ void publish(uint64_t* ring, uint64_t seq, uint64_t flag, uint32_t v)
+template <int SZ, int WORDS>
+__device__ __forceinline__ uint64_t raw_elem(const uint32_t (&w)[WORDS], int j)
 {
-    dev::st_relaxed(&ring[seq & (SLOTS - 1)], (flag << 62) | ((seq & TAG_MASK) << 32) | v);
-}
-__device__ __forceinline__ bool read_status(const uint64_t* ring, uint64_t seq, uint64_t& flag, uint32_t& v)
-{
-    const uint64_t w = dev::ld_relaxed(&ring[seq & (SLOTS - 1)]);
-    flag = w >> 62;
-    if (flag == 0 || ((w >> 32) & TAG_MASK) != (seq & TAG_MASK)) return false;
-    v = (uint32_t)w;
-    return true;
+    if constexpr (SZ == 1) return (w[j / 4] >> (8 * (j % 4))) & 0xFFu;
+    else if constexpr (SZ == 2) return (w[j / 2] >> (16 * (j % 2))) & 0xFFFFu;
+    else if constexpr (SZ == 4) return w[j];
+    else return ((uint64_t)w[2 * j + 1] << 32) | w[2 * j];
 }
 
-// Tile: THREADS x ITEMS elements; warp w owns ROWS = ITEMS / V rows of 32 x V
-// consecutive elements (V = 16 / sizeof(T): one 128-bit load per lane and
-// row), row r at tile_base + (w * ROWS + r) * 32 V, lane l holding elements
-// l V .. l V + V - 1 of the row. A ballot per element slot gives the row's
-// keep masks; an element's place among the row's kept ones is the number of
-// kept elements in lower lanes (sum over the slots of popc(mask & lower
-// lanes)) plus the lane's own kept elements before it. The rows are visited
-// by loops that are not unrolled, so the predicate's evaluator appears once
-// in the code (unrolled, its copies overflowed the instruction cache).
-template <typename T, int ITEMS> __global__ void __launch_bounds__(THREADS) k_copy_if(SelArgs<T> a)
+// The thread's elements as raw words; elements past n are 0 (the callers
+// flag them out).
+template <int SZ>
+__device__ __forceinline__ void load_raw(const SelArgs& a, uint32_t wbase, int lane, uint32_t (&w)[SelShape<SZ>::WORDS])
 {
-    constexpr int WARPS = THREADS / 32;
-    constexpr int TILE = THREADS * ITEMS;
-    constexpr int V = 16 / sizeof(T);
-    constexpr int ROWS = ITEMS / V;
-    static_assert(ITEMS % V == 0, "whole 128-bit rows");
-    __shared__ __align__(16) T s_in[TILE];
-    __shared__ uint32_t s_mask[WARPS * ROWS * V];
-    __shared__ uint32_t s_warp[WARPS];
-    __shared__ uint32_t s_prefix;
-    __shared__ uint32_t s_tile;
-    __shared__ dpredicate s_p;
+    using S = SelShape<SZ>;
+    if (((reinterpret_cast<uintptr_t>(a.in) & 15) == 0) && wbase + S::WARP_ELEMS <= a.n) {
+#pragma unroll
+        for (int r = 0; r < S::ROWS; ++r) {
+            const uint4 u = dev::ld_stream(
+                reinterpret_cast<const uint4*>(a.in + ((std::size_t)wbase + (r * 32 + lane) * S::V) * SZ));
+            w[4 * r] = u.x, w[4 * r + 1] = u.y, w[4 * r + 2] = u.z, w[4 * r + 3] = u.w;
+        }
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < S::WORDS; ++k) w[k] = 0;
+#pragma unroll
+    for (int r = 0; r < S::ROWS; ++r)
+#pragma unroll
+        for (int q = 0; q < S::V; ++q) {
+            const uint32_t idx = wbase + (r * 32 + lane) * S::V + q;
+            if (idx < a.n) {
+                const unsigned char* s = a.in + (std::size_t)idx * SZ;
+                const int j = r * S::V + q;
+                if constexpr (SZ == 1) w[j / 4] |= (uint32_t)*s << (8 * (j % 4));
+                else if constexpr (SZ == 2) w[j / 2] |= (uint32_t)*reinterpret_cast<const uint16_t*>(s) << (16 * (j % 2));
+                else if constexpr (SZ == 4) w[j] = *reinterpret_cast<const uint32_t*>(s);
+                else {
+                    const uint64_t v = *reinterpret_cast<const uint64_t*>(s);
+                    w[2 * j] = (uint32_t)v;
+                    w[2 * j + 1] = (uint32_t)(v >> 32);
+                }
+            }
+        }
+}
+
+// Elements first .. first + RUN - 1 of the thread, promoted to the program's
+// registers (char and short sign-extended, unsigned narrow types zero-extended).
+template <int SZ, typename W, int FIRST>
+__device__ __forceinline__ void promote_run(uint8_t e, const uint32_t (&w)[SelShape<SZ>::WORDS],
+                                            W (&xv)[SelShape<SZ>::RUN])
+{
+    using S = SelShape<SZ>;
+    if constexpr (SZ >= 4) {
+#pragma unroll
+        for (int i = 0; i < S::RUN; ++i) xv[i] = (W)raw_elem<SZ, S::WORDS>(w, FIRST + i);
+    } else if (e == (uint8_t)elem::i8 || e == (uint8_t)elem::i16) {
+#pragma unroll
+        for (int i = 0; i < S::RUN; ++i) {
+            const uint32_t r = (uint32_t)raw_elem<SZ, S::WORDS>(w, FIRST + i);
+            xv[i] = put<W>(SZ == 1 ? (int32_t)(int8_t)(uint8_t)r : (int32_t)(int16_t)(uint16_t)r);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < S::RUN; ++i) xv[i] = (W)raw_elem<SZ, S::WORDS>(w, FIRST + i);
+    }
+}
+
+// The program over elements FIRST .. FIRST + RUN - 1; a ballot per element
+// slot; lane j keeps slot j's mask.
+template <int SZ, typename W, bool STK, int FIRST>
+__device__ __forceinline__ void flag_run(const program& p, const uint32_t (&w)[SelShape<SZ>::WORDS], W* st,
+                                         uint32_t wbase, uint32_t n, bool whole, int lane, uint32_t& count,
+                                         uint32_t& mine)
+{
+    using S = SelShape<SZ>;
+    W xv[S::RUN], acc[S::RUN];
+    promote_run<SZ, W, FIRST>(p.x_elem, w, xv);
+    run_program<W, S::RUN, STK, THREADS>(p, acc, xv, xv, st);
+#pragma unroll
+    for (int i = 0; i < S::RUN; ++i) {
+        const int j = FIRST + i;
+        const bool keep = (uint32_t)acc[i] != 0u && (whole || wbase + ((j / S::V) * 32 + lane) * S::V + j % S::V < n);
+        const uint32_t m = __ballot_sync(FULL_MASK, keep);
+        count += __popc(m);
+        if (lane == j) mine = m;
+    }
+}
+
+// Pass 1, per warp (no CTA barrier): the keep masks of the warp's ITEMS
+// element slots, stored for pass 3 (which then evaluates nothing), and its
+// count of kept elements.
+template <int SZ, typename W, bool STK>
+__global__ void __launch_bounds__(THREADS) k_sel_count(SelArgs a, const __grid_constant__ program p)
+{
+    using S = SelShape<SZ>;
+    extern __shared__ __align__(16) unsigned char sel_smem[];  // STK: the program's stack slots
+    W* st = reinterpret_cast<W*>(sel_smem);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_p = a.p;
+    const uint32_t t = blockIdx.x;
+    const uint32_t wbase = t * S::TILE + warp * S::WARP_ELEMS;
+    uint32_t w[S::WORDS];
+    load_raw<SZ>(a, wbase, lane, w);
+    const bool whole = wbase + S::WARP_ELEMS <= a.n;
+    uint32_t count = 0, mine = 0;
+    flag_run<SZ, W, STK, 0>(p, w, st, wbase, a.n, whole, lane, count, mine);
+    if constexpr (S::ITEMS > S::RUN) flag_run<SZ, W, STK, S::RUN>(p, w, st, wbase, a.n, whole, lane, count, mine);
+    const std::size_t wi = (std::size_t)t * WARPS + warp;
+    if (lane < S::ITEMS) a.masks[wi * S::ITEMS + lane] = mine;
+    if (lane == 0) a.tiles[wi] = count;
+}
+
+// Pass 3 (after the exclusive scan of the warp counts), per warp: an
+// element's place among the warp's kept ones is the kept elements of earlier
+// rows, of lower lanes in its row (sum over the slots of popc(mask & lower
+// lanes)) and of its own earlier slots; the warp compacts its kept elements
+// in its part of shared memory and writes them as one run at its offset.
+template <int SZ>
+__global__ void __launch_bounds__(THREADS) k_sel_scatter(SelArgs a)
+{
+    using S = SelShape<SZ>;
+    __shared__ __align__(16) unsigned char s_out[WARPS][S::WARP_ELEMS * SZ];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lt_mask = dev::lanemask_lt();
-    const bool aligned = (reinterpret_cast<uintptr_t>(a.in) & 15) == 0;
-    for (;;) {
-        if (tid == 0) {
-            // taken only when the CTA can start on it; the tile a grid ahead
-            // is prefetched into L2 (cf. the scan)
-            s_tile = atomicAdd(a.tile_ctr, 1u);
-            const uint64_t ahead = (uint64_t)s_tile + gridDim.x;
-            if (aligned && (ahead + 1) * TILE <= a.n) dev::prefetch_l2(a.in + ahead * TILE, TILE * sizeof(T));
+    const uint32_t t = blockIdx.x;
+    const uint32_t wbase = t * S::TILE + warp * S::WARP_ELEMS;
+    const std::size_t wi = (std::size_t)t * WARPS + warp;
+    const uint32_t mword = lane < S::ITEMS ? a.masks[wi * S::ITEMS + lane] : 0u;
+    const uint32_t base = a.tiles[wi];
+    uint32_t w[S::WORDS];
+    load_raw<SZ>(a, wbase, lane, w);
+    unsigned char* so = s_out[warp];
+    uint32_t pos = 0;
+#pragma unroll
+    for (int r = 0; r < S::ROWS; ++r) {
+        uint32_t m[S::V], below = 0, row_total = 0;
+#pragma unroll
+        for (int q = 0; q < S::V; ++q) {
+            m[q] = __shfl_sync(FULL_MASK, mword, r * S::V + q);
+            below += __popc(m[q] & lt_mask);
+            row_total += __popc(m[q]);
         }
-        __syncthreads();
-        const uint32_t t = s_tile;
-        if (t >= a.num_tiles) break;
-        const uint32_t wbase = t * TILE + warp * ROWS * 32 * V;
-        T* srow = s_in + warp * ROWS * 32 * V;
-        uint32_t count = 0;
-#pragma unroll 1
-        for (int r = 0; r < ROWS; ++r) {
-            const uint32_t first = wbase + (r * 32 + lane) * V;
-            T x[V];
-            if (aligned && first + V <= a.n) {
-                const uint4 w = *reinterpret_cast<const uint4*>(a.in + first);
-                memcpy(x, &w, 16);
-            } else {
+        uint32_t o = pos + below;
 #pragma unroll
-                for (int q = 0; q < V; ++q) x[q] = first + q < a.n ? a.in[first + q] : T(0);
+        for (int q = 0; q < S::V; ++q)
+            if ((m[q] >> lane) & 1u) {
+                const uint64_t v = raw_elem<SZ, S::WORDS>(w, r * S::V + q);
+                unsigned char* d = so + (std::size_t)o * SZ;
+                if constexpr (SZ == 1) *d = (uint8_t)v;
+                else if constexpr (SZ == 2) *reinterpret_cast<uint16_t*>(d) = (uint16_t)v;
+                else if constexpr (SZ == 4) *reinterpret_cast<uint32_t*>(d) = (uint32_t)v;
+                else *reinterpret_cast<uint64_t*>(d) = v;
+                ++o;
             }
-            *reinterpret_cast<uint4*>(srow + (r * 32 + lane) * V) = *reinterpret_cast<const uint4*>(x);
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                const uint32_t m = __ballot_sync(FULL_MASK, first + q < a.n && eval(x[q], s_p));
-                if (lane == 0) s_mask[(warp * ROWS + r) * V + q] = m;
-                count += __popc(m);
-            }
-        }
-        if (lane == 0) s_warp[warp] = count;
-        __syncthreads();
-        if (warp == 0) {
-            const uint32_t wv = lane < WARPS ? s_warp[lane] : 0u;
-            const uint32_t wi = dev::warp_inclusive_scan(wv, [](uint32_t p, uint32_t q) { return p + q; });
-            if (lane < WARPS) s_warp[lane] = wi - wv;
-            const uint32_t agg = __shfl_sync(FULL_MASK, wi, 31);
-            const uint64_t my_seq = a.seq0 + t;
-            if (lane == 0) publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
-            uint32_t excl = 0;
-            if (t > 0) {
-                int64_t w_end = t;
-                bool gave_up = false;
-                for (;;) {
-                    uint64_t flag[LB_PER_LANE];
-                    uint32_t val[LB_PER_LANE];
-#pragma unroll
-                    for (int q = 0; q < LB_PER_LANE; ++q) {
-                        const int64_t k = w_end - 32 * LB_PER_LANE + lane * LB_PER_LANE + q;
-                        flag[q] = FLAG_PRE;
-                        val[q] = 0;
-                        if (k >= 0 && !read_status(a.ring, a.seq0 + (uint64_t)k, flag[q], val[q])) {
-                            const unsigned long long start = dev::globaltimer();
-                            for (uint32_t spin = 1;; ++spin) {
-                                if (read_status(a.ring, a.seq0 + (uint64_t)k, flag[q], val[q])) break;
-                                if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                    gave_up = true;
-                                    flag[q] = FLAG_PRE;
-                                    val[q] = 0;
-                                    break;
-                                }
-                                if (spin > 32) __nanosleep(64);
-                            }
-                        }
-                    }
-                    int hi = -1;
-#pragma unroll
-                    for (int q = 0; q < LB_PER_LANE; ++q)
-                        if (flag[q] == FLAG_PRE) hi = q;
-                    const uint32_t pre = __ballot_sync(FULL_MASK, hi >= 0);
-                    const int L = pre ? 31 - __clz(pre) : -1;
-                    uint32_t contrib = 0;
-                    if (lane >= L) {
-                        const int q0 = lane == L ? hi : 0;
-#pragma unroll
-                        for (int q = 0; q < LB_PER_LANE; ++q)
-                            if (q >= q0) contrib += val[q];
-                    }
-                    excl += dev::warp_reduce(contrib, [](uint32_t p, uint32_t q) { return p + q; });
-                    if (pre) break;
-                    w_end -= 32 * LB_PER_LANE;
-                }
-                if (__any_sync(FULL_MASK, gave_up) && lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                if (lane == 0) publish(a.ring, my_seq, FLAG_PRE, excl + agg);
-            }
-            if (lane == 0) {
-                s_prefix = excl;
-                if (t == a.num_tiles - 1) *a.total = excl + agg;
-            }
-        }
-        __syncthreads();
-        uint32_t pos = s_prefix + s_warp[warp];
-#pragma unroll 1
-        for (int r = 0; r < ROWS; ++r) {
-            uint32_t m[V], below = 0, row_total = 0;
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-                m[q] = s_mask[(warp * ROWS + r) * V + q];
-                below += __popc(m[q] & lt_mask);
-                row_total += __popc(m[q]);
-            }
-            uint32_t o = pos + below;
-            const T* src = srow + (r * 32 + lane) * V;
-#pragma unroll
-            for (int q = 0; q < V; ++q)
-                if ((m[q] >> lane) & 1u) {
-                    if (o < a.n) a.out[o] = src[q];
-                    ++o;
-                }
-            pos += row_total;
-        }
-        __syncthreads();
+        pos += row_total;
+    }
+    __syncwarp();
+    for (uint32_t i = lane; i < pos; i += 32) {
+        if (base + i >= a.n) break;
+        const unsigned char* s = so + (std::size_t)i * SZ;
+        unsigned char* d = a.out + ((std::size_t)base + i) * SZ;
+        if constexpr (SZ == 1) *d = *s;
+        else if constexpr (SZ == 2) *reinterpret_cast<uint16_t*>(d) = *reinterpret_cast<const uint16_t*>(s);
+        else if constexpr (SZ == 4) *reinterpret_cast<uint32_t*>(d) = *reinterpret_cast<const uint32_t*>(s);
+        else *reinterpret_cast<uint64_t*>(d) = *reinterpret_cast<const uint64_t*>(s);
     }
 }
 
-template <typename T>
-void launch_select(device_context& ctx, const void* in, void* out, uint32_t n, const predicate& p, uint32_t* total)
+template <int SZ, typename W, bool STK>
+void run_select(device_context& ctx, const SelArgs& a0, const program& p, unsigned long long* total)
 {
-    constexpr int ITEMS = sizeof(T) <= 4 ? 32 : 16;
-    constexpr uint32_t TILE = THREADS * ITEMS;
-    SelArgs<T> a;
-    a.in = static_cast<const T*>(in);
-    a.out = static_cast<T*>(out);
-    a.n = n;
-    a.p.count = p.count;
-    a.p.join = p.join;
-    for (int k = 0; k < p.count; ++k) {
-        const pred_clause& q = p.c[k];
-        dclause& d = a.p.c[k];
-        d.kind = q.ctype >= 4 ? 4 : q.ctype;
-        d.lhs = q.lhs;
-        d.m = q.m_i;
-        d.c = q.c_i;
-        d.cf = q.ctype == 4 ? (double)(float)q.c_f : q.c_f;  // float compare: the constant in float
-        d.lt = q.cmp == 0 || q.cmp == 1 || q.cmp == 5;
-        d.eq = q.cmp == 1 || q.cmp == 3 || q.cmp == 4;
-        d.gt = q.cmp == 2 || q.cmp == 3 || q.cmp == 5;
-        d.un = q.cmp == 5;  // only != holds for NaN
+    using S = SelShape<SZ>;
+    SelArgs a = a0;
+    const uint32_t num_tiles = (a.n + S::TILE - 1) / S::TILE;
+    const std::size_t slot_bytes = STK ? (std::size_t)STACK * S::RUN * THREADS * sizeof(W) : 0;
+    static const bool ready = [&] {
+        check_cuda(cudaFuncSetAttribute(&k_sel_count<SZ, W, STK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)slot_bytes),
+                   "cudaFuncSetAttribute");
+        return true;
+    }();
+    (void)ready;
+    temp_buffer tiles(ctx.resource, (std::size_t)num_tiles * WARPS * sizeof(uint32_t));
+    temp_buffer masks(ctx.resource, (std::size_t)num_tiles * WARPS * S::ITEMS * sizeof(uint32_t));
+    a.tiles = tiles.as<uint32_t>();
+    a.masks = masks.as<uint32_t>();
+    {
+        kernel_timer kt(ctx, "select.count");
+        k_sel_count<SZ, W, STK><<<num_tiles, THREADS, slot_bytes, ctx.stream>>>(a, p);
+        check_cuda(cudaGetLastError(), "copy_if count launch");
     }
-    a.num_tiles = (n + TILE - 1) / TILE;
-    a.ring = ctx.lookback_ring;
-    a.seq0 = ctx.reserve_seq(a.num_tiles);
-    unsigned char* ctl = ctx.d_small + 2048;
-    check_cuda(cudaMemsetAsync(ctl, 0, 16, ctx.stream), "cudaMemsetAsync");
-    a.tile_ctr = reinterpret_cast<uint32_t*>(ctl);
-    a.total = total;
-    a.err = ctx.d_error;
-    int per_sm = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, &k_copy_if<T, ITEMS>, THREADS, 0),
-               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    const int grid = (int)std::min<std::size_t>(a.num_tiles, (std::size_t)ctx.sm_count * std::max(per_sm, 1));
-    kernel_timer kt(ctx, "select.copy_if");
-    k_copy_if<T, ITEMS><<<grid, THREADS, 0, ctx.stream>>>(a);
-    check_cuda(cudaGetLastError(), "copy_if launch");
+    const uint32_t zero = 0;
+    scan(ctx, a.tiles, a.tiles, (std::size_t)num_tiles * WARPS, elem::u32, op_kind::plus, &zero, true, total);
+    {
+        kernel_timer kt(ctx, "select.scatter");
+        k_sel_scatter<SZ><<<num_tiles, THREADS, 0, ctx.stream>>>(a);
+        check_cuda(cudaGetLastError(), "copy_if scatter launch");
+    }
+}
+
+template <int SZ>
+void dispatch(device_context& ctx, const SelArgs& a, const program& p, unsigned long long* total)
+{
+    const bool stk = uses_stack(p);
+    if constexpr (SZ == 8) {
+        if (stk) run_select<SZ, uint64_t, true>(ctx, a, p, total);
+        else run_select<SZ, uint64_t, false>(ctx, a, p, total);
+    } else {
+        if (all_32bit(p)) {
+            if (stk) run_select<SZ, uint32_t, true>(ctx, a, p, total);
+            else run_select<SZ, uint32_t, false>(ctx, a, p, total);
+        } else {
+            if (stk) run_select<SZ, uint64_t, true>(ctx, a, p, total);
+            else run_select<SZ, uint64_t, false>(ctx, a, p, total);
+        }
+    }
 }
 
 }  // namespace
 
-std::size_t copy_if(device_context& ctx, const void* in, void* out, std::size_t n, elem t, const predicate& p)
+std::size_t copy_if(device_context& ctx, const void* in, void* out, std::size_t n, elem t, const program& p)
 {
     if (n == 0) return 0;
     check_size(n);
     if (in == nullptr || out == nullptr) throw std::invalid_argument("copy_if: null argument");
     if (in == out) throw std::invalid_argument("copy_if: in and out must differ");
+    if (p.nops == 0 || p.nops > (uint32_t)MAX_OPS || p.x_elem != (uint8_t)t)
+        throw std::invalid_argument("copy_if: the predicate was compiled for another element type");
     ctx.activate();
-    uint32_t* total = reinterpret_cast<uint32_t*>(ctx.d_small + 2048 + 16);
-    const uint32_t nn = (uint32_t)n;
-    switch (t) {
-    case elem::i8: launch_select<int8_t>(ctx, in, out, nn, p, total); break;
-    case elem::u8: launch_select<uint8_t>(ctx, in, out, nn, p, total); break;
-    case elem::i16: launch_select<int16_t>(ctx, in, out, nn, p, total); break;
-    case elem::u16: launch_select<uint16_t>(ctx, in, out, nn, p, total); break;
-    case elem::i32: launch_select<int32_t>(ctx, in, out, nn, p, total); break;
-    case elem::u32: launch_select<uint32_t>(ctx, in, out, nn, p, total); break;
-    case elem::i64: launch_select<int64_t>(ctx, in, out, nn, p, total); break;
-    case elem::u64: launch_select<uint64_t>(ctx, in, out, nn, p, total); break;
-    case elem::f32: launch_select<float>(ctx, in, out, nn, p, total); break;
-    case elem::f64: launch_select<double>(ctx, in, out, nn, p, total); break;
+    auto* total = reinterpret_cast<unsigned long long*>(ctx.d_small + 2048 + 16);  // exact sum of the tile counts
+    SelArgs a;
+    a.in = static_cast<const unsigned char*>(in);
+    a.out = static_cast<unsigned char*>(out);
+    a.n = (uint32_t)n;
+    a.tiles = nullptr;
+    a.masks = nullptr;
+    switch (elem_size(t)) {
+    case 1: dispatch<1>(ctx, a, p, total); break;
+    case 2: dispatch<2>(ctx, a, p, total); break;
+    case 4: dispatch<4>(ctx, a, p, total); break;
+    default: dispatch<8>(ctx, a, p, total); break;
     }
-    check_cuda(cudaMemcpyAsync(ctx.pinned, total, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    check_cuda(cudaMemcpyAsync(ctx.pinned, total, 8, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
     ctx.finish();
-    uint32_t r = 0;
-    std::memcpy(&r, ctx.pinned, 4);
-    return r;
+    unsigned long long r = 0;
+    std::memcpy(&r, ctx.pinned, 8);
+    return (std::size_t)r;
 }
 
 }  // namespace gbc

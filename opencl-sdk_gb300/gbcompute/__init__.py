@@ -484,9 +484,10 @@ def reduce(ctx: Context, inp: DeviceBuffer, op: binary_op | None = None, init=0)
 
 def copy_if(ctx: Context, inp: DeviceBuffer, out: DeviceBuffer, predicate: str) -> int:
     """Stable compaction (reference Algorithm.hpp:229-237): out[0:count] = the
-    elements x of inp with predicate(x); returns count. The predicate is an
-    OpenCL C expression over x from a fixed grammar (comparisons of x,
-    (x % c) or (x & c) with a constant, joined by && or ||)."""
+    elements x of inp for which the predicate, an OpenCL C expression over x
+    from the subset transform compiles, is nonzero; returns count. A
+    malformed predicate raises BuildError, one outside the subset
+    UnsupportedError."""
     if out.size < inp.size:
         raise ValueError("copy_if: output too small")
     count = C.c_size_t(0)

@@ -419,3 +419,10 @@ def transform(expression: str, x: np.ndarray, out_dtype, y: np.ndarray | None = 
     if out.itemsize < 4 and v.t.kind == "f":
         return convert(convert(v.a, I32), out)
     return convert(v.a, out)
+
+
+def truth(expression: str, x: np.ndarray) -> np.ndarray:
+    """The reference's copy_if flag `(PRED) ? 1u : 0u`: the expression over
+    x = x[i] is nonzero in its own type (NaN counts as nonzero)."""
+    v = _Parser(expression, _Val(x, x.dtype), None).parse()
+    return v.a != 0

@@ -1,6 +1,7 @@
 """copy_if against the reference's own test recipes and numpy (C integer
 semantics: % truncates toward zero, mixed signed/unsigned operands convert
-to unsigned), with the predicate grammar's limits."""
+to unsigned), general OpenCL C predicates against the oracle's truth value,
+and the BUILD / UNSUPPORTED classification of the rest."""
 import numpy as np
 import pytest
 from helpers import SIZES
@@ -70,9 +71,64 @@ def test_edge_sizes_and_all_or_nothing(ctx, gbc):
         assert count == 0
 
 
-@pytest.mark.parametrize("pred", ["x*2 > 3", "foo > 1", "(x % 0) == 0", "(x % 2.0) == 0", "x > 1 && x < 5 || x == 9",
-                                  "y > 0", "x >"])
-def test_outside_grammar_is_unsupported(ctx, gbc, pred):
+PREDICATES = [
+    # the reference's own and general OpenCL C predicates, checked against the
+    # oracle's truth value of the same expression
+    (np.int32, "x*2 > 3"),
+    (np.int32, "(x % 0) == 0"),                 # x % 0 is defined as 0 here
+    (np.int32, "x > 1 && x < 5 || x == 9"),
+    (np.int32, "x"),                            # truthiness: nonzero
+    (np.int32, "abs(x) < 100 ? x & 1 : x > 0"),
+    (np.uint32, "x >= 700u"),                   # compute-pipeline main.cpp:160
+    (np.uint32, "(x & 1u) == 0u"),              # lib/Compute.md:51
+    (np.float32, "x * 0.5f > 0.25f"),
+    (np.float32, "x"),                          # NaN is nonzero: kept
+    (np.float32, "x != x"),
+    (np.float64, "(x > 0.5) == (x < 0.75)"),
+    (np.int64, "x % 3 == -1"),
+    (np.uint64, "(x >> 40) > 100"),
+    (np.uint8, "x - 100"),                      # int arithmetic after promotion
+    (np.int16, "(x ^ 0x5555) < 0"),
+    (np.int32, "(x+1) * ((x+2) * (x+3)) > 0"),  # uses the temporaries
+]
+
+
+def sample(dtype, n, rng):
+    dt = np.dtype(dtype)
+    if dt.kind == "f":
+        v = (rng.standard_normal(n) * 2).astype(dt)
+        v[::37] = np.nan
+        v[::41] = 0.0
+        return v
+    info = np.iinfo(dt)
+    v = rng.integers(info.min, info.max, size=n, dtype=dt, endpoint=True)
+    v[::13] = rng.integers(-20, 20, size=v[::13].size).astype(dt)
+    return v
+
+
+@pytest.mark.parametrize("dtype,pred", PREDICATES, ids=[f"{np.dtype(d)}|{p}" for d, p in PREDICATES])
+def test_general_predicates(ctx, gbc, dtype, pred):
+    import transform_oracle as T
+
+    rng = np.random.default_rng(len(pred) * 7 + np.dtype(dtype).itemsize)
+    for n in (1, 4097, 300_001):
+        x = sample(dtype, n, rng)
+        got, count = run(ctx, gbc, x, pred)
+        want = x[T.truth(pred, x)]
+        assert count == want.size
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8))  # bit-exact, NaN included
+
+
+@pytest.mark.parametrize("pred", ["foo > 1", "(x % 2.0) == 0", "y > 0", "x >", "x +* nonsense"])
+def test_malformed_predicate_is_a_build_error(ctx, gbc, pred):
+    x = np.arange(100, dtype=np.int32)
+    with pytest.raises(gbc.BuildError) as e:
+        run(ctx, gbc, x, pred)
+    assert "build log" in str(e.value)
+
+
+@pytest.mark.parametrize("pred", ["sqrt(x) > 1", "(float4)x", "mad(x, x, x) > 0"])
+def test_outside_the_subset_is_unsupported(ctx, gbc, pred):
     x = np.arange(100, dtype=np.int32)
     with pytest.raises(gbc.UnsupportedError):
         run(ctx, gbc, x, pred)

@@ -176,6 +176,9 @@ GBC_EXPORT clc_status clc_sort(clc_context ctx, clc_buffer keys, clc_type key_ty
 GBC_EXPORT clc_status clc_transform_compile(const char* expression, clc_type in_type, int has_in2,
                                             clc_type in2_type, clc_type out_type, char* listing,
                                             size_t capacity);
+/* out[0 .. *count) = the elements x of in, in order, for which predicate
+ * (an expression over x from the clc_transform subset) is nonzero; blocks.
+ * Replaces compute_c.h:169-171 (copy_if). in and out must differ. */
 GBC_EXPORT clc_status clc_copy_if(clc_context ctx, clc_buffer in, clc_buffer out, size_t n,
                                   clc_type type, const char* predicate, size_t* count);
 

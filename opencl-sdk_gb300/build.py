@@ -90,6 +90,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     workers = min(len(SOURCES), max(2, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(lambda s: _compile(s, force, digest, verbose), SOURCES))
+    # objects of earlier header digests are never used again
+    keep = {os.path.basename(o) for o in objs}
+    for name in os.listdir(OUT_DIR):
+        if name.endswith(".o") and name not in keep:
+            os.remove(os.path.join(OUT_DIR, name))
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + ".tmp"

@@ -49,7 +49,10 @@ enum src : uint8_t { S_ACC = 0, S_IMM = 1, S_X = 2, S_Y = 3, S_POP = 4 };
 // 0/1. CVT converts acc from t to t2. EXT8S/EXT8U/EXT16S/EXT16U keep the low
 // 8/16 bits of an I32 (a cast to char/uchar/short/ushort, promoted back).
 // PUSH stores acc in stack slot `slot`; SEL sets acc = st[slot] ? st[slot+1] :
-// acc (slot holds an I32 condition).
+// acc (slot holds an I32 condition). DIVC / REMC divide by an integer literal
+// without a division (Granlund and Montgomery, "Division by Invariant
+// Integers using Multiplication", PLDI 1994: figure 4.1 for unsigned, 5.2 for
+// signed operands), with the same results as DIV / REM.
 enum kind : uint8_t {
     K_LOAD = 0,
     K_PUSH,
@@ -85,6 +88,8 @@ enum kind : uint8_t {
     K_EXT16S,
     K_EXT16U,
     K_SEL,
+    K_DIVC,  // acc / imm and acc % imm for an integer literal |imm| >= 2, by
+    K_REMC,  // multiplication with a precomputed multiplier (aux) and shift (slot)
     K_COUNT
 };
 
@@ -94,6 +99,7 @@ constexpr int STACK = 4;
 struct op {
     uint8_t kind, t, src, slot, t2, pad[3];
     uint64_t imm;  // raw bits of the immediate in type t
+    uint64_t aux;  // K_DIVC / K_REMC: the multiplier
 };
 
 struct program {

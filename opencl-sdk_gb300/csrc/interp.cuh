@@ -206,18 +206,28 @@ template <typename T> struct ops_fp {
     __device__ static T mx(T a, T b) { return a != a ? b : (b != b ? a : (a < b ? b : a)); }
 };
 
+// Operands: a broadcast immediate, or one register per value.
+template <typename W> struct imm_operand {
+    W v;
+    __device__ __forceinline__ W operator()(int) const { return v; }
+};
+template <typename W, int V> struct reg_operand {
+    const W (&r)[V];
+    __device__ __forceinline__ W operator()(int j) const { return r[j]; }
+};
+
 #define GBC_EACH(BODY)                  \
     _Pragma("unroll") for (int j = 0; j < V; ++j) \
     {                                   \
         const T a = get<T>(acc[j]);     \
-        const T b = get<T>(opd[j]);     \
+        const T b = get<T>(opd(j));     \
         (void)b;                        \
         BODY;                           \
     }                                   \
     break;
 
-template <typename T, typename W, int V>
-__device__ __forceinline__ void exec_int(uint8_t kind, W (&acc)[V], const W (&opd)[V])
+template <typename T, typename W, int V, typename OPD>
+__device__ __forceinline__ void exec_int(uint8_t kind, W (&acc)[V], const OPD& opd)
 {
     using O = ops_int<T>;
     switch (kind) {
@@ -251,8 +261,8 @@ __device__ __forceinline__ void exec_int(uint8_t kind, W (&acc)[V], const W (&op
     }
 }
 
-template <typename T, typename W, int V>
-__device__ __forceinline__ void exec_fp(uint8_t kind, W (&acc)[V], const W (&opd)[V])
+template <typename T, typename W, int V, typename OPD>
+__device__ __forceinline__ void exec_fp(uint8_t kind, W (&acc)[V], const OPD& opd)
 {
     using O = ops_fp<T>;
     switch (kind) {
@@ -310,41 +320,125 @@ __device__ __forceinline__ W* slot_ptr(W* st, int slot)
     return st + (std::size_t)slot * V * NT + threadIdx.x;
 }
 
+// acc = acc OP operand for the arithmetic kinds, by element type
+template <typename W, int V, typename OPD>
+__device__ __forceinline__ void exec_arith(uint8_t kind, uint8_t t, W (&acc)[V], const OPD& opd)
+{
+    switch (t) {
+    case I32: exec_int<int32_t>(kind, acc, opd); return;
+    case U32: exec_int<uint32_t>(kind, acc, opd); return;
+    case F32: exec_fp<float>(kind, acc, opd); return;
+    default:
+        if constexpr (sizeof(W) == 8) {
+            if (t == I64) exec_int<int64_t>(kind, acc, opd);
+            else if (t == U64) exec_int<uint64_t>(kind, acc, opd);
+            else exec_fp<double>(kind, acc, opd);
+        }
+        return;
+    }
+}
+
+// acc / d or acc % d for an integer literal d (|d| >= 2) by a multiply-high:
+// the multiplier is o.aux, l = o.slot (see K_DIVC).
+template <typename W, int V> __device__ __forceinline__ void exec_divc(const op& o, W (&acc)[V])
+{
+    const bool rem = o.kind == K_REMC;
+    const int l = o.slot;
+    const int sh1 = l > 0 ? 1 : 0, sh2 = l > 0 ? l - 1 : 0;
+    switch (o.t) {
+    case U32: {
+        const uint32_t m = (uint32_t)o.aux, d = (uint32_t)o.imm;
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+            const uint32_t n = get<uint32_t>(acc[j]);
+            const uint32_t t1 = __umulhi(m, n);
+            const uint32_t q = (t1 + ((n - t1) >> sh1)) >> sh2;
+            acc[j] = put<W>(rem ? n - q * d : q);
+        }
+        return;
+    }
+    case I32: {
+        const int32_t m = (int32_t)(uint32_t)o.aux, d = (int32_t)(uint32_t)o.imm, ds = d < 0 ? -1 : 0;
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+            const int32_t n = get<int32_t>(acc[j]);
+            int32_t q = (int32_t)((uint32_t)n + (uint32_t)__mulhi(m, n));
+            q = (q >> (l - 1)) - (n >> 31);
+            q = (q ^ ds) - ds;
+            acc[j] = put<W>(rem ? (int32_t)((uint32_t)n - (uint32_t)q * (uint32_t)d) : q);
+        }
+        return;
+    }
+    default:
+        if constexpr (sizeof(W) == 8) {
+            if (o.t == U64) {
+                const uint64_t m = o.aux, d = o.imm;
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                    const uint64_t n = get<uint64_t>(acc[j]);
+                    const uint64_t t1 = __umul64hi(m, n);
+                    const uint64_t q = (t1 + ((n - t1) >> sh1)) >> sh2;
+                    acc[j] = put<W>(rem ? n - q * d : q);
+                }
+            } else if (o.t == I64) {
+                const long long m = (long long)o.aux, d = (long long)o.imm, ds = d < 0 ? -1 : 0;
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                    const long long n = get<int64_t>(acc[j]);
+                    long long q = (long long)((unsigned long long)n + (unsigned long long)__mul64hi(m, n));
+                    q = (q >> (l - 1)) - (n >> 63);
+                    q = (q ^ ds) - ds;
+                    acc[j] = put<W>((int64_t)(rem ? (long long)((unsigned long long)n - (unsigned long long)q *
+                                                                                         (unsigned long long)d)
+                                                  : q));
+                }
+            }
+        }
+        return;
+    }
+}
+
 // STK: the program uses stack slots; NT: threads of the CTA (the slot
-// layout's stride)
+// layout's stride). The arithmetic kinds are tested first; an immediate
+// operand is used as a scalar.
 template <typename W, int V, bool STK, int NT>
 __device__ __forceinline__ void exec_op(const op& o, W (&acc)[V], const W (&xv)[V], const W (&yv)[V], W* st)
 {
-    W opd[V];
-    switch (o.src) {
-    case S_IMM:
+    if (o.kind >= K_ADD && o.kind <= K_ABS) {
+        if (o.src == S_IMM || o.src == S_ACC) {
+            exec_arith<W, V>(o.kind, o.t, acc, imm_operand<W>{(W)o.imm});
+        } else {
+            W opd[V];
+            if (o.src == S_X) {
 #pragma unroll
-        for (int j = 0; j < V; ++j) opd[j] = (W)o.imm;
-        break;
-    case S_X:
+                for (int j = 0; j < V; ++j) opd[j] = xv[j];
+            } else if (o.src == S_Y) {
 #pragma unroll
-        for (int j = 0; j < V; ++j) opd[j] = xv[j];
-        break;
-    case S_Y:
+                for (int j = 0; j < V; ++j) opd[j] = yv[j];
+            } else if constexpr (STK) {
+                const W* r = slot_ptr<W, V, NT>(st, o.slot);
 #pragma unroll
-        for (int j = 0; j < V; ++j) opd[j] = yv[j];
-        break;
-    case S_POP:
-        if constexpr (STK) {
-            const W* r = slot_ptr<W, V, NT>(st, o.slot);
+                for (int j = 0; j < V; ++j) opd[j] = r[j * NT];
+            } else {
 #pragma unroll
-            for (int j = 0; j < V; ++j) opd[j] = r[j * NT];
+                for (int j = 0; j < V; ++j) opd[j] = 0;
+            }
+            exec_arith<W, V>(o.kind, o.t, acc, reg_operand<W, V>{opd});
         }
-        break;
-    default:
-#pragma unroll
-        for (int j = 0; j < V; ++j) opd[j] = 0;
-        break;
+        return;
     }
     switch (o.kind) {
     case K_LOAD:
+        if (o.src == S_X) {
 #pragma unroll
-        for (int j = 0; j < V; ++j) acc[j] = opd[j];
+            for (int j = 0; j < V; ++j) acc[j] = xv[j];
+        } else if (o.src == S_Y) {
+#pragma unroll
+            for (int j = 0; j < V; ++j) acc[j] = yv[j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < V; ++j) acc[j] = (W)o.imm;
+        }
         return;
     case K_PUSH:
         if constexpr (STK) {
@@ -378,6 +472,8 @@ __device__ __forceinline__ void exec_op(const op& o, W (&acc)[V], const W (&xv)[
 #pragma unroll
         for (int j = 0; j < V; ++j) acc[j] = put<W>((int32_t)(uint16_t)acc[j]);
         return;
+    case K_DIVC:
+    case K_REMC: exec_divc<W, V>(o, acc); return;
     case K_CVT:
         switch (o.t2) {
         case I32: cvt_to<int32_t>(o.t, acc); return;
@@ -391,19 +487,7 @@ __device__ __forceinline__ void exec_op(const op& o, W (&acc)[V], const W (&xv)[
             }
             return;
         }
-    default: break;
-    }
-    switch (o.t) {
-    case I32: exec_int<int32_t>(o.kind, acc, opd); return;
-    case U32: exec_int<uint32_t>(o.kind, acc, opd); return;
-    case F32: exec_fp<float>(o.kind, acc, opd); return;
-    default:
-        if constexpr (sizeof(W) == 8) {
-            if (o.t == I64) exec_int<int64_t>(o.kind, acc, opd);
-            else if (o.t == U64) exec_int<uint64_t>(o.kind, acc, opd);
-            else exec_fp<double>(o.kind, acc, opd);
-        }
-        return;
+    default: return;
     }
 }
 

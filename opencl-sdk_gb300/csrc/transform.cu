@@ -95,6 +95,33 @@ elem common(elem a, elem b)
     return of_ty(s == I32 ? U32 : U64);
 }
 
+// Division by an invariant integer d (Granlund and Montgomery, PLDI 1994).
+// Unsigned N-bit (figure 4.1), 1 <= d < 2^N: l = ceil(log2 d), m = floor(2^N
+// (2^l - d) / d) + 1; then q = SRL(t1 + SRL(n - t1, min(l, 1)), max(l - 1, 0))
+// with t1 = MULUH(m, n).
+void magic_unsigned(int bits, uint64_t d, uint64_t& m, int& l)
+{
+    using u128 = unsigned __int128;
+    l = 0;
+    while (((u128)1 << l) < d) ++l;
+    const u128 num = ((u128)1 << bits) * (((u128)1 << l) - d);
+    m = (uint64_t)(num / d + 1);
+}
+// Signed N-bit (figure 5.2), |d| >= 2: l = max(ceil(log2 |d|), 1), m = 1 +
+// floor(2^(N + l - 1) / |d|) - 2^N (a negative N-bit value); then q0 = n +
+// MULSH(m, n), q0 = SRA(q0, l - 1) - XSIGN(n), q = EOR(q0, dsign) - dsign.
+void magic_signed(int bits, int64_t d, uint64_t& m, int& l)
+{
+    using u128 = unsigned __int128;
+    const uint64_t ad = d < 0 ? (uint64_t)(-(d + 1)) + 1u : (uint64_t)d;
+    l = 0;
+    while (((u128)1 << l) < ad) ++l;
+    if (l < 1) l = 1;
+    const u128 big = 1 + (((u128)1 << (bits + l - 1)) / ad);
+    m = (uint64_t)(big - ((u128)1 << bits));  // two's complement, low `bits` bits meaningful
+    if (bits == 32) m &= 0xFFFFFFFFull;
+}
+
 struct token {
     enum kind { END, NUM, ID, PUNCT } k = END;
     std::string s;
@@ -752,6 +779,30 @@ private:
         return false;
     }
 
+    // acc = acc OP leaf; an integer literal divisor with |d| >= 2 divides by
+    // multiplication
+    void push_leaf_op(uint8_t kind, ty t, uint8_t src, uint64_t imm)
+    {
+        const bool integer = t == I32 || t == U32 || t == I64 || t == U64;
+        if ((kind == K_DIV || kind == K_REM) && src == S_IMM && integer) {
+            const int bits = (t == I32 || t == U32) ? 32 : 64;
+            const bool sgn = t == I32 || t == I64;
+            const int64_t sd = bits == 32 ? (int64_t)(int32_t)(uint32_t)imm : (int64_t)imm;
+            const uint64_t ud = bits == 32 ? (uint64_t)(uint32_t)imm : imm;
+            const bool ok = sgn ? (sd >= 2 || sd <= -2) : ud >= 2;
+            if (ok) {
+                uint64_t m = 0;
+                int l = 0;
+                if (sgn) magic_signed(bits, sd, m, l);
+                else magic_unsigned(bits, ud, m, l);
+                push_op(kind == K_DIV ? K_DIVC : K_REMC, t, S_IMM, imm, (uint8_t)l);
+                prog_.ops[prog_.nops - 1].aux = m;
+                return;
+            }
+        }
+        push_op(kind, t, src, imm);
+    }
+
     static uint8_t reversed(uint8_t k)
     {
         switch (k) {
@@ -787,7 +838,7 @@ private:
         uint64_t imm;
         if (leaf(b, t, src, imm)) {
             gen_as(a, t, sp);
-            push_op(kind, t, src, imm);
+            push_leaf_op(kind, t, src, imm);
         } else if (leaf(a, t, src, imm)) {
             gen_as(b, t, sp);
             push_op(reversed(kind), t, src, imm);
@@ -806,7 +857,7 @@ private:
         uint8_t src;
         uint64_t imm;
         if (leaf(b, t, src, imm)) {
-            push_op(kind, t, src, imm);
+            push_leaf_op(kind, t, src, imm);
             return;
         }
         need_slots(sp, 1);
@@ -925,7 +976,8 @@ std::string listing(const program& p)
 {
     static const char* kinds[] = {"load", "push", "add", "sub", "rsub", "mul", "div", "rdiv", "rem", "rrem", "and", "or",
                                   "xor", "shl", "rshl", "shr", "rshr", "lt", "le", "gt", "ge", "eq", "ne", "min",
-                                  "max", "neg", "not", "abs", "cvt", "ext8s", "ext8u", "ext16s", "ext16u", "sel"};
+                                  "max", "neg", "not", "abs", "cvt", "ext8s", "ext8u", "ext16s", "ext16u", "sel",
+                                  "divc", "remc"};
     static const char* tys[] = {"i32", "u32", "i64", "u64", "f32", "f64"};
     std::ostringstream os;
     for (uint32_t k = 0; k < p.nops; ++k) {
@@ -940,6 +992,7 @@ std::string listing(const program& p)
         default: break;
         }
         if (o.kind == K_PUSH || o.kind == K_SEL) os << " st" << (int)o.slot;
+        if (o.kind == K_DIVC || o.kind == K_REMC) os << " m=0x" << std::hex << o.aux << std::dec << " l=" << (int)o.slot;
         os << '\n';
     }
     return os.str();

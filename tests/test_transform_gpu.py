@@ -182,6 +182,21 @@ CASES = [
     ("max(x, y) - min(x, y)", F64, F64, F64),
     ("(x & 0xFFFFFFFF00000000UL) | (y & 0xFFFFu)", U64, U32, U64),
     ("x ? (double)y : -1.0", I64, F32, F64),
+    # division by integer literals (multiply-high), every sign and width
+    ("x / 3 + x % 3", I32, None, I32),
+    ("x / -7 * 100 + x % -7", I32, None, I32),
+    ("x / 1000000007", I32, None, I32),
+    ("x % 65536 + x / 2", I32, None, I32),
+    ("x / 3u + x % 10u", U32, None, U32),
+    ("x / 4294967295u + x % 641u", U32, None, U32),
+    ("x / 7 + x % 2147483647", U32, None, U32),
+    ("x / 3 - x % 5", I64, None, I64),
+    ("x / -1000000000000 + x % 97", I64, None, I64),
+    ("x / 3ul + x % 1000000000039ul", U64, None, U64),
+    ("x / 18446744073709551615ul", U64, None, U64),
+    ("(x % 3u) == 0u", U32, None, U8),
+    ("x / 9 + x % 9", I16, None, I32),
+    ("100 / (x | 1)", I32, None, I32),
 ]
 
 

@@ -685,8 +685,32 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     entry("pipeline_sort_rbk_hist_u64_zipf_n2^29", np_, "Gkeys/s", ms_pipe, 212 * np_, ok,
           prof_pipe, {"runs": int(r), "key": "splitmix64(Zipf(1.1) rank over 2^24 values)",
                       "values": "u32 uniform [0, 2^16)",
-                      "note": "bytes: 8 B upfront histogram + 8 digit passes x 24 B + 12 B reduce_by_key read = 212 B/key; "
-                              "the learned-CDF form is 32-bit only"})
+                      "note": "bytes: 8 B upfront histogram + 8 digit passes x 24 B + 12 B reduce_by_key read = 212 B/key"})
+    # the learned-CDF form of the same pipeline: the key-value learned sort
+    # (64-bit keys bucketed through a monotone 32-bit projection, stable
+    # partition), then the same reduce_by_key + histogram; identical results
+    lstats = []
+
+    def pipeline_learned():
+        lstats.append(gbc.sort_learned_pairs(ctx, zk.data_ptr(), zko.data_ptr(), np.uint64, zv.data_ptr(),
+                                             zvo.data_ptr(), np_))
+        runs.append(gbc.reduce_by_key_raw(ctx, zko.data_ptr(), np.uint64, zvo.data_ptr(), np_, uk.data_ptr(),
+                                          sums.data_ptr(), cnts.data_ptr(), h16.data_ptr()))
+
+    ms_learn, prof_learn = timed(pipeline_learned, max(3, steps // 5), warmup,
+                                 ("sort.", "reduce_by_key", "learned.", "segsort."))
+    ok_l = bool(torch.equal(zko, sk_ref)) and bool(torch.equal(zvo, zv[order])) and runs[-1] == r
+    ok_l = ok_l and bool(torch.equal(uk[:r], uniq)) and bool(torch.equal(cnts[:r].long(), counts))
+    ok_l = ok_l and bool(torch.equal(sums[:r], ref_sums))
+    ok_l = ok_l and bool(torch.equal(torch.bincount(zk & 0xFFFF, minlength=65536).to(torch.int32), h16))
+    ls = lstats[-1]
+    entry("pipeline_learned_sort_rbk_hist_u64_zipf_n2^29", np_, "Gkeys/s", ms_learn, 212 * np_, ok_l, prof_learn,
+          {"plain_pipeline_ms": ms_pipe, "speedup_vs_plain": ms_pipe / ms_learn,
+           "stats": {"buckets": ls.buckets, "nonempty_buckets": ls.nonempty_buckets,
+                     "oversized_keys": ls.oversized_keys, "fallback": ls.fallback, "violation": ls.violation,
+                     "first_loss": ls.first_loss, "last_loss": ls.last_loss},
+           "note": "learned-CDF key-value sort (fit, stable bucket partition, segmented finish) + reduce_by_key + "
+                   "histogram; bytes counted as the plain form's 212 B/key"})
     # the same pipeline on the raw Zipf ranks as keys (< 2^24: the pass plan
     # runs 3 of the 8 digit passes)
     rk, _ = zipf_splitmix_keys(torch, np_, 1.1, 1 << 24, 6, raw_rank=True)

@@ -280,6 +280,13 @@ typedef struct clc_learned_stats {
 GBC_EXPORT void clc_learned_default_options(clc_learned_options* options);
 GBC_EXPORT clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
                                        size_t n, const clc_learned_options* options, clc_learned_stats* stats);
+/* Extension: the learned-CDF sort of key-value pairs, stable, out of place:
+ * keys U32 / I32 / F32 / U64 / I64 with 32-bit values; output identical to
+ * clc_sort_ex's. 64-bit keys are bucketed through a monotone 32-bit
+ * projection of the sample's key range. Synchronises. */
+GBC_EXPORT clc_status clc_sort_learned_pairs(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                             const unsigned* vals_in, unsigned* vals_out, size_t n,
+                                             const clc_learned_options* options, clc_learned_stats* stats);
 /* One forward/backward pass of the network on the GPU over m points (host
  * arrays): keys in the order-preserving 32-bit domain and target CDF values;
  * the first layer sees (key - centres[j]) * inv_span. Returns the gradient of

@@ -845,6 +845,39 @@ clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out
     });
 }
 
+clc_status clc_sort_learned_pairs(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
+                                  const unsigned* vals_in, unsigned* vals_out, size_t n,
+                                  const clc_learned_options* options, clc_learned_stats* stats)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        require(key_type == CLC_TYPE_U32 || key_type == CLC_TYPE_I32 || key_type == CLC_TYPE_F32 ||
+                    key_type == CLC_TYPE_U64 || key_type == CLC_TYPE_I64,
+                "clc_sort_learned_pairs: keys must be U32, I32, F32, U64 or I64");
+        int bytes, kind;
+        key_kind_of(key_type, bytes, kind);
+        gbc::learned_options o;
+        if (options != nullptr) {
+            o.sample = options->sample;
+            o.points = options->points;
+            o.buckets = options->buckets;
+            o.steps = options->steps;
+            o.lr = options->lr;
+            o.use_model = options->use_model != 0;
+            o.params_in = options->params_in;
+            o.params_out = options->params_out;
+            o.splitters_in = options->splitters_in;
+        }
+        gbc::learned_stats s;
+        gbc::learned_sort_pairs(*ctx->ctx, keys_in, keys_out, bytes, kind, vals_in, vals_out, n, o, &s);
+        if (stats != nullptr)
+            *stats = clc_learned_stats{s.buckets,       s.nonempty_buckets,         s.largest_bucket,
+                                       s.oversized_buckets, s.oversized_keys,      s.constant_keys,
+                                       s.estimated_oversized_keys, s.violation,    s.fallback,
+                                       s.first_loss,    s.last_loss};
+    });
+}
+
 clc_status clc_learned_mlp_gradients(clc_context ctx, const float* params, const unsigned* centres, float inv_span,
                                      const unsigned* keys, const float* ys, size_t m, float* grad, float* loss)
 {

@@ -553,7 +553,7 @@ __global__ void k_check(const uint32_t* __restrict__ out, const uint32_t* __rest
 // bucket b are those in [sp[b-1], sp[b]). est[0] receives the sample keys in
 // buckets whose size scaled to n would exceed cap.
 __global__ void k_estimate(const uint32_t* __restrict__ sorted, uint32_t s, const uint32_t* __restrict__ sp,
-                           uint32_t buckets, uint32_t n, uint32_t cap, uint32_t* est)
+                           uint32_t buckets, uint32_t n, uint32_t cap, int skip_constant, uint32_t* est)
 {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= buckets) return;
@@ -569,7 +569,146 @@ __global__ void k_estimate(const uint32_t* __restrict__ sorted, uint32_t s, cons
     const uint32_t lo = b == 0 ? 0u : lower(sp[b - 1]);
     const uint32_t hi = b + 1 == buckets ? s : lower(sp[b]);
     const uint32_t cnt = hi > lo ? hi - lo : 0u;
+    // skip_constant: a bucket whose sample keys are all equal needs no sort
+    if (skip_constant && cnt > 0 && sorted[lo] == sorted[hi - 1]) return;
     if ((uint64_t)cnt * n > (uint64_t)cap * s) atomicAdd(est, cnt);
+}
+
+// ---- key-value form: 64-bit keys through a monotone 32-bit projection --------
+// The sample of 64-bit keys (order-preserving form) is sorted; keys are
+// projected to 32 bits as p(u) = min(2^32 - 1, (u - kmin) >> shift) (0 below
+// kmin), shift chosen so that the sample's range [kmin, kmax] fits: p is
+// non-decreasing, so buckets over p are buckets over the keys. 32-bit keys
+// use p(u) = u.
+struct Proj {
+    unsigned long long kmin;
+    int shift;
+    int pad;
+};
+
+__device__ __forceinline__ uint64_t ordered64(uint64_t k, int kind)
+{
+    return kind == 1 ? k ^ 0x8000000000000000ull : k;
+}
+template <typename K> __device__ __forceinline__ uint64_t ordered_any(K k, int kind)
+{
+    if constexpr (sizeof(K) == 8) return ordered64(k, kind);
+    else return ordered(k, kind);
+}
+__device__ __forceinline__ uint32_t project(uint64_t u, const Proj& p)
+{
+    if (u <= p.kmin) return 0;
+    const uint64_t d = (u - p.kmin) >> p.shift;
+    return d > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)d;
+}
+
+__global__ void k_sample64(const uint64_t* __restrict__ keys, uint32_t n, uint64_t* __restrict__ sample, uint32_t s,
+                           int kind)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s) sample[i] = ordered64(keys[(uint32_t)(((uint64_t)i * n) / s)], kind);
+}
+
+// One CTA: the projection from the sorted 64-bit sample, and the sample
+// projected (still sorted).
+__global__ void k_project(const uint64_t* __restrict__ sorted, uint32_t s, Proj* __restrict__ pj,
+                          uint32_t* __restrict__ sorted32)
+{
+    __shared__ Proj p;
+    if (threadIdx.x == 0) {
+        const uint64_t kmin = sorted[0], span = sorted[s - 1] - kmin;
+        const int bits = span == 0 ? 0 : 64 - __clzll((long long)span);
+        p.kmin = kmin;
+        p.shift = bits > 32 ? bits - 32 : 0;
+        p.pad = 0;
+        *pj = p;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < s; i += blockDim.x) sorted32[i] = project(sorted[i], p);
+}
+
+// Bucket of every key (and its index), for the stable partition.
+template <typename K>
+__global__ void __launch_bounds__(PART_THREADS) k_bucket_ids(const K* __restrict__ keys, uint32_t n, int kind,
+                                                             const Proj* __restrict__ pj,
+                                                             const Frame* __restrict__ fr,
+                                                             const uint32_t* __restrict__ gsp,
+                                                             const uint16_t* __restrict__ glut, uint32_t buckets,
+                                                             uint32_t* __restrict__ ids, uint32_t* __restrict__ idx)
+{
+    extern __shared__ uint32_t sh[];
+    uint32_t* sp = sh;
+    uint16_t* lut = reinterpret_cast<uint16_t*>(sp + (buckets - 1));
+    for (uint32_t i = threadIdx.x; i + 1 < buckets; i += PART_THREADS) sp[i] = gsp[i];
+    for (int i = threadIdx.x; i <= NCELLS; i += PART_THREADS) lut[i] = glut[i];
+    const Proj p = *pj;
+    const Bucketer bk{sp, lut, fr->umin, lut_shift(fr->umin, fr->umax)};
+    __syncthreads();
+    const uint32_t stride = gridDim.x * PART_THREADS;
+    for (uint32_t i = blockIdx.x * PART_THREADS + threadIdx.x; i < n; i += stride) {
+        ids[i] = bk(project(ordered_any<K>(keys[i], kind), p));
+        idx[i] = i;
+    }
+}
+
+// bucket_off[b] = first position of bucket b in the sorted bucket ids.
+__global__ void k_bucket_offsets(const uint32_t* __restrict__ ids, uint32_t n, uint32_t buckets,
+                                 uint32_t* __restrict__ bucket_off)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > buckets) return;
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t m = (lo + hi) >> 1;
+        if (ids[m] < b) lo = m + 1;
+        else hi = m;
+    }
+    bucket_off[b] = lo;
+}
+
+// skip[b] = 0 for every bucket b holding two different keys (skip starts at 1):
+// ids are the sorted bucket numbers, aligned with the gathered keys.
+template <typename K>
+__global__ void k_mixed_buckets(const K* __restrict__ keys, const uint32_t* __restrict__ ids, uint32_t n,
+                                uint8_t* __restrict__ skip)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += stride) {
+        const uint32_t b = ids[i];
+        if (ids[i - 1] == b && keys[i - 1] != keys[i] && skip[b] != 0) skip[b] = 0;
+    }
+}
+
+template <typename K>
+__global__ void k_gather(const K* __restrict__ keys, const uint32_t* __restrict__ vals, const uint32_t* __restrict__ perm,
+                         uint32_t n, K* __restrict__ keys_out, uint32_t* __restrict__ vals_out)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t j = perm[i];
+        keys_out[i] = keys[j];
+        vals_out[i] = vals[j];
+    }
+}
+
+// The statistics and boundary check of k_check for either key width.
+template <typename K>
+__global__ void k_check_any(const K* __restrict__ out, const uint32_t* __restrict__ bucket_off, uint32_t buckets,
+                            int kind, uint32_t cap, uint32_t* stats)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= buckets) return;
+    const uint32_t s = bucket_off[b], e = bucket_off[b + 1];
+    const uint32_t len = e - s;
+    if (len > cap) {
+        atomicAdd(&stats[1], len);
+        atomicAdd(&stats[2], 1u);
+        if (out[s] == out[e - 1]) atomicAdd(&stats[5], len);
+    }
+    if (len > 0) atomicAdd(&stats[4], 1u);
+    atomicMax(&stats[3], len);
+    if (s > 0 && len > 0 && ordered_any<K>(out[s - 1], kind) > ordered_any<K>(out[s], kind))
+        atomicExch(&stats[0], 1u);
 }
 
 // Points per cooperative training launch: at most one CTA per SM.
@@ -598,6 +737,138 @@ static void launch_train(device_context& ctx, TrainArgs& ta, uint32_t grid)
                "learned train launch");
 }
 
+// Stages 2-4 on a sorted sample of S keys (order-preserving 32-bit form):
+// frame, parameters (fitted unless the model is off), splitters and lookup
+// table; returns the sample keys that would fall in buckets above cap
+// (reads it back: synchronises).
+struct model_scratch {
+    float* params;
+    Frame* frame;
+    float* partial;
+    uint32_t* barrier;
+    float* losses;
+    uint32_t* xs;
+    float* ys;
+    uint32_t* sp;
+    uint16_t* lut;
+    uint32_t* est;
+};
+
+uint32_t build_model(device_context& ctx, const uint32_t* sorted, uint32_t S, uint32_t M, uint32_t G,
+                     uint32_t buckets, uint32_t n, uint32_t cap, bool skip_constant, const learned_options& opt,
+                     int steps, float lr, const model_scratch& m)
+{
+    const bool own_init = opt.params_in == nullptr;
+    if (!own_init)
+        check_cuda(cudaMemcpyAsync(m.params, opt.params_in, NPARAM * 4, cudaMemcpyHostToDevice, ctx.stream),
+                   "cudaMemcpyAsync");
+    k_frame<<<1, 256, 0, ctx.stream>>>(sorted, S, m.frame, m.params, own_init ? 1 : 0);
+    k_points<<<(M + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, m.xs, m.ys, M);
+    check_cuda(cudaGetLastError(), "learned frame launch");
+    if (opt.use_model && steps > 0) {
+        kernel_timer kt(ctx, "learned.train");
+        TrainArgs ta{m.params, m.frame, m.xs, m.ys, M, m.partial, m.barrier, nullptr, m.losses, steps, lr,
+                     ctx.d_error};
+        launch_train(ctx, ta, G);
+    }
+    {
+        kernel_timer kt(ctx, "learned.splitters");
+        if (opt.splitters_in != nullptr)
+            check_cuda(cudaMemcpyAsync(m.sp, opt.splitters_in, (std::size_t)(buckets - 1) * 4,
+                                       cudaMemcpyHostToDevice, ctx.stream),
+                       "cudaMemcpyAsync");
+        else
+            k_splitters<<<(buckets + 127) / 128, 128, 0, ctx.stream>>>(m.params, m.frame, buckets, m.sp,
+                                                                       opt.use_model ? 1 : 0);
+        k_lut<<<(NCELLS + 1 + 255) / 256, 256, 0, ctx.stream>>>(m.sp, buckets, m.frame, m.lut);
+        check_cuda(cudaGetLastError(), "learned splitter launch");
+    }
+    // A model that would leave most keys in oversized buckets cannot beat the
+    // plain sort: the callers decide from the sample, before the partition.
+    k_estimate<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, m.sp, buckets, n, cap,
+                                                               skip_constant ? 1 : 0, m.est);
+    check_cuda(cudaGetLastError(), "learned estimate launch");
+    uint32_t est = 0;
+    check_cuda(cudaMemcpyAsync(&est, m.est, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    ctx.finish();
+    return est;
+}
+
+// Training losses (and the parameters, when asked) back to the host.
+void read_training(device_context& ctx, const learned_options& opt, int steps, const float* losses,
+                   const float* params, learned_stats& st)
+{
+    std::vector<float> hl(std::max(steps, 1));
+    check_cuda(cudaMemcpyAsync(hl.data(), losses, steps * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    if (opt.params_out != nullptr)
+        check_cuda(cudaMemcpyAsync(opt.params_out, params, NPARAM * 4, cudaMemcpyDeviceToHost, ctx.stream),
+                   "cudaMemcpyAsync");
+    ctx.finish();
+    st.first_loss = hl[0];
+    st.last_loss = hl[steps - 1];
+}
+
+// Sizes shared by both forms: sample S, training points M, buckets, training grid.
+struct learned_shape {
+    uint32_t S, M, buckets, G;
+    int steps;
+    float lr;
+};
+
+learned_shape shape_for(const device_context& ctx, std::size_t n, const learned_options& opt)
+{
+    learned_shape sh;
+    sh.S = (uint32_t)std::min<std::size_t>(opt.sample > 0 ? opt.sample : (1u << 20), n);
+    sh.M = std::max<uint32_t>(1, std::min<uint32_t>({(uint32_t)(opt.points > 0 ? opt.points : 8192), sh.S,
+                                                     (uint32_t)(TRAIN_THREADS * ctx.sm_count)}));
+    // Buckets: about 8192 keys each by default, as many as the partition
+    // kernels' shared memory holds (counters, splitters and the table).
+    const uint32_t max_buckets =
+        (uint32_t)std::min<std::size_t>(65536, (ctx.smem_optin - (std::size_t)(NCELLS + 1) * 2 + 4) / 8);
+    if (opt.buckets > 0) {
+        sh.buckets = (uint32_t)opt.buckets;
+        if (sh.buckets < 2 || sh.buckets > max_buckets)
+            throw std::invalid_argument("sort_learned: buckets must be in [2, " + std::to_string(max_buckets) + "]");
+    } else {
+        const uint32_t want = (uint32_t)((n / 8192 + 1023) / 1024 * 1024);
+        sh.buckets = std::max<uint32_t>(4096, std::min<uint32_t>(want, max_buckets / 1024 * 1024));
+    }
+    sh.steps = opt.steps >= 0 ? opt.steps : 32;
+    sh.lr = opt.lr > 0 ? opt.lr : 0.01f;
+    sh.G = train_grid(ctx, sh.M);
+    return sh;
+}
+
+// The model stages' scratch: points, parameters and frame, training
+// partials, splitters and table, small words (barrier, statistics, losses).
+struct model_buffers {
+    temp_buffer pts, prm, partial, spl, misc;
+    model_scratch m;
+    uint32_t* dstats;  // [0..5] k_check statistics, [6] estimate
+    model_buffers(device_context& ctx, const learned_shape& sh)
+        : pts(ctx.resource, (std::size_t)2 * sh.M * 4),
+          prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16),
+          partial(ctx.resource, (std::size_t)2 * sh.G * (NPARAM + 1) * 4),
+          spl(ctx.resource, (std::size_t)sh.buckets * 4 + (std::size_t)(NCELLS + 1) * 2 + 16),
+          misc(ctx.resource, 64 + (std::size_t)std::max(sh.steps, 1) * 4)
+    {
+        check_cuda(cudaMemsetAsync(misc.get(), 0, 64 + (std::size_t)std::max(sh.steps, 1) * 4, ctx.stream),
+                   "cudaMemsetAsync");
+        m.params = prm.as<float>();
+        m.frame = reinterpret_cast<Frame*>(
+            (reinterpret_cast<uintptr_t>(prm.as<unsigned char>() + (std::size_t)NPARAM * 4) + 15) & ~(uintptr_t)15);
+        m.partial = partial.as<float>();
+        m.barrier = misc.as<uint32_t>();  // [0]
+        dstats = m.barrier + 4;           // [4..10]
+        m.losses = reinterpret_cast<float*>(misc.as<unsigned char>() + 64);
+        m.xs = pts.as<uint32_t>();
+        m.ys = reinterpret_cast<float*>(m.xs + sh.M);
+        m.sp = spl.as<uint32_t>();
+        m.lut = reinterpret_cast<uint16_t*>(m.sp + sh.buckets);
+        m.est = dstats + 6;
+    }
+};
+
 }  // namespace learned
 
 void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_kind, std::size_t n,
@@ -620,49 +891,22 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         return;
     }
     const uint32_t nn = (uint32_t)n;
-    const uint32_t S = (uint32_t)std::min<std::size_t>(opt.sample > 0 ? opt.sample : (1u << 20), n);
-    const uint32_t M = std::max<uint32_t>(
-        1, std::min<uint32_t>({(uint32_t)(opt.points > 0 ? opt.points : 8192), S, (uint32_t)(TRAIN_THREADS * ctx.sm_count)}));
-    // Buckets: about 8192 keys each by default, as many as the partition
-    // kernels' shared memory holds (counters, splitters and the table).
-    const uint32_t max_buckets = (uint32_t)std::min<std::size_t>(
-        65536, (ctx.smem_optin - (std::size_t)(NCELLS + 1) * 2 + 4) / 8);
-    uint32_t buckets;
-    if (opt.buckets > 0) {
-        buckets = (uint32_t)opt.buckets;
-        if (buckets < 2 || buckets > max_buckets)
-            throw std::invalid_argument("sort_learned: buckets must be in [2, " + std::to_string(max_buckets) + "]");
-    } else {
-        const uint32_t want = (uint32_t)((n / 8192 + 1023) / 1024 * 1024);
-        buckets = std::max<uint32_t>(4096, std::min<uint32_t>(want, max_buckets / 1024 * 1024));
-    }
-    const int steps = opt.steps >= 0 ? opt.steps : 32;
-    const float lr = opt.lr > 0 ? opt.lr : 0.01f;
-    const uint32_t G = train_grid(ctx, M);
+    const learned_shape sh = shape_for(ctx, n, opt);
+    const uint32_t S = sh.S, buckets = sh.buckets;
+    const int steps = sh.steps;
     const std::size_t part_smem = part_smem_bytes(buckets);
 
-    // Scratch: sample, points, params, frame, partials, splitters, table,
-    // counts, offsets, totals, small words.
+    // Scratch: the model's, the sample, per-(CTA, bucket) counts, offsets, totals.
     const std::size_t rows = (std::size_t)ctx.sm_count;
+    model_buffers mb(ctx, sh);
     temp_buffer sample(ctx.resource, (std::size_t)S * 4);
-    temp_buffer pts(ctx.resource, (std::size_t)2 * M * 4);
-    temp_buffer prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16);
-    temp_buffer partial(ctx.resource, (std::size_t)2 * G * (NPARAM + 1) * 4);
-    temp_buffer spl(ctx.resource, (std::size_t)buckets * 4 + (std::size_t)(NCELLS + 1) * 2 + 16);
     temp_buffer counts(ctx.resource, rows * buckets * 4);
     temp_buffer boff(ctx.resource, ((std::size_t)buckets + 1) * 4);
     temp_buffer totals(ctx.resource, (std::size_t)buckets * 4);
-    const std::size_t misc_bytes = 64 + (std::size_t)std::max(steps, 1) * 4;
-    temp_buffer misc(ctx.resource, misc_bytes);
-    uint32_t* barrier = misc.as<uint32_t>();        // [0]
-    uint32_t* dstats = barrier + 4;                 // [4..10]
-    float* losses = reinterpret_cast<float*>(misc.as<unsigned char>() + 64);
-    check_cuda(cudaMemsetAsync(misc.get(), 0, misc_bytes, ctx.stream), "cudaMemsetAsync");
-    float* params = prm.as<float>();
-    Frame* frame = reinterpret_cast<Frame*>(
-        (reinterpret_cast<uintptr_t>(prm.as<unsigned char>() + (std::size_t)NPARAM * 4) + 15) & ~(uintptr_t)15);
-    uint32_t* sp = spl.as<uint32_t>();
-    uint16_t* lut = reinterpret_cast<uint16_t*>(sp + buckets);
+    uint32_t* dstats = mb.dstats;
+    Frame* frame = mb.m.frame;
+    uint32_t* sp = mb.m.sp;
+    uint16_t* lut = mb.m.lut;
 
     const uint32_t* in = static_cast<const uint32_t*>(keys_in);
     uint32_t* out = static_cast<uint32_t*>(keys_out);
@@ -672,57 +916,13 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         check_cuda(cudaGetLastError(), "learned sample launch");
     }
     radix_sort(ctx, sample.get(), sample.get(), 4, 0, nullptr, nullptr, S, false);
-    uint32_t* xs = pts.as<uint32_t>();
-    float* ys = reinterpret_cast<float*>(xs + M);
-    const bool own_init = opt.params_in == nullptr;
-    if (!own_init)
-        check_cuda(cudaMemcpyAsync(params, opt.params_in, NPARAM * 4, cudaMemcpyHostToDevice, ctx.stream),
-                   "cudaMemcpyAsync");
-    k_frame<<<1, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, frame, params, own_init ? 1 : 0);
-    k_points<<<(M + 255) / 256, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, xs, ys, M);
-    check_cuda(cudaGetLastError(), "learned frame launch");
-
     const bool train = opt.use_model && steps > 0;
-    std::vector<float> hl(std::max(steps, 1));
-    auto read_losses = [&] {
-        if (!train) return;
-        check_cuda(cudaMemcpyAsync(hl.data(), losses, steps * 4, cudaMemcpyDeviceToHost, ctx.stream),
-                   "cudaMemcpyAsync");
-        if (opt.params_out != nullptr)
-            check_cuda(cudaMemcpyAsync(opt.params_out, params, NPARAM * 4, cudaMemcpyDeviceToHost, ctx.stream),
-                       "cudaMemcpyAsync");
-        ctx.finish();
-        st.first_loss = hl[0];
-        st.last_loss = hl[steps - 1];
-    };
-    if (train) {
-        kernel_timer kt(ctx, "learned.train");
-        TrainArgs ta{params, frame, xs, ys, M, partial.as<float>(), barrier, nullptr, losses, steps, lr,
-                     ctx.d_error};
-        launch_train(ctx, ta, G);
-    }
-    {
-        kernel_timer kt(ctx, "learned.splitters");
-        if (opt.splitters_in != nullptr)
-            check_cuda(cudaMemcpyAsync(sp, opt.splitters_in, (std::size_t)(buckets - 1) * 4, cudaMemcpyHostToDevice,
-                                       ctx.stream),
-                       "cudaMemcpyAsync");
-        else
-            k_splitters<<<(buckets + 127) / 128, 128, 0, ctx.stream>>>(params, frame, buckets, sp,
-                                                                       opt.use_model ? 1 : 0);
-        k_lut<<<(NCELLS + 1 + 255) / 256, 256, 0, ctx.stream>>>(sp, buckets, frame, lut);
-        check_cuda(cudaGetLastError(), "learned splitter launch");
-    }
-
-    // A model that would leave most keys in oversized buckets cannot beat the
-    // plain sort: decide from the sample, before the partition.
     const uint32_t cap = segsort_cta_cap(4, false);
-    k_estimate<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(sample.as<uint32_t>(), S, sp, buckets, nn, cap,
-                                                               dstats + 6);
-    check_cuda(cudaGetLastError(), "learned estimate launch");
-    uint32_t est = 0;
-    check_cuda(cudaMemcpyAsync(&est, dstats + 6, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
-    ctx.finish();
+    const uint32_t est =
+        build_model(ctx, sample.as<uint32_t>(), S, sh.M, sh.G, buckets, nn, cap, false, opt, steps, sh.lr, mb.m);
+    auto read_losses = [&] {
+        if (train) read_training(ctx, opt, steps, mb.m.losses, mb.m.params, st);
+    };
     st.buckets = buckets;
     st.estimated_oversized_keys = (uint32_t)std::min<uint64_t>(n, (uint64_t)est * n / S);
     if ((uint64_t)est * 2 > S) {
@@ -783,6 +983,178 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         st.fallback = 1;
         radix_sort(ctx, keys_in, keys_out, 4, key_kind, nullptr, nullptr, n, false);
     }
+    if (stats_host) *stats_host = st;
+}
+
+void learned_sort_pairs(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
+                        const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, const learned_options& opt,
+                        learned_stats* stats_host)
+{
+    using namespace learned;
+    if (key_bytes != 4 && key_bytes != 8) throw std::invalid_argument("sort_learned_pairs: keys must be 4 or 8 bytes");
+    if (key_kind < 0 || key_kind > (key_bytes == 4 ? 2 : 1))
+        throw std::invalid_argument("sort_learned_pairs: unknown key kind");
+    check_size(n);
+    if (n == 0) {
+        if (stats_host) *stats_host = learned_stats{};
+        return;
+    }
+    if (keys_in == nullptr || keys_out == nullptr || vals_in == nullptr || vals_out == nullptr)
+        throw std::invalid_argument("sort_learned_pairs: null argument");
+    if (keys_in == keys_out || vals_in == vals_out)
+        throw std::invalid_argument("sort_learned_pairs: inputs and outputs must differ");
+    ctx.activate();
+    learned_stats st;
+    if (n == 1) {
+        check_cuda(cudaMemcpyAsync(keys_out, keys_in, key_bytes, cudaMemcpyDeviceToDevice, ctx.stream),
+                   "cudaMemcpyAsync");
+        check_cuda(cudaMemcpyAsync(vals_out, vals_in, 4, cudaMemcpyDeviceToDevice, ctx.stream), "cudaMemcpyAsync");
+        if (stats_host) *stats_host = st;
+        return;
+    }
+    const uint32_t nn = (uint32_t)n;
+    const learned_shape sh = shape_for(ctx, n, opt);
+    const uint32_t S = sh.S, buckets = sh.buckets;
+    const int steps = sh.steps;
+    model_buffers mb(ctx, sh);
+    temp_buffer sample(ctx.resource, (std::size_t)S * 8 + 16);
+    temp_buffer sample32(ctx.resource, (std::size_t)S * 4);
+    temp_buffer proj(ctx.resource, sizeof(Proj));
+    Proj* pj = proj.as<Proj>();
+
+    // 1. the sorted sample in the order-preserving form, projected to 32 bits
+    {
+        kernel_timer kt(ctx, "learned.sample");
+        if (key_bytes == 8) {
+            k_sample64<<<(S + 255) / 256, 256, 0, ctx.stream>>>(static_cast<const uint64_t*>(keys_in), nn,
+                                                                 sample.as<uint64_t>(), S, key_kind);
+        } else {
+            k_sample<<<(S + 255) / 256, 256, 0, ctx.stream>>>(static_cast<const uint32_t*>(keys_in), nn,
+                                                               sample32.as<uint32_t>(), S, key_kind);
+        }
+        check_cuda(cudaGetLastError(), "learned sample launch");
+    }
+    if (key_bytes == 8) {
+        radix_sort(ctx, sample.get(), sample.get(), 8, 0, nullptr, nullptr, S, false);
+        k_project<<<1, 1024, 0, ctx.stream>>>(sample.as<uint64_t>(), S, pj, sample32.as<uint32_t>());
+        check_cuda(cudaGetLastError(), "learned projection launch");
+    } else {
+        radix_sort(ctx, sample32.get(), sample32.get(), 4, 0, nullptr, nullptr, S, false);
+        const Proj identity{0ull, 0, 0};
+        check_cuda(cudaMemcpyAsync(pj, &identity, sizeof(Proj), cudaMemcpyHostToDevice, ctx.stream), "cudaMemcpyAsync");
+    }
+
+    // 2-4. the model, its splitters, and the decision from the sample
+    const bool train = opt.use_model && steps > 0;
+    const uint32_t cap = segsort_cta_cap(key_bytes, true);
+    // buckets holding one key value are left as the stable partition leaves
+    // them (already in order), so they do not count against the model
+    const uint32_t est = build_model(ctx, sample32.as<uint32_t>(), S, sh.M, sh.G, buckets, nn, cap, true, opt, steps,
+                                     sh.lr, mb.m);
+    st.buckets = buckets;
+    st.estimated_oversized_keys = (uint32_t)std::min<uint64_t>(n, (uint64_t)est * n / S);
+    auto plain = [&] {
+        st.fallback = 1;
+        radix_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, false);
+    };
+    if ((uint64_t)est * 2 > S) {
+        if (train) read_training(ctx, opt, steps, mb.m.losses, mb.m.params, st);
+        plain();
+        if (stats_host) *stats_host = st;
+        return;
+    }
+
+    // 5. stable partition: bucket of every key, the indices stably sorted by
+    // bucket (the plain radix sort, whose pass plan skips the digits that no
+    // bucket number uses), keys and values gathered in that order
+    temp_buffer ids(ctx.resource, (std::size_t)n * 4), idx(ctx.resource, (std::size_t)n * 4);
+    temp_buffer ids_sorted(ctx.resource, (std::size_t)n * 4), perm(ctx.resource, (std::size_t)n * 4);
+    temp_buffer boff(ctx.resource, ((std::size_t)buckets + 1) * 4);
+    const std::size_t ids_smem = (std::size_t)(buckets - 1) * 4 + (std::size_t)(NCELLS + 1) * 2;
+    {
+        kernel_timer kt(ctx, "learned.count");
+        const int grid = ctx.sm_count * 2;
+        if (key_bytes == 8) {
+            static const bool set8 = [&] {
+                check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)ctx.smem_optin),
+                           "cudaFuncSetAttribute");
+                return true;
+            }();
+            (void)set8;
+            k_bucket_ids<uint64_t><<<grid, PART_THREADS, ids_smem, ctx.stream>>>(
+                static_cast<const uint64_t*>(keys_in), nn, key_kind, pj, mb.m.frame, mb.m.sp, mb.m.lut, buckets,
+                ids.as<uint32_t>(), idx.as<uint32_t>());
+        } else {
+            static const bool set4 = [&] {
+                check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)ctx.smem_optin),
+                           "cudaFuncSetAttribute");
+                return true;
+            }();
+            (void)set4;
+            k_bucket_ids<uint32_t><<<grid, PART_THREADS, ids_smem, ctx.stream>>>(
+                static_cast<const uint32_t*>(keys_in), nn, key_kind, pj, mb.m.frame, mb.m.sp, mb.m.lut, buckets,
+                ids.as<uint32_t>(), idx.as<uint32_t>());
+        }
+        check_cuda(cudaGetLastError(), "learned bucket launch");
+    }
+    radix_sort(ctx, ids.get(), ids_sorted.get(), 4, 0, idx.as<uint32_t>(), perm.as<uint32_t>(), n, false);
+    {
+        kernel_timer kt(ctx, "learned.scatter");
+        k_bucket_offsets<<<(buckets + 1 + 255) / 256, 256, 0, ctx.stream>>>(ids_sorted.as<uint32_t>(), nn, buckets,
+                                                                            boff.as<uint32_t>());
+        const int grid = ctx.sm_count * 8;
+        if (key_bytes == 8)
+            k_gather<uint64_t><<<grid, 256, 0, ctx.stream>>>(static_cast<const uint64_t*>(keys_in), vals_in,
+                                                             perm.as<uint32_t>(), nn,
+                                                             static_cast<uint64_t*>(keys_out), vals_out);
+        else
+            k_gather<uint32_t><<<grid, 256, 0, ctx.stream>>>(static_cast<const uint32_t*>(keys_in), vals_in,
+                                                             perm.as<uint32_t>(), nn,
+                                                             static_cast<uint32_t*>(keys_out), vals_out);
+        check_cuda(cudaGetLastError(), "learned gather launch");
+    }
+    // 6. every bucket that holds two different keys finished in place by the
+    // stable segmented sort; the others are already in order
+    temp_buffer skip(ctx.resource, buckets);
+    check_cuda(cudaMemsetAsync(skip.get(), 1, buckets, ctx.stream), "cudaMemsetAsync");
+    {
+        kernel_timer kt(ctx, "learned.scatter");
+        if (key_bytes == 8)
+            k_mixed_buckets<uint64_t><<<ctx.sm_count * 8, 256, 0, ctx.stream>>>(
+                static_cast<const uint64_t*>(keys_out), ids_sorted.as<uint32_t>(), nn, skip.as<uint8_t>());
+        else
+            k_mixed_buckets<uint32_t><<<ctx.sm_count * 8, 256, 0, ctx.stream>>>(
+                static_cast<const uint32_t*>(keys_out), ids_sorted.as<uint32_t>(), nn, skip.as<uint8_t>());
+        check_cuda(cudaGetLastError(), "learned bucket check launch");
+    }
+    seg_options so;
+    so.skip = skip.as<uint8_t>();
+    segmented_sort(ctx, keys_out, keys_out, key_bytes, key_kind, vals_out, vals_out, n, boff.as<uint32_t>(), buckets,
+                   false, so);
+    // 7. statistics and the boundary check
+    {
+        kernel_timer kt(ctx, "learned.check");
+        if (key_bytes == 8)
+            k_check_any<uint64_t><<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(
+                static_cast<const uint64_t*>(keys_out), boff.as<uint32_t>(), buckets, key_kind, cap, mb.dstats);
+        else
+            k_check_any<uint32_t><<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(
+                static_cast<const uint32_t*>(keys_out), boff.as<uint32_t>(), buckets, key_kind, cap, mb.dstats);
+        check_cuda(cudaGetLastError(), "learned check launch");
+    }
+    std::vector<uint32_t> hs(6);
+    check_cuda(cudaMemcpyAsync(hs.data(), mb.dstats, 6 * 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    if (train) read_training(ctx, opt, steps, mb.m.losses, mb.m.params, st);
+    ctx.finish();
+    st.violation = hs[0];
+    st.oversized_keys = hs[1];
+    st.oversized_buckets = hs[2];
+    st.largest_bucket = hs[3];
+    st.nonempty_buckets = hs[4];
+    st.constant_keys = hs[5];
+    if (st.violation) plain();
     if (stats_host) *stats_host = st;
 }
 

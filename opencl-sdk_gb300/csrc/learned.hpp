@@ -45,6 +45,17 @@ struct learned_stats {
 void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_kind, std::size_t n,
                   const learned_options& opt, learned_stats* stats_host);
 
+//! The same for key-value pairs, stable: 32-bit keys (kind 0, 1, 2) or 64-bit
+//! keys (kind 0 unsigned, 1 signed) with 32-bit values; output identical to
+//! radix_sort's. 64-bit keys are bucketed through a monotone 32-bit
+//! projection fitted to the sample's range; the partition keeps the input
+//! order inside every bucket (the bucket numbers are sorted stably with the
+//! keys' indices, and keys and values gathered in that order), and the
+//! buckets are finished by the stable segmented sort.
+void learned_sort_pairs(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
+                        const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, const learned_options& opt,
+                        learned_stats* stats_host);
+
 //! One forward/backward pass of the network over m points on the GPU:
 //! gradient of the mean squared error with respect to the raw parameters.
 //! Points are keys in the order-preserving 32-bit domain; the network's first

@@ -76,6 +76,7 @@ template <typename K> struct SegArgs {
     uint32_t* out_v;
     uint32_t* alt_v;
     const uint32_t* off;
+    const uint8_t* skip;  // per segment: nonzero = already in order (in-place calls)
     uint32_t nseg;
     uint32_t cta_cap;
     dev::KeyXform<K> xf;
@@ -106,7 +107,7 @@ template <typename K> __global__ void k_seg_classify(SegArgs<K> a)
             continue;
         }
         const uint32_t len = e - b;
-        if (len == 0) continue;
+        if (len == 0 || (a.skip != nullptr && a.skip[i] != 0)) continue;
         if (len <= WARP_CAP) {
             a.warp_list[atomicAdd(&a.ctl->n_warp, 1u)] = i;
         } else if (len <= a.cta_cap) {
@@ -652,6 +653,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     a.out_v = out_v;
     a.alt_v = alt_v.as<uint32_t>();
     a.off = off;
+    a.skip = opt.skip;
     a.nseg = (uint32_t)nseg;
     a.cta_cap = cta_cap;
     a.xf = xf;
@@ -748,6 +750,8 @@ void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, in
     if (offsets == nullptr || keys_in == nullptr || keys_out == nullptr)
         throw std::invalid_argument("segmented_sort: null argument");
     if (num_segments > 0x7FFFFFFFu) throw std::length_error("segmented_sort: too many segments");
+    if (opt.skip != nullptr && (keys_in != keys_out || vals_in != vals_out))
+        throw std::invalid_argument("segmented_sort: skipped segments need an in-place call");
     ctx.activate();
     if (key_bytes == 4) {
         const auto xf = dev::make_xform<uint32_t>(key_kind, descending);

@@ -11,6 +11,9 @@ namespace gbc {
 //! Launch-shape choices of the segmented sort (picked by the autotuner).
 struct seg_options {
     int cta_cap = 0;  // largest segment a single CTA sorts in shared memory (0: the type's maximum)
+    // device, one byte per segment or null: nonzero marks a segment already in
+    // order (every key equal), left untouched; only for in-place calls
+    const uint8_t* skip = nullptr;
 };
 
 //! Sorts every segment [offsets[i], offsets[i+1]) independently and stably.

@@ -181,6 +181,7 @@ _PROTOS = {
     "clc_reduce_by_key_raw": (_i, [_vp, _vp, _i, _vp, _sz, _vp, _vp, _vp, _vp, C.POINTER(_sz)]),
     "clc_learned_default_options": (None, [_vp]),
     "clc_sort_learned": (_i, [_vp, _vp, _vp, _i, _sz, _vp, _vp]),
+    "clc_sort_learned_pairs": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _vp, _vp]),
     "clc_learned_param_count": (_i, []),
     "clc_autotune_sort": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _i, _vp, _vp]),
     "clc_autotune_segmented_sort": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _vp, _sz, _i, _vp, _vp]),
@@ -685,6 +686,17 @@ def sort_learned(ctx: Context, keys_in: int, keys_out: int, key_dtype, n: int,
     st = LearnedStats()
     _raise_for(lib.clc_sort_learned(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype), n,
                                     C.byref(options) if options is not None else None, C.byref(st)))
+    return st
+
+
+def sort_learned_pairs(ctx: Context, keys_in: int, keys_out: int, key_dtype, vals_in: int, vals_out: int, n: int,
+                       options: LearnedOptions | None = None) -> LearnedStats:
+    """Learned-CDF sort of key-value pairs (32- or 64-bit keys, 32-bit values),
+    stable, out of place, on device pointers; returns its statistics."""
+    st = LearnedStats()
+    _raise_for(lib.clc_sort_learned_pairs(ctx.handle, C.c_void_p(keys_in), C.c_void_p(keys_out), clc_type(key_dtype),
+                                          C.c_void_p(vals_in), C.c_void_p(vals_out), n,
+                                          C.byref(options) if options is not None else None, C.byref(st)))
     return st
 
 

@@ -137,3 +137,108 @@ def test_given_splitters_any_order_stays_exact(ctx, gbc, reverse):
     assert st.violation == 0
     if not reverse:
         assert st.fallback == 0 and st.nonempty_buckets > B * 3 // 4
+
+
+# ---- key-value form (64-bit keys for the sort -> reduce_by_key pipeline) ----
+
+def splitmix64(x):
+    with np.errstate(over="ignore"):
+        z = x + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def pair_keys(case, n, rng):
+    if case == "zipf_splitmix":
+        return splitmix64((rng.zipf(1.1, n) % (1 << 24)).astype(np.uint64))
+    if case == "raw_ranks":
+        return (rng.zipf(1.1, n) % (1 << 24)).astype(np.uint64)
+    if case == "uniform_i64":
+        return rng.integers(-(1 << 63), (1 << 63) - 1, size=n, dtype=np.int64)
+    return rng.integers(0, 1 << 64, size=n, dtype=np.uint64)
+
+
+def plain_pairs(ctx, gbc, keys, vals):
+    kin, vin = gbc.DeviceBuffer.from_host(ctx, keys), gbc.DeviceBuffer.from_host(ctx, vals)
+    kout, vout = gbc.DeviceBuffer(ctx, keys.size, keys.dtype), gbc.DeviceBuffer(ctx, keys.size, np.uint32)
+    gbc.sort_raw(ctx, kin.device_pointer, kout.device_pointer, keys.dtype, keys.size, vin.device_pointer,
+                 vout.device_pointer)
+    return kout.to_host(), vout.to_host()
+
+
+def learned_pairs(ctx, gbc, keys, vals, **kw):
+    kin, vin = gbc.DeviceBuffer.from_host(ctx, keys), gbc.DeviceBuffer.from_host(ctx, vals)
+    kout, vout = gbc.DeviceBuffer(ctx, max(keys.size, 1), keys.dtype), gbc.DeviceBuffer(ctx, max(keys.size, 1), np.uint32)
+    st = gbc.sort_learned_pairs(ctx, kin.device_pointer, kout.device_pointer, keys.dtype, vin.device_pointer,
+                                vout.device_pointer, keys.size, gbc.learned_options(**kw))
+    return kout.to_host()[: keys.size], vout.to_host()[: keys.size], st
+
+
+@pytest.mark.parametrize("case", ["zipf_splitmix", "raw_ranks", "uniform_u64", "uniform_i64"])
+def test_learned_pairs_64bit_bit_identical_to_plain(ctx, gbc, case):
+    # the pipeline's keys: splitmix64 of Zipf(1.1) ranks over 2^24 values, the
+    # raw ranks, and uniform 64-bit keys; values uniform in [0, 2^16) so that
+    # equal keys check stability
+    rng = np.random.default_rng(len(case))
+    n = 3_000_001
+    keys = pair_keys(case, n, rng)
+    vals = rng.integers(0, 1 << 16, size=n, dtype=np.uint32)
+    k, v, st = learned_pairs(ctx, gbc, keys, vals)
+    rk, rv = plain_pairs(ctx, gbc, keys, vals)
+    assert np.array_equal(k, rk) and np.array_equal(v, rv)
+    assert st.violation == 0
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float32, np.uint64, np.int64])
+def test_learned_pairs_key_types_and_small_sizes(ctx, gbc, dtype):
+    rng = np.random.default_rng(7)
+    for n in (0, 1, 2, 5, 255, 4097, 300_001):
+        if np.dtype(dtype).kind == "f":
+            keys = learned_mixture(max(n, 1), seed=n)[:n]
+        else:
+            info = np.iinfo(dtype)
+            keys = rng.integers(info.min, info.max, size=n, dtype=dtype, endpoint=True)
+            if n:
+                keys[::7] = keys[0]  # duplicates: stability
+        vals = np.arange(n, dtype=np.uint32)
+        k, v, st = learned_pairs(ctx, gbc, keys, vals, sample=min(max(n, 1), 1 << 16))
+        rk, rv = plain_pairs(ctx, gbc, keys, vals) if n else (keys, vals)
+        assert np.array_equal(k.view(np.uint8), rk.view(np.uint8)) and np.array_equal(v, rv)
+
+
+def test_learned_pairs_mixture_trains_and_partitions(ctx, gbc):
+    keys = learned_mixture(1 << 22, seed=13)
+    vals = np.arange(keys.size, dtype=np.uint32)
+    k, v, st = learned_pairs(ctx, gbc, keys, vals)
+    rk, rv = plain_pairs(ctx, gbc, keys, vals)
+    assert np.array_equal(k.view(np.uint32), rk.view(np.uint32)) and np.array_equal(v, rv)
+    assert st.fallback == 0 and st.violation == 0 and st.last_loss < st.first_loss
+    assert st.nonempty_buckets > st.buckets // 2
+
+
+def test_learned_pairs_bad_network_falls_back(ctx, gbc):
+    keys = pair_keys("zipf_splitmix", 1 << 20, np.random.default_rng(2))
+    vals = np.arange(keys.size, dtype=np.uint32)
+    bad = np.zeros(gbc.learned_param_count(), dtype=np.float32)
+    bad[0:H] = -30.0
+    bad[2 * H:2 * H + H * H] = -30.0
+    bad[3 * H + H * H:4 * H + H * H] = -30.0
+    k, v, st = learned_pairs(ctx, gbc, keys, vals, steps=0, params_in=bad.ctypes.data)
+    rk, rv = plain_pairs(ctx, gbc, keys, vals)
+    assert st.fallback == 1
+    assert np.array_equal(k, rk) and np.array_equal(v, rv)
+
+
+def test_learned_pairs_zipf_heads_need_no_sort(ctx, gbc):
+    # Zipf(1.1): the most frequent keys fill whole buckets with one key value;
+    # those buckets are left as the stable partition leaves them, so the model
+    # is used rather than the plain sort
+    rng = np.random.default_rng(21)
+    keys = pair_keys("zipf_splitmix", 1 << 22, rng)
+    vals = rng.integers(0, 1 << 16, size=keys.size, dtype=np.uint32)
+    k, v, st = learned_pairs(ctx, gbc, keys, vals)
+    rk, rv = plain_pairs(ctx, gbc, keys, vals)
+    assert np.array_equal(k, rk) and np.array_equal(v, rv)
+    assert st.fallback == 0 and st.violation == 0
+    assert st.constant_keys > keys.size // 10  # the heads (14% of the keys at this seed)

@@ -45,3 +45,43 @@ def test_reduce_by_key_long_runs_and_u32(ctx, gbc, orc):
         assert runs == eko.size
         assert np.array_equal(ko.to_host()[:runs], eko) and np.array_equal(so.to_host()[:runs], eso)
         assert np.array_equal(co.to_host()[:runs], eco) and np.array_equal(hist.to_host(), eh)
+
+
+def test_compute_pipeline_sample_flow(ctx, gbc, orc):
+    # samples/core/compute-pipeline/main.cpp:94-183 with its default 1,000,000
+    # readings, minus the file I/O, bitpack and static_map stages (outside the
+    # primitive core): the calibration table lookup stands in as sensor % 7,
+    # computed on the host. mt19937(42) raw outputs, four per reading (the
+    # reading's two draws taken left to right).
+    n = 1_000_000
+    r = orc.random_uints(4 * n, 0xFFFFFFFF, 42).astype(np.uint64)
+    sensors = (r[1::4] % 1000).astype(np.uint32)
+    readings = (150 + r[2::4] % 300 + np.where(r[3::4] % 1000 == 0, 600, 0)).astype(np.uint32)
+    offsets = sensors % np.uint32(7)
+
+    d_readings = gbc.DeviceBuffer.from_host(ctx, readings)
+    d_offsets = gbc.DeviceBuffer.from_host(ctx, offsets)
+    gbc.transform(ctx, d_readings, d_offsets, d_readings, "x + y")  # calibrate in place
+    cal = readings + offsets
+    hottest = gbc.reduce(ctx, d_readings, gbc.ops.maximum(np.uint32), 0)
+    hist = gbc.DeviceBuffer(ctx, 12, np.uint32)
+    gbc.histogram_even(ctx, d_readings, hist, 0.0, 1200.0)
+    d_alarms = gbc.DeviceBuffer(ctx, n, np.uint32)
+    alarms = gbc.copy_if(ctx, d_readings, d_alarms, "x >= 700u")
+    d_f = gbc.DeviceBuffer(ctx, n, np.float32)
+    gbc.transform(ctx, d_readings, d_f, "x * 0.18f + 32.0f")
+    d_order = gbc.DeviceBuffer(ctx, n, np.uint32)
+    gbc.sequence(ctx, d_order)
+    gbc.sort_by_key(ctx, d_readings, d_order, descending=True)
+    top = d_order.to_host()
+
+    # the sample's own host checks
+    assert hottest == cal.max()
+    assert alarms == int((cal >= 700).sum())
+    assert np.array_equal(hist.to_host(), np.bincount(cal[cal < 1200] // 100, minlength=12).astype(np.uint32))
+    assert cal[top[0]] == cal.max()
+    # and every array exactly
+    assert np.array_equal(d_alarms.to_host()[:alarms], cal[cal >= 700])
+    assert np.array_equal(d_f.to_host(), cal.astype(np.float32) * np.float32(0.18) + np.float32(32.0))
+    assert np.array_equal(top, np.argsort(-cal.astype(np.int64), kind="stable").astype(np.uint32))
+    assert np.array_equal(d_readings.to_host(), cal[top])

@@ -38,8 +38,10 @@
 //   4. splitters: s_b = min{u : F(u) >= b / B} by bisection over the key
 //      domain, b = 1 .. B-1; a lookup table over the top bits of (u - umin)
 //      narrows each key's search to the splitters inside its cell;
-//   5. count keys per (CTA chunk, bucket), exclusive offsets, scatter;
-//   6. segmented sort of the B buckets; 7. boundary check; fallback if needed.
+//   5. count keys per (CTA chunk, bucket), exclusive offsets, then the
+//      keys partitioned in two levels (groups of buckets, then buckets);
+//   6. segmented sort of the B buckets, except those holding one key value;
+//   7. boundary check; fallback if needed.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -63,6 +65,9 @@ constexpr int PSTRIDE = TRAIN_THREADS + 1;  // padded row of per-point activatio
 constexpr int LUT_BITS = 12;                // splitter lookup table: 2^12 cells
 constexpr int NCELLS = 1 << LUT_BITS;
 constexpr int PART_THREADS = 1024;
+constexpr int PART_ITEMS = 8;               // keys in flight per thread in the partition passes
+constexpr uint32_t PART_GROUP = 128;        // buckets per group of the first partition level
+constexpr uint32_t PART_RANGE = 2 * PART_THREADS;  // widest bucket range a second-level chunk stages
 
 __host__ __device__ __forceinline__ bool is_weight(int i)
 {
@@ -324,8 +329,18 @@ __global__ void __launch_bounds__(TRAIN_THREADS, 1) k_train(TrainArgs a)
         const float b1c = 1.f - powf(0.9f, (float)(step + 1)), b2c = 1.f - powf(0.999f, (float)(step + 1));
         const float* base = a.partial + (size_t)(step & 1) * gridDim.x * (NPARAM + 1);
         for (int i = tid; i <= NPARAM; i += TRAIN_THREADS) {
+            // 16 partials in flight per round trip to L2; summed in CTA order
+            const float* col = base + i;
             float sum = 0.f;
-            for (uint32_t c = 0; c < gridDim.x; ++c) sum += __ldcg(base + (size_t)c * (NPARAM + 1) + i);
+            uint32_t c = 0;
+            for (; c + 16 <= gridDim.x; c += 16) {
+                float v[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = __ldcg(col + (size_t)(c + q) * (NPARAM + 1));
+#pragma unroll
+                for (int q = 0; q < 16; ++q) sum += v[q];
+            }
+            for (; c < gridDim.x; ++c) sum += __ldcg(col + (size_t)c * (NPARAM + 1));
             if (i == NPARAM) {
                 if (blockIdx.x == 0 && a.loss_out != nullptr) a.loss_out[step] = sum * inv_m;
                 continue;
@@ -446,10 +461,28 @@ __host__ __device__ constexpr std::size_t part_smem_bytes(uint32_t buckets)
     return (std::size_t)buckets * 4 + (std::size_t)(buckets - 1) * 4 + (std::size_t)(NCELLS + 1) * 2;
 }
 
-// Loads the splitters and the table into shared memory; returns the bucketer.
-__device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* sh)
+// k_partition_buckets: splitters, table (rounded to words), 2 x PART_RANGE
+// words, the staged chunk's keys and buckets.
+__host__ __device__ constexpr std::size_t bucket_smem_bytes(uint32_t buckets)
 {
-    uint32_t* sp = sh + a.buckets;
+    return ((std::size_t)(buckets - 1) + (NCELLS + 2) / 2 + 2 * PART_RANGE + (std::size_t)PART_ITEMS * PART_THREADS) *
+               4 +
+           (std::size_t)PART_ITEMS * PART_THREADS * 2;
+}
+
+// k_partition_groups: splitters, table (rounded to words), 2 x groups words,
+// the staged chunk's keys and groups.
+__host__ __device__ constexpr std::size_t group_smem_bytes(uint32_t buckets)
+{
+    return ((std::size_t)(buckets - 1) + (NCELLS + 2) / 2 + 2 * ((buckets + PART_GROUP - 1) / PART_GROUP) +
+            (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
+           (std::size_t)PART_ITEMS * PART_THREADS * 2;
+}
+
+// Loads the splitters (at sp) and the table (after them) into shared
+// memory; returns the bucketer.
+__device__ __forceinline__ Bucketer load_bucketer_at(const PartArgs& a, uint32_t* sp)
+{
     uint16_t* lut = reinterpret_cast<uint16_t*>(sp + (a.buckets - 1));
     for (uint32_t i = threadIdx.x; i + 1 < a.buckets; i += PART_THREADS) sp[i] = a.sp[i];
     for (int i = threadIdx.x; i <= NCELLS; i += PART_THREADS) lut[i] = a.lut[i];
@@ -457,7 +490,13 @@ __device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* s
     return Bucketer{sp, lut, umin, lut_shift(umin, umax)};
 }
 
-__global__ void __launch_bounds__(PART_THREADS) k_count(PartArgs a)
+// The same with a buckets-word array (counts or cursors) before the splitters.
+__device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* sh)
+{
+    return load_bucketer_at(a, sh + a.buckets);
+}
+
+__global__ void __launch_bounds__(PART_THREADS, 1) k_count(PartArgs a)
 {
     extern __shared__ uint32_t sh[];
     uint32_t* hist = sh;  // buckets
@@ -466,7 +505,15 @@ __global__ void __launch_bounds__(PART_THREADS) k_count(PartArgs a)
     __syncthreads();
     const uint32_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
     const uint32_t b0 = min(a.n, blockIdx.x * chunk), b1 = min(a.n, b0 + chunk);
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += PART_THREADS) atomicAdd(&hist[bk(ordered(a.keys[i], a.kind))], 1u);
+    uint32_t i = b0 + threadIdx.x;
+    for (; i + (PART_ITEMS - 1) * PART_THREADS < b1; i += PART_ITEMS * PART_THREADS) {
+        uint32_t k[PART_ITEMS];
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) k[j] = a.keys[i + j * PART_THREADS];
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) atomicAdd(&hist[bk(ordered(k[j], a.kind))], 1u);
+    }
+    for (; i < b1; i += PART_THREADS) atomicAdd(&hist[bk(ordered(a.keys[i], a.kind))], 1u);
     __syncthreads();
     uint32_t* row = a.counts + (size_t)blockIdx.x * a.buckets;
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) row[i] = hist[i];
@@ -509,22 +556,224 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(const uint32_t* totals, ui
     if (threadIdx.x == 0) bucket_off[buckets] = s_carry;
 }
 
-// Keys only, so the order inside a bucket is free: shared-memory cursors.
-__global__ void __launch_bounds__(PART_THREADS) k_scatter(PartArgs a)
+// Start of every bucket group (GROUP consecutive buckets) and of every
+// bucket: the write cursors of the two partition levels.
+__global__ void k_cursors(const uint32_t* __restrict__ bucket_off, uint32_t buckets, uint32_t* __restrict__ group_cur,
+                          uint32_t* __restrict__ bucket_cur)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= buckets) return;
+    bucket_cur[b] = bucket_off[b];
+    if (b % PART_GROUP == 0) group_cur[b / PART_GROUP] = bucket_off[b];
+}
+
+// Second partition level, keys only (the order inside a bucket is free):
+// src holds the keys grouped by bucket group, so a chunk of PART_ITEMS x
+// PART_THREADS keys spans a narrow bucket range [L, R]. Per chunk: ranks
+// within each bucket by shared atomics over that range, the chunk staged in
+// shared memory in bucket order, one global reservation per bucket present,
+// then written out run by run with consecutive threads on consecutive
+// addresses. A chunk wider than PART_RANGE buckets (groups much smaller than
+// a chunk) takes one global cursor increment per key instead. Shared memory:
+// splitters and table, 2 x PART_RANGE words, the staged keys and their
+// buckets relative to L (u16).
+__global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs a, const uint32_t* __restrict__ src,
+                                                                    uint32_t* __restrict__ dst,
+                                                                    uint32_t* __restrict__ cursor)
 {
     extern __shared__ uint32_t sh[];
-    uint32_t* cursor = sh;
-    const uint32_t* row = a.counts + (size_t)blockIdx.x * a.buckets;
-    for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) cursor[i] = a.bucket_off[i] + row[i];
-    const Bucketer bk = load_bucketer(a, sh);
-    __syncthreads();
-    const uint32_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
-    const uint32_t b0 = min(a.n, blockIdx.x * chunk), b1 = min(a.n, b0 + chunk);
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += PART_THREADS) {
-        const uint32_t k = a.keys[i];
-        const uint32_t pos = atomicAdd(&cursor[bk(ordered(k, a.kind))], 1u);
-        if (pos < a.n) a.out[pos] = k;
+    constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
+    constexpr uint32_t NONE = 0xFFFFFFFFu;
+    static_assert(PART_RANGE == 2 * PART_THREADS, "two range entries per thread");
+    const Bucketer bk = load_bucketer_at(a, sh);
+    uint32_t* hist = sh + (a.buckets - 1) + (NCELLS + 2) / 2;  // [PART_RANGE]: counts, then chunk offsets
+    uint32_t* delta = hist + PART_RANGE;                       // [PART_RANGE]: global start - chunk offset
+    uint32_t* stage = delta + PART_RANGE;                      // [PER]
+    uint16_t* sbkt = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
+    __shared__ uint32_t s_warp[PART_THREADS / 32], s_lo, s_hi;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_lo = NONE;
+        s_hi = 0;
     }
+    const uint32_t chunks = (a.n + PER - 1) / PER;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const uint32_t first = c * PER;
+        const uint32_t count = min(PER, a.n - first);
+        uint32_t k[PART_ITEMS], b[PART_ITEMS], r[PART_ITEMS];
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) {
+            const uint32_t i = j * PART_THREADS + tid;
+            k[j] = i < count ? src[first + i] : 0u;
+        }
+        __syncthreads();  // the previous chunk is done (and the splitters are loaded, s_lo/s_hi reset)
+        uint32_t lo = NONE, hi = 0;
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) {
+            b[j] = j * PART_THREADS + tid < count ? bk(ordered(k[j], a.kind)) : NONE;
+            if (b[j] != NONE) {
+                lo = min(lo, b[j]);
+                hi = max(hi, b[j]);
+            }
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (lane == 0 && lo != NONE) {
+            atomicMin(&s_lo, lo);
+            atomicMax(&s_hi, hi);
+        }
+        __syncthreads();
+        const uint32_t L = s_lo, span = s_hi - s_lo + 1;  // every chunk holds at least one key
+        const bool wide = span > PART_RANGE;
+        if (!wide)
+            for (uint32_t e = tid; e < span; e += PART_THREADS) hist[e] = 0;
+        __syncthreads();
+        if (tid == 0) {  // for the next chunk: every thread has read L and span
+            s_lo = NONE;
+            s_hi = 0;
+        }
+        if (wide) {
+#pragma unroll
+            for (int j = 0; j < PART_ITEMS; ++j)
+                if (b[j] != NONE) {
+                    const uint32_t pos = atomicAdd(&cursor[b[j]], 1u);
+                    if (pos < a.n) dst[pos] = k[j];
+                }
+            continue;
+        }
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) r[j] = b[j] != NONE ? atomicAdd(&hist[b[j] - L], 1u) : 0u;
+        __syncthreads();
+        // chunk offsets (exclusive scan over the range, two entries per thread) and reservations
+        const uint32_t e0 = 2 * tid, e1 = e0 + 1;
+        const uint32_t v0 = e0 < span ? hist[e0] : 0u, v1 = e1 < span ? hist[e1] : 0u;
+        const uint32_t incl = dev::warp_inclusive_scan(v0 + v1, [](uint32_t p, uint32_t q) { return p + q; });
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; ++w) before += s_warp[w];
+        const uint32_t off0 = before + incl - v0 - v1, off1 = off0 + v0;
+        if (e0 < span) {
+            const uint32_t start = v0 != 0 ? atomicAdd(&cursor[L + e0], v0) : 0u;
+            hist[e0] = off0;
+            delta[e0] = start - off0;
+        }
+        if (e1 < span) {
+            const uint32_t start = v1 != 0 ? atomicAdd(&cursor[L + e1], v1) : 0u;
+            hist[e1] = off1;
+            delta[e1] = start - off1;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j)
+            if (b[j] != NONE) {
+                const uint32_t slot = hist[b[j] - L] + r[j];
+                stage[slot] = k[j];
+                sbkt[slot] = (uint16_t)(b[j] - L);
+            }
+        __syncthreads();
+        for (uint32_t i = tid; i < count; i += PART_THREADS) {
+            const uint32_t pos = delta[sbkt[i]] + i;
+            if (pos < a.n) dst[pos] = stage[i];
+        }
+    }
+}
+
+// First partition level, keys only: every key to its bucket group (its
+// bucket / PART_GROUP, from the same search as the counting pass, so the
+// group regions hold exactly their counted keys). Per chunk of PART_ITEMS x
+// PART_THREADS keys: ranks within each group by shared atomics, the chunk
+// staged in shared memory in group order, one global reservation per group
+// present, then written out run by run with consecutive threads on
+// consecutive addresses. Shared memory: splitters and table, then
+// 2 x groups words, the staged keys and their groups (u16).
+__global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a, uint32_t groups,
+                                                                   uint32_t* __restrict__ dst,
+                                                                   uint32_t* __restrict__ cursor)
+{
+    extern __shared__ uint32_t sh[];
+    constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
+    constexpr uint32_t NONE = 0xFFFFFFFFu;
+    const Bucketer bk = load_bucketer_at(a, sh);
+    uint32_t* hist = sh + (a.buckets - 1) + (NCELLS + 2) / 2;  // [groups]: counts, then chunk offsets
+    uint32_t* delta = hist + groups;                           // [groups]: global start - chunk offset
+    uint32_t* stage = delta + groups;                          // [PER]
+    uint16_t* sgrp = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
+    __shared__ uint32_t s_warp[PART_THREADS / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t chunks = (a.n + PER - 1) / PER;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const uint32_t first = c * PER;
+        const uint32_t count = min(PER, a.n - first);
+        uint32_t k[PART_ITEMS], g[PART_ITEMS], r[PART_ITEMS];
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) {
+            const uint32_t i = j * PART_THREADS + tid;
+            k[j] = i < count ? a.keys[first + i] : 0u;
+        }
+        __syncthreads();  // the previous chunk's write-out is done (and the splitters are loaded)
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j)
+            g[j] = j * PART_THREADS + tid < count ? bk(ordered(k[j], a.kind)) / PART_GROUP : NONE;
+        for (uint32_t i = tid; i < groups; i += PART_THREADS) hist[i] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j) r[j] = g[j] != NONE ? atomicAdd(&hist[g[j]], 1u) : 0u;
+        __syncthreads();
+        // chunk offsets (exclusive scan over groups <= PART_THREADS) and reservations
+        const uint32_t v = tid < groups ? hist[tid] : 0u;
+        const uint32_t incl = dev::warp_inclusive_scan(v, [](uint32_t p, uint32_t q) { return p + q; });
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (tid < groups) {
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w) before += s_warp[w];
+            const uint32_t off = before + incl - v;
+            const uint32_t start = v != 0 ? atomicAdd(&cursor[tid], v) : 0u;
+            hist[tid] = off;
+            delta[tid] = start - off;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PART_ITEMS; ++j)
+            if (g[j] != NONE) {
+                const uint32_t slot = hist[g[j]] + r[j];
+                stage[slot] = k[j];
+                sgrp[slot] = (uint16_t)g[j];
+            }
+        __syncthreads();
+        for (uint32_t i = tid; i < count; i += PART_THREADS) {
+            const uint32_t pos = delta[sgrp[i]] + i;
+            if (pos < a.n) dst[pos] = stage[i];
+        }
+    }
+}
+
+// skip[b] = 1 when bucket b holds at most one distinct key (already in
+// order, so the segmented sort leaves it alone); one CTA per bucket, leaving
+// at the first key that differs from the bucket's first.
+__global__ void __launch_bounds__(256) k_constant_buckets(const uint32_t* __restrict__ out,
+                                                          const uint32_t* __restrict__ bucket_off,
+                                                          uint8_t* __restrict__ skip)
+{
+    const uint32_t b = blockIdx.x;
+    const uint32_t s = bucket_off[b], e = bucket_off[b + 1];
+    if (e - s >= 2) {
+        const uint32_t first = out[s];
+        for (uint32_t base = s + 1; base < e; base += 256 * 8) {
+            bool diff = false;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const uint32_t i = base + j * 256 + threadIdx.x;
+                if (i < e && out[i] != first) diff = true;
+            }
+            if (__syncthreads_or(diff)) {
+                if (threadIdx.x == 0) skip[b] = 0;
+                return;
+            }
+        }
+    }
+    if (threadIdx.x == 0) skip[b] = 1;
 }
 
 // ---- 6/7. statistics and the boundary check ----------------------------------
@@ -645,7 +894,18 @@ __global__ void __launch_bounds__(PART_THREADS) k_bucket_ids(const K* __restrict
     const Bucketer bk{sp, lut, fr->umin, lut_shift(fr->umin, fr->umax)};
     __syncthreads();
     const uint32_t stride = gridDim.x * PART_THREADS;
-    for (uint32_t i = blockIdx.x * PART_THREADS + threadIdx.x; i < n; i += stride) {
+    uint32_t i = blockIdx.x * PART_THREADS + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        K k[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) k[j] = keys[i + j * stride];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            ids[i + j * stride] = bk(project(ordered_any<K>(k[j], kind), p));
+            idx[i + j * stride] = i + j * stride;
+        }
+    }
+    for (; i < n; i += stride) {
         ids[i] = bk(project(ordered_any<K>(keys[i], kind), p));
         idx[i] = i;
     }
@@ -684,7 +944,25 @@ __global__ void k_gather(const K* __restrict__ keys, const uint32_t* __restrict_
                          uint32_t n, K* __restrict__ keys_out, uint32_t* __restrict__ vals_out)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        uint32_t j[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) j[q] = perm[i + q * stride];
+        K k[4];
+        uint32_t v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            k[q] = keys[j[q]];
+            v[q] = vals[j[q]];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            keys_out[i + q * stride] = k[q];
+            vals_out[i + q * stride] = v[q];
+        }
+    }
+    for (; i < n; i += stride) {
         const uint32_t j = perm[i];
         keys_out[i] = keys[j];
         vals_out[i] = vals[j];
@@ -938,8 +1216,6 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     if (smem_part_set < part_smem) {
         check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
                    "cudaFuncSetAttribute");
-        check_cuda(cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
-                   "cudaFuncSetAttribute");
         smem_part_set = part_smem;
     }
     {
@@ -952,13 +1228,52 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     k_bucket_scan<<<1, 1024, 0, ctx.stream>>>(totals.as<uint32_t>(), buckets, boff.as<uint32_t>());
     check_cuda(cudaGetLastError(), "learned offsets launch");
     {
-        kernel_timer kt(ctx, "learned.scatter");
-        k_scatter<<<(int)rows, PART_THREADS, part_smem, ctx.stream>>>(pa);
-        check_cuda(cudaGetLastError(), "learned scatter launch");
+        // two levels: bucket groups into tmp, then buckets into out
+        const uint32_t groups = (buckets + PART_GROUP - 1) / PART_GROUP;
+        temp_buffer tmp(ctx.resource, (std::size_t)n * 4);
+        temp_buffer cur(ctx.resource, ((std::size_t)buckets + groups) * 4);
+        uint32_t* bucket_cur = cur.as<uint32_t>();
+        uint32_t* group_cur = bucket_cur + buckets;
+        k_cursors<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(boff.as<uint32_t>(), buckets, group_cur, bucket_cur);
+        {
+            kernel_timer kt(ctx, "learned.partition_groups");
+            const std::size_t gsmem = group_smem_bytes(buckets);
+            static std::size_t gsmem_set = 0;
+            if (gsmem_set < gsmem) {
+                check_cuda(cudaFuncSetAttribute(k_partition_groups, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)gsmem),
+                           "cudaFuncSetAttribute");
+                gsmem_set = gsmem;
+            }
+            k_partition_groups<<<(int)rows, PART_THREADS, gsmem, ctx.stream>>>(pa, groups, tmp.as<uint32_t>(),
+                                                                               group_cur);
+        }
+        {
+            kernel_timer kt(ctx, "learned.partition_buckets");
+            const std::size_t bsmem = bucket_smem_bytes(buckets);
+            static std::size_t bsmem_set = 0;
+            if (bsmem_set < bsmem) {
+                check_cuda(cudaFuncSetAttribute(k_partition_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)bsmem),
+                           "cudaFuncSetAttribute");
+                bsmem_set = bsmem;
+            }
+            k_partition_buckets<<<(int)rows, PART_THREADS, bsmem, ctx.stream>>>(pa, tmp.as<uint32_t>(), out,
+                                                                                bucket_cur);
+        }
+        check_cuda(cudaGetLastError(), "learned partition launch");
     }
-    // Finish every bucket in place (shared-memory sorts; oversized buckets
-    // take the batched onesweep path).
+    // Finish every bucket that holds two different keys in place
+    // (shared-memory sorts; oversized buckets take the batched onesweep
+    // path); buckets of one key value are already in order.
+    temp_buffer skip(ctx.resource, buckets);
+    {
+        kernel_timer kt(ctx, "learned.check");
+        k_constant_buckets<<<buckets, 256, 0, ctx.stream>>>(out, boff.as<uint32_t>(), skip.as<uint8_t>());
+        check_cuda(cudaGetLastError(), "learned bucket check launch");
+    }
     seg_options so;
+    so.skip = skip.as<uint8_t>();
     segmented_sort(ctx, out, out, 4, key_kind, nullptr, nullptr, n, boff.as<uint32_t>(), buckets, false, so);
     {
         kernel_timer kt(ctx, "learned.check");

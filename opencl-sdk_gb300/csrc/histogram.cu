@@ -16,7 +16,10 @@
 // integer inputs whose bin rule reduces exactly to value - offset (checked on
 // the host over every value of the type), the float arithmetic is skipped.
 // (Lane-private 16-bit counters, bank-conflict free but 64 KiB per 4 warps,
-// measured slower: occupancy.)
+// measured slower: occupancy. Four or eight interleaved copies of each
+// warp's histogram, lane l counting into copy l % copies, measured no faster
+// for 2^30 bytes (0.41 / 0.37 ms against 0.38) and slower for floats: the
+// shared atomic instruction rate, not bank conflicts, is the limit.)
 #include <cmath>
 #include <cstring>
 #include <limits>

@@ -583,10 +583,11 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                              steps, warmup, ("learned.", "segsort.", "sort."))
     ok = bool(torch.equal(lout, pout))
     st = stats[-1].as_dict() if stats else {}
-    entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 20 * n, ok, prof_l,
+    entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 28 * n, ok, prof_l,
           {"plain_sort_ms": ms_plain, "plain_sort_gkeys": n / (ms_plain * 1e-3) / 1e9,
            "speedup_vs_plain": ms_plain / ms_learn, "stats": st,
-           "note": "includes sampling, the sample sort and the MLP fit; bytes = 20n (count, scatter, finish)"})
+           "note": "includes sampling, the sample sort and the MLP fit; bytes = 28n (count read, two partition "
+                   "levels, finish; oversized buckets move more)"})
     del lk, lout, pout
     torch.cuda.empty_cache()
 
@@ -643,12 +644,21 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                                    torch.from_numpy(lens).cuda())
     ok = ok and bool(torch.equal(sy.to(torch.int64), csum - sx.to(torch.int64) - base))
     graph.release()
-    entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, 32 * total, ok, prof_s,
+    # bytes the chosen pass counts move: segments up to the one-CTA capacity
+    # are read and written once (24 B per u64 key + u32 value); larger ones
+    # take the batched onesweep: an 8 B histogram read and 8 digit passes of
+    # 24 B (uniform 64-bit keys: no digit position is skipped); the scan 8 B
+    large_keys = int(lens[lens > int(seg_cap)].sum())
+    seg_bytes = 24 * (total - large_keys) + (8 + 8 * 24) * large_keys + 8 * total
+    entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, seg_bytes, ok, prof_s,
           {"segments": int(lens.size), "total_keys": total, "graph": True, "autotuned_cta_capacity": seg_cap,
+           "keys_in_large_segments": large_keys,
            "includes": "segmented sort (u64 keys + u32 values) and segmented exclusive int32 scan",
            "plain_per_array_estimate_ms": per_array_est_ms,
            "speedup_vs_per_array": per_array_est_ms / ms_seg,
-           "note": "bytes: 24 B/pair (one read + one write) + 8 B/elem scan; large segments move more"})
+           "hbm_frac_one_pass": 32 * total / (ms_seg * 1e-3) / 1e9 / peak,
+           "note": "bytes: 24 B/pair in segments <= the one-CTA capacity, 200 B/pair above it (8 B histogram "
+                   "+ 8 digit passes x 24 B), 8 B/elem scan; hbm_frac_one_pass counts 32 B/key"})
     del sk, sv, sko, svo, sx, sy, seg_id, order, csum, base
     torch.cuda.empty_cache()
 

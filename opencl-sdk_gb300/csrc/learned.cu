@@ -266,21 +266,27 @@ __global__ void __launch_bounds__(TRAIN_THREADS, 1) k_train(TrainArgs a)
             }
             G[tid] = g;
             __syncthreads();
+#pragma unroll 8
             for (int q = 0; q < TRAIN_THREADS; ++q) {
                 const float d = D2[k2 * PSTRIDE + q];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) acc2[i] = fmaf(d, H1[(j2 + i) * PSTRIDE + q], acc2[i]);
             }
             if (tid < 5 * H + 1) {
+                // one loop per kind (the kind is fixed per thread): the same
+                // sums in the same order, with the loads pipelined
                 const int kind = tid / H, u1 = tid % H;
-                for (int q = 0; q < TRAIN_THREADS; ++q) {
-                    switch (kind) {
-                    case 0: acc1 += P1[u1 * PSTRIDE + q]; break;
-                    case 1: acc1 += D1[u1 * PSTRIDE + q]; break;
-                    case 2: acc1 += D2[u1 * PSTRIDE + q]; break;
-                    case 3: acc1 = fmaf(G[q], H2[u1 * PSTRIDE + q], acc1); break;
-                    default: acc1 += G[q]; break;
-                    }
+                if (kind == 3) {
+                    const float* h2 = H2 + u1 * PSTRIDE;
+#pragma unroll 8
+                    for (int q = 0; q < TRAIN_THREADS; ++q) acc1 = fmaf(G[q], h2[q], acc1);
+                } else {
+                    const float* row = kind == 0 ? P1 + u1 * PSTRIDE
+                                     : kind == 1 ? D1 + u1 * PSTRIDE
+                                     : kind == 2 ? D2 + u1 * PSTRIDE
+                                                 : G;
+#pragma unroll 8
+                    for (int q = 0; q < TRAIN_THREADS; ++q) acc1 += row[q];
                 }
             }
             __syncthreads();  // the buffers are rewritten by the next round

@@ -61,6 +61,7 @@ constexpr int OFF_V1 = 0, OFF_B1 = H, OFF_V2 = 2 * H, OFF_B2 = 2 * H + H * H, OF
 static_assert(OFF_B3 + 1 == NPARAM, "parameter layout");
 
 constexpr int TRAIN_THREADS = 256;          // one training point per thread and round
+constexpr int PSTR = (NPARAM + 1 + 3) / 4 * 4;  // a CTA's partial row (gradient sums, loss), 16-byte multiple
 constexpr int PSTRIDE = TRAIN_THREADS + 1;  // padded row of per-point activations
 constexpr int LUT_BITS = 12;                // splitter lookup table: 2^12 cells
 constexpr int NCELLS = 1 << LUT_BITS;
@@ -175,7 +176,7 @@ struct TrainArgs {
     const uint32_t* xs;  // m training keys (order-preserving form)
     const float* ys;
     uint32_t m;
-    float* partial;      // [2][gridDim.x][NPARAM + 1]
+    float* partial;      // [2][gridDim.x][PSTR]: gradient sums and the loss
     uint32_t* barrier;   // zero before the launch
     float* grad_out;     // optional: gradient at the starting parameters
     float* loss_out;     // optional: [steps] loss before each update
@@ -291,7 +292,7 @@ __global__ void __launch_bounds__(TRAIN_THREADS, 1) k_train(TrainArgs a)
             }
             __syncthreads();  // the buffers are rewritten by the next round
         }
-        float* out = a.partial + ((size_t)(step & 1) * gridDim.x + blockIdx.x) * (NPARAM + 1);
+        float* out = a.partial + ((size_t)(step & 1) * gridDim.x + blockIdx.x) * PSTR;
 #pragma unroll
         for (int i = 0; i < 4; ++i) out[OFF_V2 + k2 * H + j2 + i] = acc2[i];
         if (tid < 5 * H + 1) {
@@ -333,32 +334,50 @@ __global__ void __launch_bounds__(TRAIN_THREADS, 1) k_train(TrainArgs a)
         if (s_abort) return;
         // Every CTA sums the partials in CTA order and applies the same update.
         const float b1c = 1.f - powf(0.9f, (float)(step + 1)), b2c = 1.f - powf(0.999f, (float)(step + 1));
-        const float* base = a.partial + (size_t)(step & 1) * gridDim.x * (NPARAM + 1);
-        for (int i = tid; i <= NPARAM; i += TRAIN_THREADS) {
-            // 16 partials in flight per round trip to L2; summed in CTA order
-            const float* col = base + i;
-            float sum = 0.f;
+        const float4* base = reinterpret_cast<const float4*>(a.partial + (size_t)(step & 1) * gridDim.x * PSTR);
+        for (int c4 = tid; c4 < PSTR / 4; c4 += TRAIN_THREADS) {
+            // four sums per thread, 16 partial vectors in flight per round
+            // trip to L2; each sum taken in CTA order
+            const float4* col = base + c4;
+            float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
             uint32_t c = 0;
             for (; c + 16 <= gridDim.x; c += 16) {
-                float v[16];
+                float4 v[16];
 #pragma unroll
-                for (int q = 0; q < 16; ++q) v[q] = __ldcg(col + (size_t)(c + q) * (NPARAM + 1));
+                for (int q = 0; q < 16; ++q) v[q] = __ldcg(col + (size_t)(c + q) * (PSTR / 4));
 #pragma unroll
-                for (int q = 0; q < 16; ++q) sum += v[q];
+                for (int q = 0; q < 16; ++q) {
+                    sum.x += v[q].x;
+                    sum.y += v[q].y;
+                    sum.z += v[q].z;
+                    sum.w += v[q].w;
+                }
             }
-            for (; c < gridDim.x; ++c) sum += __ldcg(col + (size_t)c * (NPARAM + 1));
-            if (i == NPARAM) {
-                if (blockIdx.x == 0 && a.loss_out != nullptr) a.loss_out[step] = sum * inv_m;
-                continue;
+            for (; c < gridDim.x; ++c) {
+                const float4 v = __ldcg(col + (size_t)c * (PSTR / 4));
+                sum.x += v.x;
+                sum.y += v.y;
+                sum.z += v.z;
+                sum.w += v.w;
             }
-            const float grad = is_weight(i) ? sum * w[i] : sum;  // d exp(v) / dv = exp(v)
-            if (step == 0 && blockIdx.x == 0 && a.grad_out != nullptr) a.grad_out[i] = grad;
-            if (a.lr > 0.f) {
-                const float m1 = 0.9f * am[i] + 0.1f * grad;
-                const float s1 = 0.999f * as[i] + 0.001f * grad * grad;
-                am[i] = m1;
-                as[i] = s1;
-                p[i] -= a.lr * (m1 / b1c) / (sqrtf(s1 / b2c) + 1e-8f);
+            const float sums[4] = {sum.x, sum.y, sum.z, sum.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int i = 4 * c4 + e;
+                if (i > NPARAM) break;
+                if (i == NPARAM) {
+                    if (blockIdx.x == 0 && a.loss_out != nullptr) a.loss_out[step] = sums[e] * inv_m;
+                    break;
+                }
+                const float grad = is_weight(i) ? sums[e] * w[i] : sums[e];  // d exp(v) / dv = exp(v)
+                if (step == 0 && blockIdx.x == 0 && a.grad_out != nullptr) a.grad_out[i] = grad;
+                if (a.lr > 0.f) {
+                    const float m1 = 0.9f * am[i] + 0.1f * grad;
+                    const float s1 = 0.999f * as[i] + 0.001f * grad * grad;
+                    am[i] = m1;
+                    as[i] = s1;
+                    p[i] -= a.lr * (m1 / b1c) / (sqrtf(s1 / b2c) + 1e-8f);
+                }
             }
         }
         __syncthreads();
@@ -1132,7 +1151,7 @@ struct model_buffers {
     model_buffers(device_context& ctx, const learned_shape& sh)
         : pts(ctx.resource, (std::size_t)2 * sh.M * 4),
           prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16),
-          partial(ctx.resource, (std::size_t)2 * sh.G * (NPARAM + 1) * 4),
+          partial(ctx.resource, (std::size_t)2 * sh.G * PSTR * 4),
           spl(ctx.resource, (std::size_t)sh.buckets * 4 + (std::size_t)(NCELLS + 1) * 2 + 16),
           misc(ctx.resource, 64 + (std::size_t)std::max(sh.steps, 1) * 4)
     {
@@ -1488,7 +1507,7 @@ void mlp_gradients(device_context& ctx, const float* params_host, const uint32_t
     const uint32_t G = train_grid(ctx, (uint32_t)m);
     temp_buffer prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16);
     temp_buffer pts(ctx.resource, (std::size_t)2 * m * 4);
-    temp_buffer partial(ctx.resource, (std::size_t)2 * G * (NPARAM + 1) * 4);
+    temp_buffer partial(ctx.resource, (std::size_t)2 * G * PSTR * 4);
     temp_buffer misc(ctx.resource, 64 + (std::size_t)NPARAM * 4);
     float* params = prm.as<float>();
     Frame* frame = reinterpret_cast<Frame*>(

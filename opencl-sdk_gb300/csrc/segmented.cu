@@ -63,9 +63,8 @@ struct SegControl {
     uint32_t n_warp, n_cta, n_large;  // list lengths
     uint32_t large_tiles;             // tiles of all large segments
     uint32_t warp_next, cta_next;     // work queue heads
-    uint32_t hist_next;
     uint32_t tile_ctr[8];
-    uint32_t pad[5];
+    uint32_t pad[6];
 };
 
 template <typename K> struct SegArgs {
@@ -347,37 +346,89 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
 }
 
 // ---------------------------------------------------------------------------
-// Large segments: per-segment digit histograms -> absolute bin starts.
-// One CTA per large segment (work queue).
+// Large segments: per-segment digit histograms -> absolute bin starts, in
+// three steps over the large-segment tile sequence that the passes use (so
+// a long segment is spread over many CTAs): zero the rows of the large
+// segments present; count runs of HIST_TILES tiles in shared memory and add
+// the counts to the segment's row whenever the segment changes or the run
+// ends; turn every row into absolute bin starts.
 // ---------------------------------------------------------------------------
-template <typename K> __global__ void __launch_bounds__(256) k_seg_large_hist(SegArgs<K> a)
+constexpr uint32_t HIST_TILES = 8;
+
+template <typename K> __global__ void k_seg_large_zero(SegArgs<K> a)
 {
     constexpr int P = Traits<K>::PASSES;
-    __shared__ uint32_t sh[2][P * RADIX];
-    __shared__ uint32_t s_scratch[8];
-    __shared__ uint32_t s_work;
     const uint32_t nl = min(a.ctl->n_large, a.max_large);
-    for (;;) {
-        if (threadIdx.x == 0) s_work = atomicAdd(&a.ctl->hist_next, 1u);
-        for (int i = threadIdx.x; i < 2 * P * RADIX; i += 256) (&sh[0][0])[i] = 0;
+    const std::size_t words = (std::size_t)nl * P * RADIX;
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) a.seg_hist[i] = 0;
+}
+
+template <typename K, int TILE> __global__ void __launch_bounds__(256) k_seg_large_count(SegArgs<K> a)
+{
+    constexpr int P = Traits<K>::PASSES;
+    constexpr int BATCH = 8;  // keys in flight per thread
+    __shared__ uint32_t sh[2][P * RADIX];  // two copies (warp parity)
+    uint32_t* my = sh[(threadIdx.x >> 5) & 1];
+    const uint32_t total = a.ctl->large_tiles;
+    const uint32_t runs = (total + HIST_TILES - 1) / HIST_TILES;
+    auto flush = [&](uint32_t j) {  // adds the counts to row j and clears them
         __syncthreads();
-        const uint32_t j = s_work;
-        if (j >= nl) break;
-        const uint32_t s = a.large_list[j];
-        const uint32_t b = a.off[s], e = a.off[s + 1];
-        uint32_t* my = sh[(threadIdx.x >> 5) & 1];
-        for (uint32_t i = b + threadIdx.x; i < e; i += 256) {
-            const K t = a.xf(a.in_k[i]);
+        uint32_t* row = a.seg_hist + (std::size_t)j * P * RADIX;
+        for (int i = threadIdx.x; i < P * RADIX; i += 256) {
+            const uint32_t v = sh[0][i] + sh[1][i];
+            if (v != 0) atomicAdd(&row[i], v);
+            sh[0][i] = 0;
+            sh[1][i] = 0;
+        }
+        __syncthreads();
+    };
+    for (int i = threadIdx.x; i < 2 * P * RADIX; i += 256) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t r = blockIdx.x; r < runs; r += gridDim.x) {
+        const uint32_t t0 = r * HIST_TILES, t1 = min(total, t0 + HIST_TILES);
+        uint32_t j = a.tile_seg[t0];
+        for (uint32_t t = t0; t < t1; ++t) {
+            const uint32_t jt = a.tile_seg[t];  // the same for every thread
+            if (jt != j) {
+                flush(j);
+                j = jt;
+            }
+            const uint32_t s = a.large_list[jt];
+            const uint32_t b = a.off[s] + (t - a.tile_begin[jt]) * TILE;
+            const uint32_t e = min(a.off[s + 1], b + TILE);
+            for (uint32_t i0 = b; i0 < e; i0 += 256 * BATCH) {
+                K k[BATCH];
 #pragma unroll
-            for (int p = 0; p < P; ++p) atomicAdd(&my[p * RADIX + (uint32_t)((t >> (8 * p)) & 0xFF)], 1u);
+                for (int q = 0; q < BATCH; ++q) {
+                    const uint32_t i = i0 + q * 256 + threadIdx.x;
+                    k[q] = i < e ? a.in_k[i] : K(0);
+                }
+#pragma unroll
+                for (int q = 0; q < BATCH; ++q) {
+                    if (i0 + q * 256 + threadIdx.x >= e) break;
+                    const K x = a.xf(k[q]);
+#pragma unroll
+                    for (int p = 0; p < P; ++p) atomicAdd(&my[p * RADIX + (uint32_t)((x >> (8 * p)) & 0xFF)], 1u);
+                }
+            }
         }
-        __syncthreads();
+        flush(j);
+    }
+}
+
+template <typename K> __global__ void __launch_bounds__(256) k_seg_large_starts(SegArgs<K> a)
+{
+    constexpr int P = Traits<K>::PASSES;
+    __shared__ uint32_t s_scratch[8];
+    const uint32_t nl = min(a.ctl->n_large, a.max_large);
+    for (uint32_t j = blockIdx.x; j < nl; j += gridDim.x) {
+        const uint32_t b = a.off[a.large_list[j]];
         for (int p = 0; p < P; ++p) {
-            const uint32_t c = sh[0][p * RADIX + (threadIdx.x & 255)] + sh[1][p * RADIX + (threadIdx.x & 255)];
-            const uint32_t ex = dev::bins_exclusive_sum(c, s_scratch);
-            a.seg_hist[((size_t)j * P + p) * RADIX + threadIdx.x] = b + ex;
+            uint32_t* row = a.seg_hist + ((std::size_t)j * P + p) * RADIX;
+            const uint32_t ex = dev::bins_exclusive_sum(row[threadIdx.x], s_scratch);
+            row[threadIdx.x] = b + ex;
         }
-        __syncthreads();
     }
 }
 
@@ -704,8 +755,10 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     if (maybe_large) {
         k_seg_plan<K, TILE><<<1, 1024, 0, aux>>>(a);
         check_cuda(cudaGetLastError(), "segmented sort plan launch");
-        auto hk = &k_seg_large_hist<K>;
-        k_seg_large_hist<K><<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
+        k_seg_large_zero<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
+        auto hk = &k_seg_large_count<K, TILE>;
+        hk<<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
+        k_seg_large_starts<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
         check_cuda(cudaGetLastError(), "segmented sort histogram launch");
         auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS, LS::MINB, LS::LBW>;
         const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +

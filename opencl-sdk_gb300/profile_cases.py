@@ -8,7 +8,10 @@ Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
 hist-u8 (256 bins), segsort-u64kv (lognormal segments, median 256, sigma 2,
 n = total keys), rbk-u64 (reduce_by_key over sorted keys with runs, fused
 65,536-bin histogram), copy-if-i32 ("x > 0"), transform-u32f32 ("x * 0.18f +
-32.0f", uint -> float), transform2-u32 ("x + y"). Inputs are seeded synthetic
+32.0f", uint -> float), transform2-u32 ("x + y"), learned-f32 (learned-CDF
+sort of float32 keys: 75% from 8 Gaussians with means in [-1e3, 1e3] and
+sigmas log-uniform in [1e-2, 1e2], 20% lognormal(0, 2), 5% copies of 1,000 of
+those values, shuffled). Inputs are seeded synthetic
 data generated on the device; every call goes through the C ABI on the
 library's stream.
 """
@@ -126,6 +129,21 @@ def main() -> None:
                 gbc.transform(ctx, xb, ob, "x * 0.18f + 32.0f")
             else:
                 gbc.transform(ctx, xb, yb, ob, "x + y")
+    elif args.case == "learned-f32":
+        n75, n20 = int(0.75 * n), int(0.20 * n)
+        means = torch.rand(8, device="cuda", generator=g, dtype=torch.float64) * 2e3 - 1e3
+        sig = torch.exp((torch.rand(8, device="cuda", generator=g, dtype=torch.float64) * 2 - 1) * np.log(100.0))
+        comp = torch.randint(0, 8, (n75,), device="cuda", generator=g)
+        a = (means[comp] + sig[comp] * torch.randn(n75, device="cuda", generator=g, dtype=torch.float64)).float()
+        b = torch.exp(2.0 * torch.randn(n20, device="cuda", generator=g))
+        pool = torch.cat([a[:500], b[:500]])
+        c = pool[torch.randint(0, 1000, (n - n75 - n20,), device="cuda", generator=g)]
+        k = torch.cat([a, b, c])[torch.randperm(n, device="cuda", generator=g)].contiguous()
+        del a, b, c, comp
+        ko = torch.empty_like(k)
+
+        def step():
+            gbc.sort_learned(ctx, k.data_ptr(), ko.data_ptr(), np.float32, n)
     else:
         raise SystemExit(f"unknown case {args.case}")
 

@@ -1024,12 +1024,9 @@ constexpr std::size_t TRAIN_SMEM = (std::size_t)(4 * NPARAM + 5 * H * PSTRIDE + 
 
 static void launch_train(device_context& ctx, TrainArgs& ta, uint32_t grid)
 {
-    static bool smem_set = false;
-    if (!smem_set) {
-        check_cuda(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM),
-                   "cudaFuncSetAttribute");
-        smem_set = true;
-    }
+    // per device, so set on every call
+    check_cuda(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM),
+               "cudaFuncSetAttribute");
     int per_sm = 0;
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_train, TRAIN_THREADS, TRAIN_SMEM),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -1237,12 +1234,9 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     }
 
     PartArgs pa{in, out, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), boff.as<uint32_t>()};
-    static std::size_t smem_part_set = 0;
-    if (smem_part_set < part_smem) {
-        check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
-                   "cudaFuncSetAttribute");
-        smem_part_set = part_smem;
-    }
+    // shared-memory opt-in is per device: set on every call
+    check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
+               "cudaFuncSetAttribute");
     {
         kernel_timer kt(ctx, "learned.count");
         k_count<<<(int)rows, PART_THREADS, part_smem, ctx.stream>>>(pa);
@@ -1263,26 +1257,18 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         {
             kernel_timer kt(ctx, "learned.partition_groups");
             const std::size_t gsmem = group_smem_bytes(buckets);
-            static std::size_t gsmem_set = 0;
-            if (gsmem_set < gsmem) {
-                check_cuda(cudaFuncSetAttribute(k_partition_groups, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)gsmem),
-                           "cudaFuncSetAttribute");
-                gsmem_set = gsmem;
-            }
+            check_cuda(cudaFuncSetAttribute(k_partition_groups, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)gsmem),
+                       "cudaFuncSetAttribute");
             k_partition_groups<<<(int)rows, PART_THREADS, gsmem, ctx.stream>>>(pa, groups, tmp.as<uint32_t>(),
                                                                                group_cur);
         }
         {
             kernel_timer kt(ctx, "learned.partition_buckets");
             const std::size_t bsmem = bucket_smem_bytes(buckets);
-            static std::size_t bsmem_set = 0;
-            if (bsmem_set < bsmem) {
-                check_cuda(cudaFuncSetAttribute(k_partition_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)bsmem),
-                           "cudaFuncSetAttribute");
-                bsmem_set = bsmem;
-            }
+            check_cuda(cudaFuncSetAttribute(k_partition_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)bsmem),
+                       "cudaFuncSetAttribute");
             k_partition_buckets<<<(int)rows, PART_THREADS, bsmem, ctx.stream>>>(pa, tmp.as<uint32_t>(), out,
                                                                                 bucket_cur);
         }
@@ -1415,24 +1401,16 @@ void learned_sort_pairs(device_context& ctx, const void* keys_in, void* keys_out
         kernel_timer kt(ctx, "learned.count");
         const int grid = ctx.sm_count * 2;
         if (key_bytes == 8) {
-            static const bool set8 = [&] {
-                check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)ctx.smem_optin),
-                           "cudaFuncSetAttribute");
-                return true;
-            }();
-            (void)set8;
+            check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)ids_smem),
+                       "cudaFuncSetAttribute");
             k_bucket_ids<uint64_t><<<grid, PART_THREADS, ids_smem, ctx.stream>>>(
                 static_cast<const uint64_t*>(keys_in), nn, key_kind, pj, mb.m.frame, mb.m.sp, mb.m.lut, buckets,
                 ids.as<uint32_t>(), idx.as<uint32_t>());
         } else {
-            static const bool set4 = [&] {
-                check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)ctx.smem_optin),
-                           "cudaFuncSetAttribute");
-                return true;
-            }();
-            (void)set4;
+            check_cuda(cudaFuncSetAttribute(k_bucket_ids<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)ids_smem),
+                       "cudaFuncSetAttribute");
             k_bucket_ids<uint32_t><<<grid, PART_THREADS, ids_smem, ctx.stream>>>(
                 static_cast<const uint32_t*>(keys_in), nn, key_kind, pj, mb.m.frame, mb.m.sp, mb.m.lut, buckets,
                 ids.as<uint32_t>(), idx.as<uint32_t>());

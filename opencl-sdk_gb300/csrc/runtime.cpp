@@ -12,6 +12,8 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <set>
+#include <utility>
 
 #include "sort_internal.hpp"
 
@@ -389,6 +391,16 @@ std::string tuning_table::size_class(std::size_t n)
     int k = 0;
     while ((std::size_t(1) << k) < n && k < 63) ++k;
     return "2^" + std::to_string(k);
+}
+
+bool first_use_on_device(const void* kernel)
+{
+    static std::mutex m;
+    static std::set<std::pair<int, const void*>> seen;
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(m);
+    return seen.emplace(dev, kernel).second;
 }
 
 }  // namespace gbc

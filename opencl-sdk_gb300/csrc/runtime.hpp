@@ -48,6 +48,11 @@ struct build_error : std::runtime_error {
 //! Throws out_of_memory for allocation failures and device_error otherwise.
 void check_cuda(cudaError_t e, const char* what);
 
+//! True the first time it is called for `kernel` on the current device
+//! (thread-safe): for one-time per-device kernel setup such as the
+//! shared-memory opt-in, which CUDA keeps per device.
+bool first_use_on_device(const void* kernel);
+
 //! Kernels index elements with 32-bit integers: at most 2^31-1 per call
 //! (lib/src/Compute/Detail.hpp:18-23).
 void check_size(std::size_t n);

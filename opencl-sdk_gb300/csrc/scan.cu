@@ -345,13 +345,16 @@ __global__ void __launch_bounds__(THREADS, MINB) k_scan(ScanArgs<T> a)
     }
 }
 
-std::map<const void*, int> g_occ;
+std::map<std::pair<int, const void*>, int> g_occ;  // (device, kernel): attributes and occupancy are per device
 std::mutex g_occ_m;
 
 template <typename F> int blocks_per_sm(F* kernel, std::size_t smem = 0)
 {
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    const std::pair<int, const void*> key(dev, (const void*)kernel);
     std::lock_guard<std::mutex> lock(g_occ_m);
-    auto it = g_occ.find((const void*)kernel);
+    auto it = g_occ.find(key);
     if (it != g_occ.end()) return it->second;
     check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                     (int)cudaSharedmemCarveoutMaxShared),
@@ -360,7 +363,7 @@ template <typename F> int blocks_per_sm(F* kernel, std::size_t smem = 0)
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, THREADS, smem),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     b = std::max(b, 1);
-    g_occ[(const void*)kernel] = b;
+    g_occ[key] = b;
     return b;
 }
 

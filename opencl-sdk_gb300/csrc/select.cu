@@ -236,13 +236,10 @@ void run_select(device_context& ctx, const SelArgs& a0, const program& p, unsign
     SelArgs a = a0;
     const uint32_t num_tiles = (a.n + S::TILE - 1) / S::TILE;
     const std::size_t slot_bytes = STK ? (std::size_t)STACK * S::RUN * THREADS * sizeof(W) : 0;
-    static const bool ready = [&] {
+    if (first_use_on_device((const void*)&k_sel_count<SZ, W, STK>))
         check_cuda(cudaFuncSetAttribute(&k_sel_count<SZ, W, STK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)slot_bytes),
                    "cudaFuncSetAttribute");
-        return true;
-    }();
-    (void)ready;
     temp_buffer tiles(ctx.resource, (std::size_t)num_tiles * WARPS * sizeof(uint32_t));
     temp_buffer masks(ctx.resource, (std::size_t)num_tiles * WARPS * S::ITEMS * sizeof(uint32_t));
     a.tiles = tiles.as<uint32_t>();

@@ -821,11 +821,15 @@ struct KernelInfo {
 };
 
 template <typename F>
-static int prepare_kernel(F* kernel, int threads, std::size_t smem, std::map<const void*, int>& cache,
+static int prepare_kernel(F* kernel, int threads, std::size_t smem, std::map<std::pair<int, const void*>, int>& cache,
                           std::mutex& m)
 {
+    // attributes and occupancy are per device
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    const std::pair<int, const void*> key(dev, (const void*)kernel);
     std::lock_guard<std::mutex> lock(m);
-    auto it = cache.find((const void*)kernel);
+    auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     // always: static shared memory adds to the dynamic amount against the 48 KiB default
     if (smem > 0)
@@ -840,11 +844,11 @@ static int prepare_kernel(F* kernel, int threads, std::size_t smem, std::map<con
     int blocks = 0;
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, smem),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    cache[(const void*)kernel] = std::max(blocks, 1);
+    cache[key] = std::max(blocks, 1);
     return std::max(blocks, 1);
 }
 
-static std::map<const void*, int> g_occupancy;
+static std::map<std::pair<int, const void*>, int> g_occupancy;  // (device, kernel)
 static std::mutex g_occupancy_mutex;
 
 template <typename K, bool HAS_V>

@@ -1199,13 +1199,9 @@ void launch_variant(device_context& ctx, const program& p, const void* x, const 
     constexpr int V = E * K;
     auto kernel = &k_transform<W, E, K, HAS_Y, STK>;
     const std::size_t smem = STK ? (std::size_t)STACK * V * THREADS * sizeof(W) : 0;
-    static const bool ready = [&] {
-        if (smem > 48 * 1024)
-            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                       "cudaFuncSetAttribute");
-        return true;
-    }();
-    (void)ready;
+    if (smem > 48 * 1024 && first_use_on_device((const void*)kernel))
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                   "cudaFuncSetAttribute");
     const std::size_t chunks = (n + (std::size_t)THREADS * V - 1) / ((std::size_t)THREADS * V);
     kernel<<<(unsigned)chunks, THREADS, smem, ctx.stream>>>(static_cast<const unsigned char*>(x),
                                                            static_cast<const unsigned char*>(y),

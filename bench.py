@@ -11,7 +11,9 @@ flush is needed between steps.
 Printed (rank 0, one JSON line): Gkeys/s over the timed steps (CUDA events on
 the library's stream, max over ranks), the digit-pass kernel's achieved
 HBM bandwidth against MEASURED_PEAKS.json, an end-to-end figure through
-clc_buffer_write -> clc_sort -> clc_buffer_read from pinned host memory, the
+clc_buffer_write -> clc_sort -> clc_buffer_read from pinned host memory
+(double-buffered over two contexts and two host threads, with the one-step-
+at-a-time figure beside it), the
 CPU baseline (the oracle's restatement of the reference's 4-bit LSD sort on
 all host cores, on a bounded sample), SM clocks sampled during the run, and
 the other configuration workloads measured the same way under "workloads".

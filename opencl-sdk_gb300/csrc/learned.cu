@@ -38,8 +38,9 @@
 //   4. splitters: s_b = min{u : F(u) >= b / B} by bisection over the key
 //      domain, b = 1 .. B-1; a lookup table over the top bits of (u - umin)
 //      narrows each key's search to the splitters inside its cell;
-//   5. count keys per (CTA chunk, bucket), exclusive offsets, then the
-//      keys partitioned in two levels (groups of buckets, then buckets);
+//   5. count keys per (CTA chunk, bucket), storing every key's bucket,
+//      exclusive offsets, then the keys partitioned in two levels (groups
+//      of buckets, then buckets) by the stored buckets;
 //   6. segmented sort of the B buckets, except those holding one key value;
 //   7. boundary check; fallback if needed.
 #include <algorithm>
@@ -458,6 +459,7 @@ struct PartArgs {
     uint32_t buckets;
     uint32_t* counts;       // [gridDim.x][buckets]: counts, then exclusive column offsets
     uint32_t* bucket_off;   // [buckets + 1]
+    uint16_t* ids;          // [n]: every key's bucket, written by the counting pass
 };
 
 // Bucket of a key: the number of splitters <= u, searched among the splitters
@@ -486,39 +488,31 @@ __host__ __device__ constexpr std::size_t part_smem_bytes(uint32_t buckets)
     return (std::size_t)buckets * 4 + (std::size_t)(buckets - 1) * 4 + (std::size_t)(NCELLS + 1) * 2;
 }
 
-// k_partition_buckets: splitters, table (rounded to words), 2 x PART_RANGE
-// words, the staged chunk's keys and buckets.
-__host__ __device__ constexpr std::size_t bucket_smem_bytes(uint32_t buckets)
+// k_partition_buckets: 2 x PART_RANGE words, the staged chunk's keys and
+// buckets.
+__host__ __device__ constexpr std::size_t bucket_smem_bytes()
 {
-    return ((std::size_t)(buckets - 1) + (NCELLS + 2) / 2 + 2 * PART_RANGE + (std::size_t)PART_ITEMS * PART_THREADS) *
-               4 +
+    return ((std::size_t)2 * PART_RANGE + (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
            (std::size_t)PART_ITEMS * PART_THREADS * 2;
 }
 
-// k_partition_groups: splitters, table (rounded to words), 2 x groups words,
-// the staged chunk's keys and groups.
+// k_partition_groups: 2 x groups words, the staged chunk's keys and buckets.
 __host__ __device__ constexpr std::size_t group_smem_bytes(uint32_t buckets)
 {
-    return ((std::size_t)(buckets - 1) + (NCELLS + 2) / 2 + 2 * ((buckets + PART_GROUP - 1) / PART_GROUP) +
-            (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
+    return ((std::size_t)2 * ((buckets + PART_GROUP - 1) / PART_GROUP) + (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
            (std::size_t)PART_ITEMS * PART_THREADS * 2;
 }
 
-// Loads the splitters (at sp) and the table (after them) into shared
-// memory; returns the bucketer.
-__device__ __forceinline__ Bucketer load_bucketer_at(const PartArgs& a, uint32_t* sp)
+// Loads the splitters and the table into shared memory after a buckets-word
+// array (the counts); returns the bucketer.
+__device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* sh)
 {
+    uint32_t* sp = sh + a.buckets;
     uint16_t* lut = reinterpret_cast<uint16_t*>(sp + (a.buckets - 1));
     for (uint32_t i = threadIdx.x; i + 1 < a.buckets; i += PART_THREADS) sp[i] = a.sp[i];
     for (int i = threadIdx.x; i <= NCELLS; i += PART_THREADS) lut[i] = a.lut[i];
     const uint32_t umin = a.frame->umin, umax = a.frame->umax;
     return Bucketer{sp, lut, umin, lut_shift(umin, umax)};
-}
-
-// The same with a buckets-word array (counts or cursors) before the splitters.
-__device__ __forceinline__ Bucketer load_bucketer(const PartArgs& a, uint32_t* sh)
-{
-    return load_bucketer_at(a, sh + a.buckets);
 }
 
 __global__ void __launch_bounds__(PART_THREADS, 1) k_count(PartArgs a)
@@ -536,9 +530,17 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_count(PartArgs a)
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) k[j] = a.keys[i + j * PART_THREADS];
 #pragma unroll
-        for (int j = 0; j < PART_ITEMS; ++j) atomicAdd(&hist[bk(ordered(k[j], a.kind))], 1u);
+        for (int j = 0; j < PART_ITEMS; ++j) {
+            const uint32_t b = bk(ordered(k[j], a.kind));
+            atomicAdd(&hist[b], 1u);
+            a.ids[i + j * PART_THREADS] = (uint16_t)b;
+        }
     }
-    for (; i < b1; i += PART_THREADS) atomicAdd(&hist[bk(ordered(a.keys[i], a.kind))], 1u);
+    for (; i < b1; i += PART_THREADS) {
+        const uint32_t b = bk(ordered(a.keys[i], a.kind));
+        atomicAdd(&hist[b], 1u);
+        a.ids[i] = (uint16_t)b;
+    }
     __syncthreads();
     uint32_t* row = a.counts + (size_t)blockIdx.x * a.buckets;
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) row[i] = hist[i];
@@ -599,10 +601,11 @@ __global__ void k_cursors(const uint32_t* __restrict__ bucket_off, uint32_t buck
 // shared memory in bucket order, one global reservation per bucket present,
 // then written out run by run with consecutive threads on consecutive
 // addresses. A chunk wider than PART_RANGE buckets (groups much smaller than
-// a chunk) takes one global cursor increment per key instead. Shared memory:
-// splitters and table, 2 x PART_RANGE words, the staged keys and their
-// buckets relative to L (u16).
+// a chunk) takes one global cursor increment per key instead. The buckets
+// come with the keys (src_ids), so there is no search. Shared memory:
+// 2 x PART_RANGE words, the staged keys and their buckets relative to L (u16).
 __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs a, const uint32_t* __restrict__ src,
+                                                                    const uint16_t* __restrict__ src_ids,
                                                                     uint32_t* __restrict__ dst,
                                                                     uint32_t* __restrict__ cursor)
 {
@@ -610,8 +613,7 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
     constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
     constexpr uint32_t NONE = 0xFFFFFFFFu;
     static_assert(PART_RANGE == 2 * PART_THREADS, "two range entries per thread");
-    const Bucketer bk = load_bucketer_at(a, sh);
-    uint32_t* hist = sh + (a.buckets - 1) + (NCELLS + 2) / 2;  // [PART_RANGE]: counts, then chunk offsets
+    uint32_t* hist = sh;                                       // [PART_RANGE]: counts, then chunk offsets
     uint32_t* delta = hist + PART_RANGE;                       // [PART_RANGE]: global start - chunk offset
     uint32_t* stage = delta + PART_RANGE;                      // [PER]
     uint16_t* sbkt = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
@@ -630,12 +632,12 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
         for (int j = 0; j < PART_ITEMS; ++j) {
             const uint32_t i = j * PART_THREADS + tid;
             k[j] = i < count ? src[first + i] : 0u;
+            b[j] = i < count ? (uint32_t)src_ids[first + i] : NONE;
         }
-        __syncthreads();  // the previous chunk is done (and the splitters are loaded, s_lo/s_hi reset)
+        __syncthreads();  // the previous chunk is done (and s_lo/s_hi are reset)
         uint32_t lo = NONE, hi = 0;
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) {
-            b[j] = j * PART_THREADS + tid < count ? bk(ordered(k[j], a.kind)) : NONE;
             if (b[j] != NONE) {
                 lo = min(lo, b[j]);
                 hi = max(hi, b[j]);
@@ -704,42 +706,42 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
     }
 }
 
-// First partition level, keys only: every key to its bucket group (its
-// bucket / PART_GROUP, from the same search as the counting pass, so the
-// group regions hold exactly their counted keys). Per chunk of PART_ITEMS x
-// PART_THREADS keys: ranks within each group by shared atomics, the chunk
-// staged in shared memory in group order, one global reservation per group
-// present, then written out run by run with consecutive threads on
-// consecutive addresses. Shared memory: splitters and table, then
-// 2 x groups words, the staged keys and their groups (u16).
+// First partition level, keys only: every key, with its bucket, to its
+// bucket group (bucket / PART_GROUP; the buckets are those the counting pass
+// stored, so the group regions hold exactly their counted keys). Per chunk
+// of PART_ITEMS x PART_THREADS keys: ranks within each group by shared
+// atomics, the chunk staged in shared memory in group order, one global
+// reservation per group present, then written out run by run with
+// consecutive threads on consecutive addresses. Shared memory: 2 x groups
+// words, the staged keys and their buckets (u16).
 __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a, uint32_t groups,
                                                                    uint32_t* __restrict__ dst,
+                                                                   uint16_t* __restrict__ dst_ids,
                                                                    uint32_t* __restrict__ cursor)
 {
     extern __shared__ uint32_t sh[];
     constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
     constexpr uint32_t NONE = 0xFFFFFFFFu;
-    const Bucketer bk = load_bucketer_at(a, sh);
-    uint32_t* hist = sh + (a.buckets - 1) + (NCELLS + 2) / 2;  // [groups]: counts, then chunk offsets
+    uint32_t* hist = sh;                                       // [groups]: counts, then chunk offsets
     uint32_t* delta = hist + groups;                           // [groups]: global start - chunk offset
     uint32_t* stage = delta + groups;                          // [PER]
-    uint16_t* sgrp = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
+    uint16_t* sbkt = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
     __shared__ uint32_t s_warp[PART_THREADS / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t chunks = (a.n + PER - 1) / PER;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
         const uint32_t first = c * PER;
         const uint32_t count = min(PER, a.n - first);
-        uint32_t k[PART_ITEMS], g[PART_ITEMS], r[PART_ITEMS];
+        uint32_t k[PART_ITEMS], bb[PART_ITEMS], g[PART_ITEMS], r[PART_ITEMS];
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) {
             const uint32_t i = j * PART_THREADS + tid;
             k[j] = i < count ? a.keys[first + i] : 0u;
+            bb[j] = i < count ? (uint32_t)a.ids[first + i] : 0u;
         }
-        __syncthreads();  // the previous chunk's write-out is done (and the splitters are loaded)
+        __syncthreads();  // the previous chunk's write-out is done
 #pragma unroll
-        for (int j = 0; j < PART_ITEMS; ++j)
-            g[j] = j * PART_THREADS + tid < count ? bk(ordered(k[j], a.kind)) / PART_GROUP : NONE;
+        for (int j = 0; j < PART_ITEMS; ++j) g[j] = j * PART_THREADS + tid < count ? bb[j] / PART_GROUP : NONE;
         for (uint32_t i = tid; i < groups; i += PART_THREADS) hist[i] = 0;
         __syncthreads();
 #pragma unroll
@@ -764,12 +766,16 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a
             if (g[j] != NONE) {
                 const uint32_t slot = hist[g[j]] + r[j];
                 stage[slot] = k[j];
-                sgrp[slot] = (uint16_t)g[j];
+                sbkt[slot] = (uint16_t)bb[j];
             }
         __syncthreads();
         for (uint32_t i = tid; i < count; i += PART_THREADS) {
-            const uint32_t pos = delta[sgrp[i]] + i;
-            if (pos < a.n) dst[pos] = stage[i];
+            const uint32_t b = sbkt[i];
+            const uint32_t pos = delta[b / PART_GROUP] + i;
+            if (pos < a.n) {
+                dst[pos] = stage[i];
+                dst_ids[pos] = (uint16_t)b;
+            }
         }
     }
 }
@@ -1233,7 +1239,9 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         return;
     }
 
-    PartArgs pa{in, out, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), boff.as<uint32_t>()};
+    temp_buffer ids(ctx.resource, (std::size_t)n * 2);  // every key's bucket (u16: buckets <= 65536)
+    PartArgs pa{in, out, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), boff.as<uint32_t>(),
+                ids.as<uint16_t>()};
     // shared-memory opt-in is per device: set on every call
     check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
                "cudaFuncSetAttribute");
@@ -1249,7 +1257,7 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     {
         // two levels: bucket groups into tmp, then buckets into out
         const uint32_t groups = (buckets + PART_GROUP - 1) / PART_GROUP;
-        temp_buffer tmp(ctx.resource, (std::size_t)n * 4);
+        temp_buffer tmp(ctx.resource, (std::size_t)n * 4), tmp_ids(ctx.resource, (std::size_t)n * 2);
         temp_buffer cur(ctx.resource, ((std::size_t)buckets + groups) * 4);
         uint32_t* bucket_cur = cur.as<uint32_t>();
         uint32_t* group_cur = bucket_cur + buckets;
@@ -1261,15 +1269,16 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
                                             (int)gsmem),
                        "cudaFuncSetAttribute");
             k_partition_groups<<<(int)rows, PART_THREADS, gsmem, ctx.stream>>>(pa, groups, tmp.as<uint32_t>(),
-                                                                               group_cur);
+                                                                               tmp_ids.as<uint16_t>(), group_cur);
         }
         {
             kernel_timer kt(ctx, "learned.partition_buckets");
-            const std::size_t bsmem = bucket_smem_bytes(buckets);
+            const std::size_t bsmem = bucket_smem_bytes();
             check_cuda(cudaFuncSetAttribute(k_partition_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)bsmem),
                        "cudaFuncSetAttribute");
-            k_partition_buckets<<<(int)rows, PART_THREADS, bsmem, ctx.stream>>>(pa, tmp.as<uint32_t>(), out,
+            k_partition_buckets<<<(int)rows, PART_THREADS, bsmem, ctx.stream>>>(pa, tmp.as<uint32_t>(),
+                                                                                tmp_ids.as<uint16_t>(), out,
                                                                                 bucket_cur);
         }
         check_cuda(cudaGetLastError(), "learned partition launch");

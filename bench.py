@@ -639,11 +639,12 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                              steps, warmup, ("learned.", "segsort.", "sort."))
     ok = bool(torch.equal(lout, pout))
     st = stats[-1].as_dict() if stats else {}
-    entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 28 * n, ok, prof_l,
+    entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 36 * n, ok, prof_l,
           {"plain_sort_ms": ms_plain, "plain_sort_gkeys": n / (ms_plain * 1e-3) / 1e9,
            "speedup_vs_plain": ms_plain / ms_learn, "stats": st,
-           "note": "includes sampling, the sample sort and the MLP fit; bytes = 28n (count read, two partition "
-                   "levels, finish; oversized buckets move more)"})
+           "note": "includes sampling, the sample sort and the MLP fit; bytes = 36n: count (key read, u16 bucket "
+                   "write), group level (key + bucket read and write), bucket level (key + bucket read, key "
+                   "write), finish (read + write); oversized buckets move more"})
     del lk, lout, pout
     torch.cuda.empty_cache()
 

@@ -450,15 +450,13 @@ __global__ void k_lut(const uint32_t* __restrict__ sp, uint32_t buckets, const F
 // ---- 5. partition ----------------------------------------------------------
 struct PartArgs {
     const uint32_t* keys;
-    uint32_t* out;
     uint32_t n;
     int kind;
     const Frame* frame;
     const uint32_t* sp;     // buckets - 1 splitters
     const uint16_t* lut;    // NCELLS + 1 entries
     uint32_t buckets;
-    uint32_t* counts;       // [gridDim.x][buckets]: counts, then exclusive column offsets
-    uint32_t* bucket_off;   // [buckets + 1]
+    uint32_t* counts;       // [gridDim.x][buckets]: per-CTA counts
     uint16_t* ids;          // [n]: every key's bucket, written by the counting pass
 };
 
@@ -546,17 +544,14 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_count(PartArgs a)
     for (uint32_t i = threadIdx.x; i < a.buckets; i += PART_THREADS) row[i] = hist[i];
 }
 
-// Column prefix over CTAs (per bucket) and bucket totals; one thread per bucket.
-__global__ void k_columns(uint32_t* counts, uint32_t rows, uint32_t buckets, uint32_t* totals)
+// Bucket totals: the column sums of the per-CTA counts; one thread per bucket.
+__global__ void k_columns(const uint32_t* __restrict__ counts, uint32_t rows, uint32_t buckets,
+                          uint32_t* __restrict__ totals)
 {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= buckets) return;
     uint32_t run = 0;
-    for (uint32_t r = 0; r < rows; ++r) {
-        const uint32_t c = counts[(size_t)r * buckets + b];
-        counts[(size_t)r * buckets + b] = run;
-        run += c;
-    }
+    for (uint32_t r = 0; r < rows; ++r) run += counts[(size_t)r * buckets + b];
     totals[b] = run;
 }
 
@@ -1240,8 +1235,7 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     }
 
     temp_buffer ids(ctx.resource, (std::size_t)n * 2);  // every key's bucket (u16: buckets <= 65536)
-    PartArgs pa{in, out, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), boff.as<uint32_t>(),
-                ids.as<uint16_t>()};
+    PartArgs pa{in, nn, key_kind, frame, sp, lut, buckets, counts.as<uint32_t>(), ids.as<uint16_t>()};
     // shared-memory opt-in is per device: set on every call
     check_cuda(cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem),
                "cudaFuncSetAttribute");

@@ -1,7 +1,7 @@
 // CPU ORACLE — test infrastructure only.
 //
-// This file is the checker for gbcompute's parity tests and the CPU baseline
-// of bench.py. It is never linked into libgbcompute.so and nothing on the
+// This file is the reference oracle for gbcompute's parity tests and the CPU
+// baseline of bench.py. It is never linked into libgbcompute.so and nothing on the
 // product path calls it. Only tests/, __graft_entry__.smoke() and bench.py's
 // CPU-baseline leg load it.
 //

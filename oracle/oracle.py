@@ -2,7 +2,7 @@
 
 ctypes access to oracle/_build/liboracle.so (built from oracle.cpp by
 oracle/Makefile). Used by tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline leg as the checker; never by the product path.
+CPU-baseline leg to check results against; never by the product path.
 """
 from __future__ import annotations
 

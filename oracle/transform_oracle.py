@@ -14,7 +14,7 @@ fmax of a NaN give the other operand. Float arithmetic is numpy's IEEE
 float32 / float64 (round to nearest, no fused multiply-add).
 
 A second, independent implementation of the expression language (its own
-tokenizer, parser and typing) used only by tests/ as the checker. Float
+tokenizer, parser and typing) used only by tests/ to check results. Float
 literals with an f suffix are read through a double (the literals the tests
 use are exact or far from a rounding tie). Raises SyntaxError for malformed
 text and NotImplementedError for constructs outside the supported subset.

@@ -103,6 +103,19 @@ def test_learned_integer_keys_and_small_sizes(ctx, gbc, dtype):
         assert np.array_equal(out, np.sort(keys))
 
 
+def test_learned_constant_and_few_valued_keys(ctx, gbc):
+    # a zero-width key range (every key equal), two values, and 5 values
+    # with one holding most keys: buckets of one key value everywhere
+    i = np.arange(300_001)
+    cases = [np.full(100_000, 7.5, dtype=np.float32),
+             np.where(i % 3 == 0, -1.0, 2.0).astype(np.float32),
+             np.where(i % 10 < 7, 1e3, (i % 10).astype(np.float64)).astype(np.float32)]
+    for keys in cases:
+        out, st = learned(ctx, gbc, keys)
+        assert np.array_equal(out.view(np.uint32), plain_sort(ctx, gbc, keys).view(np.uint32))
+        assert st.violation == 0
+
+
 def test_bad_network_falls_back_to_plain_sort(ctx, gbc):
     # Every weight ~ 0: the network's CDF is flat, every splitter lands past
     # the largest sampled key and all keys would share one bucket; the sample

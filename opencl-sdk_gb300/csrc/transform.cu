@@ -180,6 +180,27 @@ private:
     const char* who_;
     std::vector<token> toks_;
     std::size_t at_ = 0;
+    // Bounds on the recursion of the parser, the code generator and the
+    // tree's destructor, so that hostile text is refused, not a stack
+    // overflow: nesting levels (parentheses, prefix operators, casts,
+    // ternaries, call arguments) and nodes created. A program has at most
+    // MAX_OPS operations, far fewer than MAX_NODES nodes.
+    static constexpr int MAX_NEST = 128;
+    static constexpr std::size_t MAX_NODES = 256;
+    int nest_ = 0;
+    std::size_t nodes_ = 0;
+
+    struct nest_guard {
+        compiler& c;
+        explicit nest_guard(compiler& cc) : c(cc)
+        {
+            if (++c.nest_ > MAX_NEST)
+                c.fail_unsupported("an expression nested deeper than " + std::to_string(MAX_NEST) + " levels");
+        }
+        ~nest_guard() { --c.nest_; }
+        nest_guard(const nest_guard&) = delete;
+        nest_guard& operator=(const nest_guard&) = delete;
+    };
     program prog_;
 
     [[noreturn]] void fail_build(std::size_t pos, const std::string& what) const
@@ -281,14 +302,15 @@ private:
     }
 
     // ---- node builders ----
-    static node_ptr make(node_kind k, elem t)
+    node_ptr make(node_kind k, elem t)
     {
+        if (++nodes_ > MAX_NODES) fail_unsupported("an expression longer than " + std::to_string(MAX_OPS) + " operations");
         node_ptr n(new node);
         n->k = k;
         n->t = t;
         return n;
     }
-    static node_ptr literal(elem t, uint64_t bits)
+    node_ptr literal(elem t, uint64_t bits)
     {
         node_ptr n = make(N_LIT, t);
         n->bits = bits;
@@ -310,6 +332,7 @@ private:
 
     node_ptr conditional()
     {
+        const nest_guard guard(*this);
         node_ptr c = binary(0);
         if (!is("?")) return c;
         ++at_;
@@ -445,6 +468,7 @@ private:
 
     node_ptr unary()
     {
+        const nest_guard guard(*this);
         const token t = peek();
         if (is("+") || is("-") || is("~") || is("!")) {
             ++at_;

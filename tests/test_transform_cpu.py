@@ -125,3 +125,40 @@ def test_compiler_unsupported(gbc, expr):
 def test_oracle_agrees_on_build_errors(expr):
     with pytest.raises(SyntaxError):
         T.transform(expr, np.arange(4, dtype=np.int32), np.int32)
+
+
+HOSTILE = {
+    "parentheses": lambda k: "(" * k + "x" + ")" * k,
+    "prefix_operators": lambda k: "!" * k + "x",
+    "casts": lambda k: "(int)" * k + "x",
+    "ternaries": lambda k: "x ? " * k + "x" + " : x" * k,
+    "operator_chain": lambda k: "x" + " + x" * k,
+    "call_arguments": lambda k: "min(" * k + "x" + ", 1)" * k,
+}
+
+
+@pytest.mark.parametrize("form", sorted(HOSTILE))
+def test_compiler_refuses_hostile_nesting(form):
+    # 100,000 levels must come back as an error status, not a stack
+    # overflow of the caller's process: run in a child process so that a
+    # crash fails this test instead of the test run.
+    import os
+    import subprocess
+    import sys
+
+    text = HOSTILE[form](100_000)
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = (
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {os.path.join(os.path.dirname(here), 'opencl-sdk_gb300')!r})\n"
+        "import gbcompute as gbc\n"
+        "text = sys.stdin.read()\n"
+        "try:\n"
+        "    gbc.transform_compile(text, np.int32, np.int32)\n"
+        "    print('compiled')\n"
+        "except (gbc.UnsupportedError, gbc.BuildError) as e:\n"
+        "    print(type(e).__name__)\n"
+    )
+    r = subprocess.run([sys.executable, "-c", code], input=text, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stderr[-500:])
+    assert r.stdout.strip() in ("UnsupportedError", "BuildError"), r.stdout

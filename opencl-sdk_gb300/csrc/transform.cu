@@ -856,6 +856,10 @@ private:
     }
 
     // acc = a OP b, both converted to t
+    // min / max of floating-point values keep their operand order: with a +0
+    // and a -0 the first operand wins (OpenCL C max: y if x < y, otherwise x)
+    static bool ordered_minmax(uint8_t kind, ty t) { return (kind == K_MIN || kind == K_MAX) && (t == F32 || t == F64); }
+
     void gen_binary(uint8_t kind, ty t, const node& a, const node& b, int sp)
     {
         uint8_t src;
@@ -863,6 +867,13 @@ private:
         if (leaf(b, t, src, imm)) {
             gen_as(a, t, sp);
             push_leaf_op(kind, t, src, imm);
+        } else if (ordered_minmax(kind, t)) {
+            // b into a slot first, then acc = a OP slot
+            gen_as(b, t, sp);
+            need_slots(sp, 1);
+            push_op(K_PUSH, t, S_ACC, 0, (uint8_t)sp);
+            gen_as(a, t, sp + 1);
+            push_op(kind, t, S_POP, 0, (uint8_t)sp);
         } else if (leaf(a, t, src, imm)) {
             gen_as(b, t, sp);
             push_op(reversed(kind), t, src, imm);
@@ -940,10 +951,21 @@ private:
             return;
         }
         case N_MINMAX: gen_binary((uint8_t)e.op, arith(e.opt), *e.a, *e.b, sp); return;
-        case N_CLAMP: {
+        case N_CLAMP: {  // min(max(a, b), c)
             const ty t = arith(e.opt);
-            gen_binary(K_MAX, t, *e.a, *e.b, sp);
-            gen_rhs(K_MIN, t, *e.c, sp);
+            uint8_t src;
+            uint64_t imm;
+            if (ordered_minmax(K_MIN, t) && !leaf(*e.c, t, src, imm)) {
+                // the upper bound into a slot first, so that min keeps its order
+                gen_as(*e.c, t, sp);
+                need_slots(sp, 1);
+                push_op(K_PUSH, t, S_ACC, 0, (uint8_t)sp);
+                gen_binary(K_MAX, t, *e.a, *e.b, sp + 1);
+                push_op(K_MIN, t, S_POP, 0, (uint8_t)sp);
+            } else {
+                gen_binary(K_MAX, t, *e.a, *e.b, sp);
+                gen_rhs(K_MIN, t, *e.c, sp);
+            }
             if (is_narrow(e.t)) convert_to(I32, e.t);
             return;
         }

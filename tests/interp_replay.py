@@ -227,8 +227,9 @@ BINOPS = ["+", "-", "*", "/", "%", "&", "|", "^", "<<", ">>", "<", ">", "<=", ">
 
 def random_expression(rng, depth: int, has_y: bool) -> str:
     """A random expression over x (and y) with literals of every kind,
-    binary and unary operators, casts, ternaries and min/max/clamp/abs/fabs/
-    fmin/fmax calls (not all well typed: some must be refused)."""
+    binary and unary operators, casts, ternaries, as_T / convert_T and
+    min/max/clamp/abs/fabs/fmin/fmax calls (not all well typed: some must be
+    refused)."""
     def gen(d):
         if d <= 0 or rng.random() < 0.25:
             return rng.choice(["x", "y"] if has_y else ["x"]) if rng.random() < 0.6 else rng.choice(LITERALS)
@@ -241,6 +242,8 @@ def random_expression(rng, depth: int, has_y: bool) -> str:
             return f"({rng.choice(CASTS)})({gen(d - 1)})"
         if r < 0.72:
             return f"({gen(d - 1)} ? {gen(d - 1)} : {gen(d - 1)})"
+        if r < 0.78:
+            return f"{rng.choice(['as_', 'convert_'])}{rng.choice(CASTS)}({gen(d - 1)})"
         f = rng.choice(["min", "max", "abs", "fabs", "fmin", "fmax", "clamp"])
         if f in ("abs", "fabs"):
             return f"{f}({gen(d - 1)})"

@@ -165,47 +165,24 @@ def test_compiler_refuses_hostile_nesting(form):
 
 
 def test_compiler_and_oracle_agree_on_generated_expressions(gbc):
-    # Seeded random expressions of the subset (literals of every kind,
-    # binary/unary operators, casts, ternaries, min/max/clamp/abs/fabs/fmin/
-    # fmax) over random element types: the library's compiler and the
-    # oracle's independent parser must accept and reject the same texts
-    # (the compiler may also refuse programs beyond its 48 operations or 4
-    # temporaries as UNSUPPORTED).
+    # Seeded random expressions of the subset (interp_replay.random_expression)
+    # over random element types: the library's compiler and the oracle's
+    # independent parser must accept and reject the same texts (the compiler
+    # may also refuse programs beyond its 48 operations or 4 temporaries as
+    # UNSUPPORTED).
     import random
+
+    import interp_replay as R
 
     rng = random.Random(2024)
     types = [np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64, np.uint64, np.float32,
              np.float64]
-    casts = ["char", "uchar", "short", "ushort", "int", "uint", "long", "ulong", "float", "double"]
-    lits = ["0", "1", "3", "7u", "255", "1000000", "3000000000", "5L", "2ul", "0x7f", "0xffffffffu", "1.5f", "0.5",
-            "2.0f", "-1", "INT_MAX", "UINT_MAX", "FLT_MAX", "NAN", "INFINITY"]
-    binops = ["+", "-", "*", "/", "%", "&", "|", "^", "<<", ">>", "<", ">", "<=", ">=", "==", "!=", "&&", "||"]
-
-    def gen(d, has_y):
-        if d <= 0 or rng.random() < 0.25:
-            return rng.choice(["x", "y"] if has_y else ["x"]) if rng.random() < 0.6 else rng.choice(lits)
-        r = rng.random()
-        if r < 0.45:
-            return f"({gen(d - 1, has_y)} {rng.choice(binops)} {gen(d - 1, has_y)})"
-        if r < 0.55:
-            return rng.choice(["-", "~", "!", "+"]) + f"({gen(d - 1, has_y)})"
-        if r < 0.65:
-            return f"({rng.choice(casts)})({gen(d - 1, has_y)})"
-        if r < 0.72:
-            return f"({gen(d - 1, has_y)} ? {gen(d - 1, has_y)} : {gen(d - 1, has_y)})"
-        f = rng.choice(["min", "max", "abs", "fabs", "fmin", "fmax", "clamp"])
-        if f in ("abs", "fabs"):
-            return f"{f}({gen(d - 1, has_y)})"
-        if f == "clamp":
-            return f"clamp({gen(d - 1, has_y)}, {gen(d - 1, has_y)}, {gen(d - 1, has_y)})"
-        return f"{f}({gen(d - 1, has_y)}, {gen(d - 1, has_y)})"
-
     seen = {"ok": 0, "build": 0}
     for _ in range(20000):
         has_y = rng.random() < 0.5
         tx, to = rng.choice(types), rng.choice(types)
         ty = rng.choice(types) if has_y else None
-        expr = gen(rng.randint(1, 5), has_y)
+        expr = R.random_expression(rng, rng.randint(1, 5), has_y)
         try:
             gbc.transform_compile(expr, tx, to, ty)
             lib = "ok"

@@ -145,6 +145,10 @@ public:
     compiler(const std::string& text, elem tx, bool has_y, elem ty2, const char* who)
         : text_(text), tx_(tx), has_y_(has_y), ty_(ty2), who_(who)
     {
+        // bounds the token list before lexing; a program of MAX_OPS
+        // operations needs far less text
+        if (text.size() > MAX_TEXT)
+            fail_unsupported("an expression text longer than " + std::to_string(MAX_TEXT) + " characters");
         lex();
     }
 
@@ -187,6 +191,7 @@ private:
     // MAX_OPS operations, far fewer than MAX_NODES nodes.
     static constexpr int MAX_NEST = 128;
     static constexpr std::size_t MAX_NODES = 256;
+    static constexpr std::size_t MAX_TEXT = 65536;
     int nest_ = 0;
     std::size_t nodes_ = 0;
 
@@ -203,14 +208,17 @@ private:
     };
     program prog_;
 
+    // the expression as quoted in messages: at most 200 characters
+    std::string quoted() const { return text_.size() <= 200 ? text_ : text_.substr(0, 200) + "..."; }
+
     [[noreturn]] void fail_build(std::size_t pos, const std::string& what) const
     {
         throw build_error(std::string(who_) + ": build log: error at column " + std::to_string(pos + 1) + ": " + what +
-                          " in \"" + text_ + "\"");
+                          " in \"" + quoted() + "\"");
     }
     [[noreturn]] void fail_unsupported(const std::string& what) const
     {
-        throw unsupported_error(std::string(who_) + ": " + what + " in \"" + text_ +
+        throw unsupported_error(std::string(who_) + ": " + what + " in \"" + quoted() +
                                 "\" is outside the supported expression subset");
     }
 

@@ -198,3 +198,16 @@ def test_compiler_and_oracle_agree_on_generated_expressions(gbc):
         assert lib == orc, (expr, np.dtype(tx).name, np.dtype(ty).name if ty else None, np.dtype(to).name)
         seen[lib] += 1
     assert seen["ok"] > 8000 and seen["build"] > 4000
+
+
+def test_compiler_refuses_oversized_text_quickly(gbc):
+    # 10 MB of text is refused before lexing, and the message quotes only
+    # the start of it
+    import time
+
+    text = "x+" * 5_000_000 + "x"
+    t0 = time.perf_counter()
+    with pytest.raises(gbc.UnsupportedError) as e:
+        gbc.transform_compile(text, np.int32, np.int32)
+    assert time.perf_counter() - t0 < 2.0
+    assert len(str(e.value)) < 1000

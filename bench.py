@@ -15,7 +15,8 @@ clc_buffer_write -> clc_sort -> clc_buffer_read from pinned host memory
 (double-buffered over two contexts and two host threads, with the one-step-
 at-a-time figure beside it), the
 CPU baseline (the oracle's restatement of the reference's 4-bit LSD sort on
-all host cores, on a bounded sample), SM clocks sampled during the run, and
+all host cores, on the same 2^28 pairs, with std::stable_sort on one thread
+beside it), SM clocks sampled during the run, and
 the other configuration workloads measured the same way under "workloads".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -37,7 +38,7 @@ sys.path.insert(0, PKG)
 
 METRIC = "sort Gkeys/s & % HBM roofline: batched / learned-CDF vs plain LSD, bit-exact"
 N_MAIN = 1 << 28
-CPU_SAMPLE = 1 << 24
+STD_FLOOR_N = 1 << 24
 
 
 def load_peak_gbs() -> tuple[float, str]:
@@ -149,68 +150,108 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 def cpu_reference_sample(n: int, seed: int = 1):
+    """n uniform uint32 keys (the headline workload's distribution) and their
+    indices as values."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
-    keys = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    keys = rng.integers(0, 2**32, size=n, dtype=np.uint32)
     vals = np.arange(n, dtype=np.uint32)
     return keys, vals
 
 
-def time_cpu_reference(steps: int, warmup: int, n: int) -> dict:
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+class CpuSort:
+    """The reference's sort algorithm on the host: the oracle's C++
+    restatement of its 4-bit LSD (8 passes over 128 x 8 key tiles, digit-major
+    count table, exclusive scan, stable scatter) on every host thread, and
+    std::stable_sort on one thread as the floor. Each timed call sorts fresh
+    copies of the same pairs; the copies are made outside the timing."""
 
-    oracle.build()
-    threads = oracle.hardware_threads()
-    keys, vals = cpu_reference_sample(n)
-    for _ in range(warmup):
-        oracle.ref_radix_sort(keys, vals, threads=threads)
-    times = []
-    for _ in range(steps):
+    def __init__(self, n: int):
+        import numpy as np
+
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        self.oracle = oracle
+        self.np = np
+        self.threads = oracle.hardware_threads()
+        self.keys, self.vals = cpu_reference_sample(n)
+        self.work_k = np.empty_like(self.keys)
+        self.work_v = np.empty_like(self.vals)
+
+    def time_lsd(self) -> float:
+        self.np.copyto(self.work_k, self.keys)
+        self.np.copyto(self.work_v, self.vals)
         t0 = time.perf_counter()
-        oracle.ref_radix_sort(keys, vals, threads=threads)
-        times.append(time.perf_counter() - t0)
-    return {"threads": threads, "times": times, "n": n}
+        self.oracle.ref_radix_sort_inplace(self.work_k, self.work_v, threads=self.threads)
+        return time.perf_counter() - t0
+
+    def check(self) -> bool:
+        """The last sort's output is sorted and pairs every key with its index."""
+        np = self.np
+        k, v = self.work_k, self.work_v
+        return bool(np.all(k[1:] >= k[:-1])) and bool(np.array_equal(self.keys[v], k))
+
+    def std_floor(self, n: int) -> dict:
+        """std::stable_sort of the first n pairs on one thread (median of 3)."""
+        times = []
+        for _ in range(3):
+            k, v = self.keys[:n].copy(), self.vals[:n].copy()
+            t0 = time.perf_counter()
+            self.oracle.std_sort_inplace(k, v)
+            times.append(time.perf_counter() - t0)
+        t = statistics.median(times)
+        return {"value": n / t / 1e9, "unit": "Gkeys/s", "cores": 1, "n": n, "ms": t * 1e3,
+                "what": f"std::stable_sort of {n} (key, index) pairs on one host thread, median of 3"}
 
 
-def cpu_baseline_block(seconds: float = 10.0) -> dict:
-    """Times the oracle's restated reference sort for about `seconds`."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-
-    oracle.build()
-    threads = oracle.hardware_threads()
-    keys, vals = cpu_reference_sample(CPU_SAMPLE)
-    oracle.ref_radix_sort(keys, vals, threads=threads)  # warm
+def cpu_baseline_block(seconds: float = 12.0) -> dict:
+    """The restated reference sort of the headline's own 2^28 pairs on all
+    host threads, repeated for about `seconds` (median), plus the std:: floor
+    on a 2^24 sample."""
+    cs = CpuSort(N_MAIN)
+    cs.time_lsd()  # warm
     times, t_end = [], time.perf_counter() + seconds
-    while time.perf_counter() < t_end or len(times) < 2:
-        t0 = time.perf_counter()
-        oracle.ref_radix_sort(keys, vals, threads=threads)
-        times.append(time.perf_counter() - t0)
+    while time.perf_counter() < t_end or len(times) < 3:
+        times.append(cs.time_lsd())
+    ok = cs.check()
     t = statistics.median(times)
-    return {"value": CPU_SAMPLE / t / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
-            "sample": f"2^24 uniform uint32 key/value pairs (same distribution as the 2^28 workload), "
-                      f"median of {len(times)} runs of the restated reference 4-bit LSD sort "
-                      f"(8 passes, 128x8 tiles) on {threads} host threads"}
+    return {"value": N_MAIN / t / 1e9, "unit": "Gkeys/s", "cores": cs.threads, "kind": "port",
+            "ms_per_sort": t * 1e3, "checked": ok,
+            "sample": f"the full 2^28 uniform uint32 key/index workload, median of {len(times)} sorts by the "
+                      f"oracle's restatement of the reference's 4-bit LSD (8 passes, 128x8 tiles) on "
+                      f"{cs.threads} host threads",
+            "std_floor": cs.std_floor(STD_FLOOR_N)}
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference's sort algorithm on the host cores,
+    on the headline workload itself (2^28 uniform uint32 keys with their
+    indices as values, out of place), every step one whole sort."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    r = time_cpu_reference(args.steps, args.warmup, CPU_SAMPLE)
-    t = statistics.median(r["times"])
-    value = r["n"] / t / 1e9
+    cs = CpuSort(N_MAIN)
+    for _ in range(args.warmup):
+        cs.time_lsd()
+    times = [cs.time_lsd() for _ in range(args.steps)]
+    ok = cs.check()
+    t = statistics.median(times)
+    value = N_MAIN / t / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "kv_sort_u32_uniform", "n_per_step": r["n"], "key": "u32", "value": "u32"},
-        "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": r["threads"], "kind": "port",
-                         "sample": f"2^24 pairs per step (bounded sample of the 2^28 workload); the reference "
-                                   f"Compute library needs an OpenCL runtime, absent here, so its algorithm "
-                                   f"runs as the oracle's C++ restatement"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic: seeded uniform uint32 keys, "
+                                                                       "uint32 values = index",
+        "config": {"workload": "kv_sort_u32_uniform_n2^28", "n": N_MAIN, "key": "u32", "value": "u32 (index)"},
+        "bitexact": ok,
+        "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": cs.threads, "kind": "port",
+                         "sample": f"the full 2^28-pair workload every step (median of {args.steps}); the reference "
+                                   f"Compute library needs an OpenCL runtime, which neither machine has, so its "
+                                   f"algorithm runs as the oracle's C++ restatement on {cs.threads} host threads",
+                         "std_floor": cs.std_floor(STD_FLOOR_N)},
         "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

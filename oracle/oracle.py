@@ -112,6 +112,21 @@ def ref_radix_sort(keys: np.ndarray, values: np.ndarray | None = None, descendin
     return k, v
 
 
+def ref_radix_sort_inplace(keys: np.ndarray, values: np.ndarray | None = None, threads: int = 0) -> None:
+    """The restated reference sort on the caller's own (contiguous) arrays,
+    ascending: no copies, so a caller can time the sort alone."""
+    assert keys.flags.c_contiguous and (values is None or (values.flags.c_contiguous and values.dtype == np.uint32))
+    lib().orc_ref_radix_sort(_p(keys), None if values is None else _p(values), keys.size, keys.dtype.itemsize,
+                             key_kind(keys.dtype), 0, threads)
+
+
+def std_sort_inplace(keys: np.ndarray, values: np.ndarray | None = None) -> None:
+    """std::stable_sort (one thread) on the caller's own arrays, ascending."""
+    assert keys.flags.c_contiguous and (values is None or (values.flags.c_contiguous and values.dtype == np.uint32))
+    lib().orc_std_sort(_p(keys), None if values is None else _p(values), keys.size, keys.dtype.itemsize,
+                       key_kind(keys.dtype), 0)
+
+
 def _ident(dtype, identity) -> np.ndarray:
     return np.array([identity], dtype=dtype)
 

@@ -329,15 +329,16 @@ GBC_EXPORT clc_status clc_buffer_wrap(clc_context ctx, void* device_pointer, siz
                                       clc_buffer* out);
 /* The context's CUDA stream (a cudaStream_t). */
 GBC_EXPORT void* clc_context_stream(clc_context ctx);
-/* Memory statistics of the context's resource (current/peak/total bytes,
- * current/total allocations) and the pool's cached bytes. */
+/* Memory statistics of the context's arena: bytes and allocations live,
+ * their peak and totals (of the sizes asked for), and cached_bytes, the
+ * device memory the arena holds idle for reuse. */
 typedef struct clc_memory_stats {
     size_t current_bytes, peak_bytes, total_bytes;
     size_t current_allocations, total_allocations;
     size_t cached_bytes;
 } clc_memory_stats;
 GBC_EXPORT clc_status clc_context_memory_stats(clc_context ctx, clc_memory_stats* out);
-/* Returns the pool's cached blocks to the device. */
+/* Hands every idle slab of the context's arena back to the device. */
 GBC_EXPORT clc_status clc_context_release_cache(clc_context ctx);
 
 /* Raw-pointer forms: the same algorithms on device pointers, asynchronous on
@@ -376,9 +377,28 @@ GBC_EXPORT clc_status clc_reduce_raw(clc_context ctx, const void* in, size_t n, 
  * before any stream capture. Every call shares the one array and clears the
  * part it uses before its kernel runs, so calls whose work may overlap on the
  * GPU (other streams, other host threads) race and must be serialised by the
- * caller. */
+ * caller. The stream, in and out must belong to the current device
+ * (CLC_ERROR_INVALID_ARGUMENT otherwise).
+ *
+ * The scan's look-back waits are bounded (about one second). A wait that runs
+ * out sets an error word in the same array and leaves that call's output
+ * incomplete; since the call has returned by then, ask
+ * clc_scan_i32_noalloc_status afterwards. */
 GBC_EXPORT clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size_t n, int exclusive,
                                            void* stream);
+
+/* Companion of clc_scan_i32_noalloc, allocating nothing either: waits for
+ * `stream`, then returns CLC_ERROR_OPENCL if any clc_scan_i32_noalloc call on
+ * the current device had a look-back wait run out since the last status
+ * query (and clears that error word), CLC_SUCCESS otherwise. */
+GBC_EXPORT clc_status clc_scan_i32_noalloc_status(void* stream);
+
+/* Failure-path self-test of the allocation-free scan: scans buf (2 to 16,384
+ * tiles of 16,384 int32, device memory of the current device) with its first
+ * tile never run, so the next tile's bounded wait gives up after about one
+ * second and sets the error word; clc_scan_i32_noalloc_status then reports
+ * it. buf's contents are overwritten. */
+GBC_EXPORT clc_status clc_selftest_noalloc_timeout(int32_t* buf, size_t n, void* stream);
 
 /* Failure-path self-test: runs one scan tile whose predecessor never
  * publishes its status, so the tile's bounded look-back wait gives up after

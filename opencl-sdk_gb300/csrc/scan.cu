@@ -497,16 +497,22 @@ void scan(device_context& ctx, const void* in, void* out, std::size_t n, elem t,
 // not call cudaMalloc behind that allocator's back, and cudaFree synchronises
 // the whole device, which a latency-bound caller cannot afford. This entry
 // point therefore keeps its scratch -- the look-back status word of every
-// tile and the tile counter -- in a fixed array compiled into the library, and
-// it needs no clc_context (creating one allocates). The caller passes the
-// input, the output and the stream.
+// tile, the tile counter and an error word -- in a fixed array compiled into
+// the library, and it needs no clc_context (creating one allocates). The
+// caller passes the input, the output and the stream.
 //
 // The array holds 16,384 tiles of 16,384 elements (the int32 tile shape of
 // the pooled scan): at most 2^28 elements per call (128 KiB of status words,
-// held by every GPU that loads the library until the process exits). Every call shares it and it keeps the last call's
-// contents, so each call first clears the words it will read; calls whose
-// work overlaps on the GPU (different streams, or different host threads)
-// race on it and must be serialised by the caller.
+// held by every GPU that loads the library until the process exits). Every
+// call shares it and it keeps the last call's contents, so each call first
+// clears the words it will read; calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on it and must be
+// serialised by the caller.
+//
+// A look-back wait that runs out (about one second: only a GPU that stalls a
+// predecessor tile that long) makes the kernel skip the writes that depend on
+// it and set the error word; the call has already returned by then, so
+// clc_scan_i32_noalloc_status reports it (and clears it) afterwards.
 // ---------------------------------------------------------------------------
 namespace noalloc {
 
@@ -515,7 +521,10 @@ constexpr uint32_t TILE = ScanShape<int32_t, ROWS>::TILE;
 constexpr std::size_t MAX_ELEMENTS = std::size_t(1) << 28;
 constexpr uint32_t MAX_TILES = (uint32_t)(MAX_ELEMENTS / TILE);
 
-// [0, MAX_TILES): status word of each tile; [MAX_TILES]: the tile counter.
+// [0, MAX_TILES): status word of each tile; [MAX_TILES]: the tile counter;
+// [MAX_TILES + 1]: the error word (an int in its low half, sticky until
+// clc_scan_i32_noalloc_status clears it).
+constexpr uint32_t CTR_WORD = MAX_TILES, ERR_WORD = MAX_TILES + 1;
 static __device__ __align__(256) uint64_t scan_scratch[MAX_TILES + 32];
 
 struct device_setup {
@@ -547,6 +556,77 @@ device_setup setup_current_device(int dev)
     return s;
 }
 
+
+// Argument checks shared by the entry points below: the stream and any
+// device-memory pointer must belong to the current device, whose scratch
+// array and grid size the call uses.
+int check_device(void* stream, const void* const* ptrs, int count, std::string& why)
+{
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    int sdev = dev;
+    if (stream != nullptr) check_cuda(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev), "cudaStreamGetDevice");
+    if (sdev != dev) {
+        why = "the stream belongs to device " + std::to_string(sdev) + ", not the current device " + std::to_string(dev);
+        return -1;
+    }
+    for (int i = 0; i < count; ++i) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, ptrs[i]) != cudaSuccess) {
+            (void)cudaGetLastError();
+            continue;  // not memory the runtime knows: the caller's responsibility
+        }
+        if (pa.type == cudaMemoryTypeDevice && pa.device != dev) {
+            why = "a pointer is device memory of device " + std::to_string(pa.device) + ", not the current device " +
+                  std::to_string(dev);
+            return -1;
+        }
+    }
+    return dev;
+}
+
+void launch(const device_setup& s, const int32_t* in, int32_t* out, std::size_t n, bool exclusive, cudaStream_t st,
+            uint32_t first_tile)
+{
+    const uint32_t num_tiles = (uint32_t)((n + TILE - 1) / TILE);
+    // Clear what this call reads before it is written: the tile counter
+    // and the status words of its tiles (an earlier call left its own).
+    // The error word is left alone: it stays set until it is read.
+    check_cuda(cudaMemsetAsync(s.scratch, 0, (std::size_t)num_tiles * sizeof(uint64_t), st), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(s.scratch + CTR_WORD, 0, sizeof(uint64_t), st), "cudaMemsetAsync");
+    if (first_tile != 0)
+        check_cuda(cudaMemsetAsync(s.scratch + CTR_WORD, (int)first_tile, 1, st), "cudaMemsetAsync");
+    ScanArgs<int32_t> a;
+    a.in = in;
+    a.out = out;
+    a.n = (uint32_t)n;
+    a.identity = 0;
+    a.exclusive = exclusive ? 1 : 0;
+    a.aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+    a.num_tiles = num_tiles;
+    a.ring = s.scratch;  // tile t uses word t (sequence numbers start at 0)
+    a.seq0 = 0;
+    a.tile_ctr = reinterpret_cast<uint32_t*>(s.scratch + CTR_WORD);
+    a.wide_sum = nullptr;
+    a.total = nullptr;
+    a.err = reinterpret_cast<int*>(s.scratch + ERR_WORD);
+    const uint32_t tiles_left = num_tiles - std::min(first_tile, num_tiles);
+    const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>(tiles_left, (uint32_t)s.grid_cap));
+    k_scan<int32_t, ops::Plus, false, ROWS, MINB, PREFETCH_GRIDS><<<grid, THREADS, 0, st>>>(a);
+    check_cuda(cudaGetLastError(), "clc_scan_i32_noalloc launch");
+}
+
+template <typename F> clc_status guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const device_error& e) {
+        return (clc_status)set_last_error(CLC_ERROR_OPENCL, e.what(), e.code);
+    } catch (const std::exception& e) {
+        return (clc_status)set_last_error(CLC_ERROR_INTERNAL, e.what(), 0);
+    }
+}
+
 }  // namespace noalloc
 
 }  // namespace gbc
@@ -554,7 +634,7 @@ device_setup setup_current_device(int dev)
 extern "C" clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size_t n, int exclusive, void* stream)
 {
     using namespace gbc;
-    try {
+    return noalloc::guarded([&]() -> clc_status {
         if (n == 0) return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
         if (n > noalloc::MAX_ELEMENTS)
             return (clc_status)set_last_error(
@@ -565,36 +645,61 @@ extern "C" clc_status clc_scan_i32_noalloc(const int32_t* in, int32_t* out, size
                 0);
         if (in == nullptr || out == nullptr)
             return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT, "clc_scan_i32_noalloc: null pointer", 0);
-        int dev = 0;
-        check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+        std::string why;
+        const void* ptrs[2] = {in, out};
+        const int dev = noalloc::check_device(stream, ptrs, 2, why);
+        if (dev < 0)
+            return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT, ("clc_scan_i32_noalloc: " + why).c_str(), 0);
+        const noalloc::device_setup s = noalloc::setup_current_device(dev);
+        noalloc::launch(s, in, out, n, exclusive != 0, static_cast<cudaStream_t>(stream), 0);
+        return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
+    });
+}
+
+extern "C" clc_status clc_scan_i32_noalloc_status(void* stream)
+{
+    using namespace gbc;
+    return noalloc::guarded([&]() -> clc_status {
+        std::string why;
+        const int dev = noalloc::check_device(stream, nullptr, 0, why);
+        if (dev < 0)
+            return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT,
+                                              ("clc_scan_i32_noalloc_status: " + why).c_str(), 0);
         const noalloc::device_setup s = noalloc::setup_current_device(dev);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        const uint32_t num_tiles = (uint32_t)((n + noalloc::TILE - 1) / noalloc::TILE);
-        // Clear what this call reads before it is written: the tile counter
-        // and the status words of its tiles (an earlier call left its own).
-        check_cuda(cudaMemsetAsync(s.scratch, 0, (std::size_t)num_tiles * sizeof(uint64_t), st), "cudaMemsetAsync");
-        check_cuda(cudaMemsetAsync(s.scratch + noalloc::MAX_TILES, 0, sizeof(uint64_t), st), "cudaMemsetAsync");
-        ScanArgs<int32_t> a;
-        a.in = in;
-        a.out = out;
-        a.n = (uint32_t)n;
-        a.identity = 0;
-        a.exclusive = exclusive ? 1 : 0;
-        a.aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
-        a.num_tiles = num_tiles;
-        a.ring = s.scratch;  // tile t uses word t (sequence numbers start at 0)
-        a.seq0 = 0;
-        a.tile_ctr = reinterpret_cast<uint32_t*>(s.scratch + noalloc::MAX_TILES);
-        a.wide_sum = nullptr;
-        a.total = nullptr;
-        a.err = nullptr;  // a wait that runs out ends the kernel; there is no context to report to
-        const int grid = (int)std::min<uint32_t>(num_tiles, (uint32_t)s.grid_cap);
-        k_scan<int32_t, ops::Plus, false, noalloc::ROWS, noalloc::MINB, PREFETCH_GRIDS><<<grid, THREADS, 0, st>>>(a);
-        check_cuda(cudaGetLastError(), "clc_scan_i32_noalloc launch");
+        int word = 0;  // pageable destination: the copy completes before it returns
+        check_cuda(cudaMemcpyAsync(&word, s.scratch + noalloc::ERR_WORD, sizeof(int), cudaMemcpyDeviceToHost, st),
+                   "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        if (word == 0) return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
+        check_cuda(cudaMemsetAsync(s.scratch + noalloc::ERR_WORD, 0, sizeof(uint64_t), st), "cudaMemsetAsync");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        return (clc_status)set_last_error(CLC_ERROR_OPENCL,
+                                          "clc_scan_i32_noalloc: a look-back wait timed out; the output of an "
+                                          "earlier call on this device is incomplete",
+                                          0);
+    });
+}
+
+extern "C" clc_status clc_selftest_noalloc_timeout(int32_t* buf, size_t n, void* stream)
+{
+    using namespace gbc;
+    return noalloc::guarded([&]() -> clc_status {
+        // Two or more tiles scanned with the tile counter starting at 1: tile
+        // 0 never runs, so tile 1's bounded wait must give up and set the
+        // error word. Every access stays inside the caller's n elements.
+        if (buf == nullptr || n < 2 * (std::size_t)noalloc::TILE || n > noalloc::MAX_ELEMENTS)
+            return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT,
+                                              "clc_selftest_noalloc_timeout: needs 2 to 16384 tiles of 16384 int32",
+                                              0);
+        std::string why;
+        const void* ptrs[1] = {buf};
+        const int dev = noalloc::check_device(stream, ptrs, 1, why);
+        if (dev < 0)
+            return (clc_status)set_last_error(CLC_ERROR_INVALID_ARGUMENT,
+                                              ("clc_selftest_noalloc_timeout: " + why).c_str(), 0);
+        const noalloc::device_setup s = noalloc::setup_current_device(dev);
+        noalloc::launch(s, buf, buf, n, false, static_cast<cudaStream_t>(stream), 1);
         return (clc_status)set_last_error(CLC_SUCCESS, "", 0);
-    } catch (const device_error& e) {
-        return (clc_status)set_last_error(CLC_ERROR_OPENCL, e.what(), e.code);
-    } catch (const std::exception& e) {
-        return (clc_status)set_last_error(CLC_ERROR_INTERNAL, e.what(), 0);
-    }
+    });
 }

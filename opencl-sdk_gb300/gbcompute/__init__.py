@@ -200,6 +200,8 @@ _PROTOS = {
     "clc_histogram_even_raw": (_i, [_vp, _vp, _sz, _i, _vp, _sz, C.c_double, C.c_double]),
     "clc_reduce_raw": (_i, [_vp, _vp, _sz, _i, _cp, _cp, _vp, _vp]),
     "clc_scan_i32_noalloc": (_i, [_vp, _vp, _sz, _i, _vp]),
+    "clc_scan_i32_noalloc_status": (_i, [_vp]),
+    "clc_selftest_noalloc_timeout": (_i, [_vp, _sz, _vp]),
     "clc_selftest_lookback_timeout": (_i, [_vp]),
     "clc_profile_enable": (_i, [_vp, _i]),
     "clc_profile_reset": (_i, [_vp]),

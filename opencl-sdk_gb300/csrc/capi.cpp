@@ -372,7 +372,7 @@ clc_status clc_context_create_with_cache(size_t index, const char* cache_dir, cl
         cudaDeviceProp p;
         gbc::check_cuda(cudaGetDeviceProperties(&p, (int)index), "cudaGetDeviceProperties");
         auto ctx = std::make_unique<gbc::device_context>(
-            (int)index, nullptr, gbc::default_pool_options(p.totalGlobalMem),
+            (int)index, nullptr, gbc::default_arena_config(p.totalGlobalMem),
             cache_dir != nullptr ? cache_dir : "");
         *out = new clc_context_s{std::move(ctx)};
     });
@@ -958,13 +958,13 @@ clc_status clc_context_memory_stats(clc_context ctx, clc_memory_stats* out)
 {
     if (ctx == nullptr || out == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
     return guarded([&] {
-        const auto s = ctx->ctx->stats->statistics();
-        out->current_bytes = s.current_bytes;
-        out->peak_bytes = s.peak_bytes;
-        out->total_bytes = s.total_bytes;
-        out->current_allocations = s.current_allocations;
-        out->total_allocations = s.total_allocations;
-        out->cached_bytes = ctx->ctx->pool->cached_bytes();
+        const gbc::stream_arena::usage u = ctx->ctx->arena->stats();
+        out->current_bytes = u.current_bytes;
+        out->peak_bytes = u.peak_bytes;
+        out->total_bytes = u.total_bytes;
+        out->current_allocations = u.current_allocations;
+        out->total_allocations = u.total_allocations;
+        out->cached_bytes = u.idle_bytes;
     });
 }
 
@@ -973,7 +973,7 @@ clc_status clc_context_release_cache(clc_context ctx)
     if (ctx == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
     return guarded([&] {
         ctx->ctx->activate();
-        ctx->ctx->pool->release();
+        ctx->ctx->arena->trim();
     });
 }
 

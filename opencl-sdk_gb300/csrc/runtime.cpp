@@ -107,20 +107,20 @@ void cuda_async_resource::flush_deferred()
     deferred_.clear();
 }
 
-pool_resource::options default_pool_options(std::size_t global_memory)
+stream_arena::config default_arena_config(std::size_t global_memory)
 {
-    pool_resource::options o;
-    o.max_cached_bytes = std::max<std::size_t>(o.max_cached_bytes, global_memory / 8);
+    stream_arena::config c;
+    c.retain_bytes = std::max<std::size_t>(c.retain_bytes, global_memory / 8);
     if (const char* env = std::getenv("CLC_POOL_MAX_CACHED_BYTES")) {
         char* end = nullptr;
         const unsigned long long v = std::strtoull(env, &end, 10);
-        if (end != env) o.max_cached_bytes = (std::size_t)v;
+        if (end != env) c.retain_bytes = (std::size_t)v;
     }
-    return o;
+    return c;
 }
 
 device_context::device_context(int dev, cudaStream_t external_stream,
-                               const pool_resource::options& opts, const std::string& tuning_dir)
+                               const stream_arena::config& arena_cfg, const std::string& tuning_dir)
     : device(dev)
 {
     check_cuda(cudaSetDevice(dev), "cudaSetDevice");
@@ -143,9 +143,8 @@ device_context::device_context(int dev, cudaStream_t external_stream,
     }
     stream = holder->stream;
     upstream = std::make_shared<cuda_async_resource>(holder);
-    pool = std::make_shared<pool_resource>(upstream, opts);
-    stats = std::make_shared<statistics_adaptor>(pool);
-    resource = stats;
+    arena = std::make_shared<stream_arena>(upstream, arena_cfg);
+    resource = arena;
 
     try {
         check_cuda(cudaMalloc(&d_error, sizeof(int)), "cudaMalloc");

@@ -5,15 +5,17 @@
 // The reference's compute_context bundles an in-order cl::CommandQueue, a
 // memory_resource and a JIT program_cache
 // (lib/include/CL/Compute/Context.hpp:25-59, MemoryResource.cpp:169-197).
-// Here the queue is a CUDA stream, the pool sits on stream-ordered
-// cudaMallocAsync, and the program cache is replaced by kernels compiled
-// ahead of time for sm_103a plus a tuning table of launch shapes.
+// Here the queue is a CUDA stream, temporaries come from a stream-ordered
+// slab arena over cudaMallocAsync, and the program cache is replaced by
+// kernels compiled ahead of time for sm_103a plus a tuning table of launch
+// shapes.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -21,7 +23,7 @@
 #include <string>
 #include <vector>
 
-#include "pool.hpp"
+#include "arena.hpp"
 
 namespace gbc {
 
@@ -174,9 +176,8 @@ struct device_context {
     std::string name;
     std::shared_ptr<stream_holder> holder;
     cudaStream_t stream = nullptr;
-    std::shared_ptr<pool_resource> pool;
-    std::shared_ptr<statistics_adaptor> stats;  // what algorithms allocate from
-    std::shared_ptr<memory_resource> resource;  // == stats
+    std::shared_ptr<stream_arena> arena;        // temporaries and buffers
+    std::shared_ptr<memory_resource> resource;  // == arena: what algorithms allocate from
     tuning_table tuning;
     std::string tuning_path;
     profiler prof;
@@ -195,7 +196,7 @@ struct device_context {
     cudaStream_t aux_stream();
 
     device_context(int device, cudaStream_t external_stream,
-                   const pool_resource::options& opts, const std::string& tuning_dir);
+                   const stream_arena::config& arena_cfg, const std::string& tuning_dir);
     ~device_context();
     device_context(const device_context&) = delete;
     device_context& operator=(const device_context&) = delete;
@@ -214,10 +215,10 @@ struct device_context {
     int take_device_error();
 };
 
-//! The memory resource's default cache limit on this device: the reference
-//! keeps 1 GiB, which is too small to hold one 2^28-pair sort's temporaries;
-//! a GB300 keeps up to 1/8 of HBM (CLC_POOL_MAX_CACHED_BYTES overrides).
-pool_resource::options default_pool_options(std::size_t global_memory);
+//! The arena's settings on a device with `global_memory` bytes: idle space
+//! kept for reuse up to 1/8 of HBM (at least 1 GiB; one 2^28-pair sort needs
+//! 2 GiB of temporaries); CLC_POOL_MAX_CACHED_BYTES overrides the limit.
+stream_arena::config default_arena_config(std::size_t global_memory);
 
 // ---- algorithms (internal C++ entry points) -------------------------------
 // Every function enqueues on ctx.stream and returns without synchronising

@@ -752,3 +752,4 @@ def reduce_by_key_raw(ctx: Context, keys: int, key_dtype, values: int, n: int, k
                                          C.c_void_p(keys_out), C.c_void_p(sums_out), C.c_void_p(counts_out or None),
                                          C.c_void_p(hist16 or None), C.byref(runs) if want_count else None))
     return runs.value if want_count else None
+

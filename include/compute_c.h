@@ -41,6 +41,7 @@ extern "C" {
 typedef struct clc_context_s* clc_context;
 typedef struct clc_buffer_s* clc_buffer;
 typedef struct clc_kernel_s* clc_kernel;
+typedef struct clc_map_s* clc_map; /* extension: static_map */
 
 /* Numeric values as in the reference (compute_c.h:30-41). */
 typedef enum clc_status {
@@ -338,6 +339,10 @@ typedef struct clc_memory_stats {
     size_t cached_bytes;
 } clc_memory_stats;
 GBC_EXPORT clc_status clc_context_memory_stats(clc_context ctx, clc_memory_stats* out);
+/* The arena's slabs: device bytes held, slab count, and how many slabs it
+ * has taken from and handed back to the device so far. */
+GBC_EXPORT clc_status clc_context_arena_info(clc_context ctx, size_t* held_bytes, size_t* slabs,
+                                             size_t* slab_allocations, size_t* slab_releases);
 /* Hands every idle slab of the context's arena back to the device. */
 GBC_EXPORT clc_status clc_context_release_cache(clc_context ctx);
 
@@ -355,6 +360,74 @@ GBC_EXPORT clc_status clc_histogram_even_raw(clc_context ctx, const void* in, si
 GBC_EXPORT clc_status clc_reduce_raw(clc_context ctx, const void* in, size_t n, clc_type type,
                                      const char* op, const char* identity, const void* init,
                                      void* result);
+
+/* Bitpack compression of uint32 data: the reference's compress_bitpack /
+ * decompress_bitpack and compressed_buffer::serialize / deserialize
+ * (lib/include/CL/Compute/Compression.hpp, Compression.cpp:139-278), which
+ * have no C entry points there. The device format is the reference's: per
+ * chunk of chunk_size elements (a power of two in [256, 65536]) three words
+ * {base, bit width, offset of its packed words}, then the packed words;
+ * delta != 0 packs zigzag-encoded differences of consecutive elements.
+ *
+ * clc_bitpack_compress allocates *out (exactly *out_words words) from the
+ * context and blocks once to learn the size. clc_bitpack_decompress writes n
+ * elements to out, asynchronously. clc_bitpack_serialize writes the blob
+ * (8-word header + data words) when blob is not NULL and reports its size in
+ * *needed; clc_bitpack_deserialize validates a blob (magic, version, sizes,
+ * and that every chunk header stays inside the data) and uploads its data.
+ * The _raw forms work on device pointers: clc_bitpack_compress_raw needs an
+ * output capacity of at least the compressed size, which
+ * clc_bitpack_words_bound(n, chunk_size) bounds (0 for an invalid
+ * chunk_size). */
+GBC_EXPORT size_t clc_bitpack_words_bound(size_t n, size_t chunk_size);
+GBC_EXPORT clc_status clc_bitpack_compress(clc_context ctx, clc_buffer in, size_t n, size_t chunk_size,
+                                           int delta, clc_buffer* out, size_t* out_words);
+GBC_EXPORT clc_status clc_bitpack_decompress(clc_context ctx, clc_buffer data, size_t n, size_t chunk_size,
+                                             int delta, clc_buffer out);
+GBC_EXPORT clc_status clc_bitpack_compress_raw(clc_context ctx, const uint32_t* in, size_t n, size_t chunk_size,
+                                               int delta, uint32_t* out, size_t out_capacity_words,
+                                               size_t* out_words);
+GBC_EXPORT clc_status clc_bitpack_decompress_raw(clc_context ctx, const uint32_t* data, size_t words, size_t n,
+                                                 size_t chunk_size, int delta, uint32_t* out);
+GBC_EXPORT clc_status clc_bitpack_serialize(clc_context ctx, clc_buffer data, size_t n, size_t chunk_size,
+                                            int delta, void* blob, size_t blob_bytes, size_t* needed);
+GBC_EXPORT clc_status clc_bitpack_deserialize(clc_context ctx, const void* blob, size_t blob_bytes,
+                                              clc_buffer* data, size_t* n, size_t* chunk_size, int* delta);
+
+/* static_map: a fixed-capacity hash map from uint32 keys to uint32 values,
+ * the reference's cl::compute::static_map (lib/include/CL/Compute/
+ * HashMap.hpp, HashMap.cpp) through C, which the reference does not offer.
+ * Open addressing with linear probing over a power-of-two table (capacity
+ * rounded up, at least 2, at most 2^31), hashed with the MurmurHash3
+ * finalizer; empty_key marks free slots and is never inserted; find returns
+ * empty_value for absent keys; inserting a key already present keeps its
+ * first value. Keep the load factor below ~0.7 for short probes.
+ *
+ * clc_map_insert blocks and reports how many keys were new; a full table
+ * returns CLC_ERROR_OUT_OF_MEMORY ("table is full", as the reference throws
+ * std::overflow_error) after inserting what fits. find/contains run
+ * asynchronously on the context's stream and see every earlier insert;
+ * found[i] is a byte, 1 when keys[i] is present. clc_map_slots copies the
+ * table into separate slot-key and slot-value arrays (either may be NULL),
+ * the reference's slot_keys()/slot_values(). A map holds its device memory
+ * until clc_map_release and may outlive its context. */
+GBC_EXPORT clc_status clc_map_create(clc_context ctx, size_t capacity, uint32_t empty_key, uint32_t empty_value,
+                                     clc_map* out);
+GBC_EXPORT void clc_map_release(clc_map map);
+GBC_EXPORT clc_status clc_map_info(clc_map map, size_t* size, size_t* capacity, uint32_t* empty_key,
+                                   uint32_t* empty_value);
+GBC_EXPORT clc_status clc_map_clear(clc_context ctx, clc_map map);
+GBC_EXPORT clc_status clc_map_insert(clc_context ctx, clc_map map, clc_buffer keys, clc_buffer values, size_t n,
+                                     size_t* inserted);
+GBC_EXPORT clc_status clc_map_find(clc_context ctx, clc_map map, clc_buffer keys, size_t n, clc_buffer values);
+GBC_EXPORT clc_status clc_map_contains(clc_context ctx, clc_map map, clc_buffer keys, size_t n, clc_buffer found);
+GBC_EXPORT clc_status clc_map_slots(clc_context ctx, clc_map map, clc_buffer slot_keys, clc_buffer slot_values);
+GBC_EXPORT clc_status clc_map_insert_raw(clc_context ctx, clc_map map, const uint32_t* keys, const uint32_t* values,
+                                         size_t n, size_t* inserted);
+GBC_EXPORT clc_status clc_map_find_raw(clc_context ctx, clc_map map, const uint32_t* keys, size_t n,
+                                       uint32_t* values);
+GBC_EXPORT clc_status clc_map_contains_raw(clc_context ctx, clc_map map, const uint32_t* keys, size_t n,
+                                           uint8_t* found);
 
 /* Allocation-free int32 plus-scan. No counterpart in the reference.
  *

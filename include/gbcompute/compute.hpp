@@ -324,6 +324,14 @@ public:
         copy_to_host(ctx.queue(), out.data(), size_);
         return out;
     }
+    //! Takes ownership of a buffer handle from the C interface.
+    static device_buffer adopt(clc_buffer handle, std::size_t size)
+    {
+        device_buffer b;
+        b.buf_ = handle;
+        b.size_ = size;
+        return b;
+    }
     static device_buffer from_host(compute_context& ctx, const std::vector<T>& values)
     {
         device_buffer b(ctx, values.size());
@@ -461,6 +469,154 @@ void histogram_even(compute_context& ctx, const device_buffer<T>& in, device_buf
     detail::check(clc_histogram_even(ctx.handle(), in.get(), in.size(), detail::type_of<T>::value, histogram.get(),
                                      histogram.size(), lower, upper));
 }
+
+// ---- bitpack compression (Compression.hpp) ----------------------------------
+
+//! Options of compress_bitpack: delta coding of consecutive elements, and the
+//! chunk size (a power of two in [256, 65536]).
+struct bitpack_options {
+    bool delta = false;
+    std::size_t chunk_size = 2048;
+};
+
+//! The reference's compressed_buffer: the device words of its chunk format
+//! (per chunk {base, width, offset}, then the packed words).
+struct compressed_buffer {
+    device_buffer<cl_uint> data;
+    std::size_t num_elements = 0;
+    std::size_t chunk_size = 0;
+    bool delta = false;
+
+    std::size_t num_chunks() const { return chunk_size == 0 ? 0 : (num_elements + chunk_size - 1) / chunk_size; }
+    std::size_t compressed_bytes() const { return data.bytes(); }
+    std::size_t uncompressed_bytes() const { return num_elements * sizeof(cl_uint); }
+
+    //! Host blob: an 8-word header, then the device words.
+    std::vector<unsigned char> serialize(compute_context& ctx) const
+    {
+        std::size_t needed = 0;
+        detail::check(clc_bitpack_serialize(ctx.handle(), data.get(), num_elements, chunk_size, delta ? 1 : 0,
+                                            nullptr, 0, &needed));
+        std::vector<unsigned char> blob(needed);
+        detail::check(clc_bitpack_serialize(ctx.handle(), data.get(), num_elements, chunk_size, delta ? 1 : 0,
+                                            blob.data(), blob.size(), &needed));
+        return blob;
+    }
+    //! Validates the blob (std::invalid_argument when it is not one) and
+    //! uploads its words.
+    static compressed_buffer deserialize(compute_context& ctx, const std::vector<unsigned char>& blob)
+    {
+        clc_buffer h = nullptr;
+        std::size_t n = 0, chunk = 0;
+        int d = 0;
+        detail::check(clc_bitpack_deserialize(ctx.handle(), blob.data(), blob.size(), &h, &n, &chunk, &d));
+        compressed_buffer r;
+        r.data = device_buffer<cl_uint>::adopt(h, clc_buffer_size(h) / sizeof(cl_uint));
+        r.num_elements = n;
+        r.chunk_size = chunk;
+        r.delta = d != 0;
+        return r;
+    }
+};
+
+inline compressed_buffer compress_bitpack(compute_context& ctx, const device_buffer<cl_uint>& in,
+                                          bitpack_options options = bitpack_options())
+{
+    clc_buffer h = nullptr;
+    std::size_t words = 0;
+    detail::check(clc_bitpack_compress(ctx.handle(), in.get(), in.size(), options.chunk_size, options.delta ? 1 : 0,
+                                       &h, &words));
+    compressed_buffer r;
+    r.data = device_buffer<cl_uint>::adopt(h, words);
+    r.num_elements = in.size();
+    r.chunk_size = options.chunk_size;
+    r.delta = options.delta;
+    return r;
+}
+
+//! Decompresses into out, which must hold in.num_elements values.
+inline void decompress_bitpack(compute_context& ctx, const compressed_buffer& in, device_buffer<cl_uint>& out)
+{
+    if (out.size() < in.num_elements) throw std::invalid_argument("decompress_bitpack: output too small");
+    detail::check(clc_bitpack_decompress(ctx.handle(), in.data.get(), in.num_elements, in.chunk_size,
+                                         in.delta ? 1 : 0, out.get()));
+}
+
+// ---- static_map (HashMap.hpp) --------------------------------------------------
+
+//! Fixed-capacity hash map from cl_uint keys to cl_uint values: linear
+//! probing over a power-of-two table, MurmurHash3 finalizer; empty_key marks
+//! free slots, find returns empty_value for absent keys, insert keeps a
+//! key's first value and throws std::overflow_error when the table is full.
+class static_map {
+public:
+    static_map(compute_context& ctx, std::size_t capacity, cl_uint empty_key = 0xFFFFFFFFu,
+               cl_uint empty_value = 0xFFFFFFFFu)
+        : ctx_(ctx)
+    {
+        detail::check(clc_map_create(ctx.handle(), capacity, empty_key, empty_value, &map_));
+    }
+    ~static_map() { clc_map_release(map_); }
+    static_map(const static_map&) = delete;
+    static_map& operator=(const static_map&) = delete;
+
+    //! Inserts n pairs; returns how many keys were new.
+    std::size_t insert(const device_buffer<cl_uint>& keys, const device_buffer<cl_uint>& values, std::size_t n)
+    {
+        if (n > keys.size() || n > values.size()) throw std::invalid_argument("static_map::insert: n out of range");
+        std::size_t added = 0;
+        const clc_status s = clc_map_insert(ctx_.handle(), map_, keys.get(), values.get(), n, &added);
+        if (s == CLC_ERROR_OUT_OF_MEMORY) throw std::overflow_error(clc_last_error());
+        detail::check(s);
+        return added;
+    }
+    std::size_t insert(const device_buffer<cl_uint>& keys, const device_buffer<cl_uint>& values)
+    {
+        return insert(keys, values, keys.size());
+    }
+    //! values[i] = map[keys[i]], or empty_value when absent.
+    void find(const device_buffer<cl_uint>& keys, device_buffer<cl_uint>& values) const
+    {
+        if (values.size() < keys.size()) throw std::invalid_argument("static_map::find: output too small");
+        detail::check(clc_map_find(ctx_.handle(), map_, keys.get(), keys.size(), values.get()));
+    }
+    //! found[i] = 1 when keys[i] is present, else 0.
+    void contains(const device_buffer<cl_uint>& keys, device_buffer<cl_uchar>& found) const
+    {
+        if (found.size() < keys.size()) throw std::invalid_argument("static_map::contains: output too small");
+        detail::check(clc_map_contains(ctx_.handle(), map_, keys.get(), keys.size(), found.get()));
+    }
+    void clear() { detail::check(clc_map_clear(ctx_.handle(), map_)); }
+
+    std::size_t size() const { return info().size; }
+    std::size_t capacity() const { return info().capacity; }
+    double load_factor() const { return double(size()) / double(capacity()); }
+    cl_uint empty_key() const { return info().empty_key; }
+    cl_uint empty_value() const { return info().empty_value; }
+    //! The table's slot keys and values (copies of the device table).
+    device_buffer<cl_uint> slot_keys() const { return slots(true); }
+    device_buffer<cl_uint> slot_values() const { return slots(false); }
+
+private:
+    struct info_t {
+        std::size_t size, capacity;
+        cl_uint empty_key, empty_value;
+    };
+    info_t info() const
+    {
+        info_t i{};
+        detail::check(clc_map_info(map_, &i.size, &i.capacity, &i.empty_key, &i.empty_value));
+        return i;
+    }
+    device_buffer<cl_uint> slots(bool keys) const
+    {
+        device_buffer<cl_uint> b(ctx_, capacity());
+        detail::check(clc_map_slots(ctx_.handle(), map_, keys ? b.get() : nullptr, keys ? nullptr : b.get()));
+        return b;
+    }
+    compute_context& ctx_;
+    clc_map map_ = nullptr;
+};
 
 // ---- extensions (no counterpart in the reference's C++ API) -----------------
 

@@ -35,6 +35,8 @@ SOURCES = [
     "reduce_by_key.cu",
     "select.cu",
     "transform.cu",
+    "bitpack.cu",
+    "static_map.cu",
 ]
 
 COMMON = [

@@ -71,6 +71,7 @@ public:
         std::size_t current_bytes = 0, peak_bytes = 0, total_bytes = 0;
         std::size_t current_allocations = 0, total_allocations = 0;
         std::size_t held_bytes = 0, idle_bytes = 0, slabs = 0;
+        std::size_t slab_allocations = 0, slab_releases = 0;  // upstream calls so far
     };
 
     stream_arena(std::shared_ptr<memory_resource> upstream, config c) : up_(std::move(upstream)), cfg_(c)
@@ -229,6 +230,7 @@ private:
         }
         slabs_.push_back(std::unique_ptr<slab>(new slab{static_cast<char*>(mem), bytes, 0}));
         held_ += bytes;
+        ++use_.slab_allocations;
         index_free(slabs_.back()->base, bytes, slabs_.back().get());
     }
     //! Hands empty slabs back, largest first, until at most `keep` idle bytes
@@ -246,6 +248,7 @@ private:
             up_->deallocate(s->base, s->bytes);
             held_ -= s->bytes;
             freed += s->bytes;
+            ++use_.slab_releases;
             slabs_.erase(std::find_if(slabs_.begin(), slabs_.end(),
                                       [s](const std::unique_ptr<slab>& q) { return q.get() == s; }));
         }

@@ -1,0 +1,330 @@
+// Bitpack compression of 32-bit integers: frame-of-reference bit packing per
+// chunk, optionally after a delta + zigzag transform.
+//
+// Reference path replaced: compress_bitpack / decompress_bitpack
+// (lib/src/Compute/Compression.cpp:139-200) with kernels clc_bitpack_analyze,
+// clc_bitpack_pack and clc_bitpack_unpack (Compression.cpp:39-124). The
+// device format is kept word for word, since compressed data outlives the
+// library that wrote it (Compression.cpp:19-24): per chunk three words {base,
+// width, offset of its packed words relative to the packed area}, then the
+// packed area; element j of a chunk occupies bits [j * width, (j + 1) *
+// width) of the chunk's words, least significant bits first; width = 32 -
+// clz(max - min) of the chunk's encoded values (0 when they are all equal);
+// delta mode stores zigzag(x[i] - x[i-1]) with wrapping arithmetic and
+// x[-1] = 0, and decoding ends with a wrapping inclusive prefix sum over the
+// whole array.
+//
+// How it runs here:
+//   * analyze: one warp per chunk, 128-bit loads, warp min/max; the chunks'
+//     word counts are turned into offsets by the library's single-pass scan
+//     (the reference's scan client at Compression.cpp:178), which also
+//     yields the total size;
+//   * pack: one warp per chunk, in rounds of 2,048 elements. Lane l packs
+//     elements 64 l .. 64 l + 63 of the round, which occupy exactly 2 x width
+//     whole words, so no word is shared between lanes (the reference ORs
+//     every element into global memory with atomics). The lanes' words are
+//     staged in shared memory at an odd per-lane stride (2 width + 1: the
+//     lanes hit different banks) and written out by the warp in order,
+//     coalesced;
+//   * unpack: one thread per 4 elements (a 128-bit store), reading the 1-5
+//     packed words that hold them; delta mode then runs the library's scan in
+//     place.
+#include <algorithm>
+#include <cstring>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/compute_c.h"
+#include "device_common.cuh"
+#include "runtime.hpp"
+
+namespace gbc {
+namespace bitpack {
+
+using dev::FULL_MASK;
+
+constexpr int THREADS = 256;
+constexpr int WARPS = THREADS / 32;
+constexpr int PACK_THREADS = 128;  // 4 warps x 8.1 KiB of staging: static shared memory
+constexpr int PACK_WARPS = PACK_THREADS / 32;
+constexpr uint32_t LANE_ELEMS = 64;          // per lane and round
+constexpr uint32_t ROUND = 32 * LANE_ELEMS;  // per warp and round
+
+__device__ __forceinline__ uint32_t zigzag(uint32_t d) { return (d << 1) ^ (0u - (d >> 31)); }
+__device__ __forceinline__ uint32_t unzigzag(uint32_t v) { return (v >> 1) ^ (0u - (v & 1u)); }
+
+// Encoded values in[i .. i+3] (i a multiple of 4; `prev` = in[i - 1], or 0).
+template <bool DELTA> __device__ __forceinline__ void encode4(uint4 w, uint32_t prev, uint32_t (&e)[4])
+{
+    if (DELTA) {
+        e[0] = zigzag(w.x - prev);
+        e[1] = zigzag(w.y - w.x);
+        e[2] = zigzag(w.z - w.y);
+        e[3] = zigzag(w.w - w.z);
+    } else {
+        e[0] = w.x, e[1] = w.y, e[2] = w.z, e[3] = w.w;
+    }
+}
+
+template <bool DELTA> __device__ __forceinline__ uint32_t encode_at(const uint32_t* in, uint32_t i)
+{
+    if (!DELTA) return in[i];
+    return zigzag(in[i] - (i > 0 ? in[i - 1] : 0u));
+}
+
+// One warp per chunk: base and width into hdr[2c], hdr[2c + 1], the chunk's
+// packed word count into words[c].
+template <bool DELTA>
+__global__ void __launch_bounds__(THREADS) k_bp_analyze(const uint32_t* __restrict__ in, uint32_t n, uint32_t chunk,
+                                                        uint32_t chunks, uint32_t* __restrict__ hdr,
+                                                        uint32_t* __restrict__ words)
+{
+    const int lane = threadIdx.x & 31;
+    const bool vec = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    for (uint32_t c = blockIdx.x * WARPS + (threadIdx.x >> 5); c < chunks; c += gridDim.x * WARPS) {
+        const uint32_t start = c * chunk, count = min(chunk, n - start);
+        uint32_t lo = 0xFFFFFFFFu, hi = 0;
+        uint32_t j = 0;
+        if (vec) {
+            for (; j + 4 * 32 <= count; j += 4 * 32) {
+                const uint32_t i = start + j + 4 * lane;
+                const uint4 w = dev::ld_stream(reinterpret_cast<const uint4*>(in + i));
+                uint32_t e[4];
+                encode4<DELTA>(w, DELTA && i > 0 ? in[i - 1] : 0u, e);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) lo = min(lo, e[q]), hi = max(hi, e[q]);
+            }
+        }
+        for (uint32_t k = j + lane; k < count; k += 32) {
+            const uint32_t e = encode_at<DELTA>(in, start + k);
+            lo = min(lo, e), hi = max(hi, e);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(FULL_MASK, lo, o));
+            hi = max(hi, __shfl_xor_sync(FULL_MASK, hi, o));
+        }
+        if (lane == 0) {
+            const uint32_t range = hi - lo;
+            const uint32_t width = range == 0 ? 0u : 32u - __clz(range);
+            hdr[2 * c] = lo;
+            hdr[2 * c + 1] = width;
+            words[c] = (uint32_t)(((uint64_t)count * width + 31) / 32);
+        }
+    }
+}
+
+// One warp per chunk: the header triple and the chunk's packed words.
+template <bool DELTA>
+__global__ void __launch_bounds__(PACK_THREADS) k_bp_pack(const uint32_t* __restrict__ in, uint32_t n, uint32_t chunk,
+                                                     uint32_t chunks, const uint32_t* __restrict__ hdr,
+                                                     const uint32_t* __restrict__ offsets, uint32_t* __restrict__ out)
+{
+    __shared__ uint32_t stage[PACK_WARPS][32 * 65];  // per lane 2 x width + 1 <= 65 words
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* my = stage[warp];
+    const bool vec = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    for (uint32_t c = blockIdx.x * PACK_WARPS + warp; c < chunks; c += gridDim.x * PACK_WARPS) {
+        const uint32_t start = c * chunk, count = min(chunk, n - start);
+        const uint32_t base = hdr[2 * c], width = hdr[2 * c + 1], off = offsets[c];
+        if (lane == 0) {
+            out[3 * c] = base;
+            out[3 * c + 1] = width;
+            out[3 * c + 2] = off;
+        }
+        if (width == 0) continue;
+        uint32_t* packed = out + 3 * (size_t)chunks + off;
+        const uint32_t lane_words = 2 * width, pitch = lane_words + 1;
+        for (uint32_t r0 = 0; r0 < count; r0 += ROUND) {
+            // this lane's elements of the round
+            const uint32_t j0 = r0 + lane * LANE_ELEMS;
+            const uint32_t mine = j0 < count ? min(LANE_ELEMS, count - j0) : 0u;
+            uint64_t acc = 0;
+            uint32_t bits = 0, k = 0;
+            auto put = [&](uint32_t v) {
+                acc |= (uint64_t)(v - base) << bits;
+                bits += width;
+                if (bits >= 32) {
+                    my[lane * pitch + k++] = (uint32_t)acc;
+                    acc >>= 32;
+                    bits -= 32;
+                }
+            };
+            const uint32_t i0 = start + j0;
+            if (vec && mine == LANE_ELEMS) {
+                uint32_t prev = DELTA && i0 > 0 ? in[i0 - 1] : 0u;
+#pragma unroll 4
+                for (uint32_t q = 0; q < LANE_ELEMS; q += 4) {
+                    const uint4 w = *reinterpret_cast<const uint4*>(in + i0 + q);
+                    uint32_t e[4];
+                    encode4<DELTA>(w, prev, e);
+                    prev = w.w;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) put(e[t]);
+                }
+            } else {
+                for (uint32_t q = 0; q < mine; ++q) put(encode_at<DELTA>(in, i0 + q));
+            }
+            if (bits > 0) my[lane * pitch + k++] = (uint32_t)acc;  // the partial last word
+            __syncwarp();
+            // the round's words, in order: lane l's words are words
+            // [l * 2 width, ...) of the round
+            const uint32_t rcount = min(ROUND, count - r0);
+            const uint32_t rwords = (uint32_t)(((uint64_t)rcount * width + 31) / 32);
+            uint32_t* dst = packed + (size_t)(r0 / 32) * width;  // r0 * width / 32 (r0 is a multiple of 2048)
+            for (uint32_t m = lane; m < rwords; m += 32) {
+                const uint32_t l = m / lane_words, kk = m - l * lane_words;
+                dst[m] = my[l * pitch + kk];
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// One thread per 4 elements. Chunks hold a multiple of 4 elements (at least
+// 256), so a group never straddles two chunks.
+template <bool DELTA>
+__global__ void __launch_bounds__(THREADS) k_bp_unpack(const uint32_t* __restrict__ data, uint32_t n,
+                                                       uint32_t chunk_shift, uint32_t chunks,
+                                                       uint32_t* __restrict__ out)
+{
+    const uint32_t groups = (n + 3) / 4;
+    const bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    for (uint32_t g = blockIdx.x * THREADS + threadIdx.x; g < groups; g += gridDim.x * THREADS) {
+        const uint32_t i = 4 * g;
+        const uint32_t c = i >> chunk_shift, j = i & ((1u << chunk_shift) - 1u);
+        const uint32_t base = __ldg(data + 3 * c), width = __ldg(data + 3 * c + 1);
+        uint32_t v[4] = {base, base, base, base};
+        if (width != 0) {
+            const uint32_t* p = data + 3 * (size_t)chunks + __ldg(data + 3 * c + 2);
+            const uint64_t first = (uint64_t)j * width;
+            const uint32_t w0 = (uint32_t)(first >> 5);
+            const uint32_t mask = width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u);
+            // the group's elements below n lie in bits [first, first + valid
+            // x width): at most 5 words from w0; words past the last of them
+            // may lie beyond the chunk's packed words and are not read
+            const uint32_t valid = min(4u, n - i);
+            const uint32_t last_word = (uint32_t)((first + (uint64_t)valid * width - 1) >> 5);
+            uint32_t wv[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) wv[q] = (w0 + q <= last_word) ? __ldg(p + w0 + q) : 0u;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const uint64_t bit = first + (uint64_t)t * width;
+                const uint32_t q = (uint32_t)(bit >> 5) - w0, sh = (uint32_t)(bit & 31);
+                const uint64_t both = (uint64_t)wv[q] | ((uint64_t)(q + 1 < 5 ? wv[q + 1] : 0u) << 32);
+                v[t] = (uint32_t)(both >> sh) & mask;
+                v[t] += base;
+            }
+        }
+        if (DELTA) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) v[t] = unzigzag(v[t]);
+        }
+        if (vec && i + 4 <= n) {
+            *reinterpret_cast<uint4*>(out + i) = make_uint4(v[0], v[1], v[2], v[3]);
+        } else {
+            for (int t = 0; t < 4 && i + t < n; ++t) out[i + t] = v[t];
+        }
+    }
+}
+
+void check_chunk(std::size_t chunk)
+{
+    if (chunk < 256 || chunk > 65536 || (chunk & (chunk - 1)) != 0)
+        throw std::invalid_argument("bitpack: chunk_size must be a power of two in [256, 65536]");
+}
+
+int grid_for(device_context& ctx, std::size_t work_warps, int warps_per_cta)
+{
+    const std::size_t ctas = (work_warps + warps_per_cta - 1) / warps_per_cta;
+    return (int)std::max<std::size_t>(1, std::min<std::size_t>(ctas, (std::size_t)ctx.sm_count * 64 / warps_per_cta));
+}
+
+}  // namespace bitpack
+
+std::size_t bitpack_words_bound(std::size_t n, std::size_t chunk)
+{
+    bitpack::check_chunk(chunk);
+    return n == 0 ? 0 : 3 * ((n + chunk - 1) / chunk) + n;
+}
+
+std::size_t bitpack_compress(device_context& ctx, const uint32_t* in, std::size_t n, std::size_t chunk, bool delta,
+                             const std::function<uint32_t*(std::size_t)>& make_output)
+{
+    using namespace bitpack;
+    check_chunk(chunk);
+    if (n == 0) return 0;
+    check_size(n);
+    if (in == nullptr) throw std::invalid_argument("bitpack: null input");
+    ctx.activate();
+    const uint32_t chunks = (uint32_t)((n + chunk - 1) / chunk);
+    temp_buffer hdr(ctx.resource, (std::size_t)chunks * 2 * 4);
+    temp_buffer words(ctx.resource, (std::size_t)chunks * 4);
+    temp_buffer offs(ctx.resource, (std::size_t)chunks * 4);
+    temp_buffer total(ctx.resource, 8);
+    const int grid = grid_for(ctx, chunks, WARPS);
+    {
+        kernel_timer kt(ctx, "bitpack.analyze");
+        if (delta)
+            k_bp_analyze<true><<<grid, THREADS, 0, ctx.stream>>>(in, (uint32_t)n, (uint32_t)chunk, chunks,
+                                                                 hdr.as<uint32_t>(), words.as<uint32_t>());
+        else
+            k_bp_analyze<false><<<grid, THREADS, 0, ctx.stream>>>(in, (uint32_t)n, (uint32_t)chunk, chunks,
+                                                                  hdr.as<uint32_t>(), words.as<uint32_t>());
+        check_cuda(cudaGetLastError(), "bitpack analyze launch");
+    }
+    const uint32_t zero = 0;
+    scan(ctx, words.get(), offs.get(), chunks, elem::u32, op_kind::plus, &zero, true, total.get());
+    uint64_t packed = 0;
+    check_cuda(cudaMemcpyAsync(&packed, total.get(), 8, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    check_cuda(cudaStreamSynchronize(ctx.stream), "cudaStreamSynchronize");
+    const std::size_t out_words = 3 * (std::size_t)chunks + packed;
+    uint32_t* out = make_output(out_words);
+    const int pgrid = grid_for(ctx, chunks, PACK_WARPS);
+    {
+        kernel_timer kt(ctx, "bitpack.pack");
+        if (delta)
+            k_bp_pack<true><<<pgrid, PACK_THREADS, 0, ctx.stream>>>(in, (uint32_t)n, (uint32_t)chunk, chunks,
+                                                              hdr.as<uint32_t>(), offs.as<uint32_t>(), out);
+        else
+            k_bp_pack<false><<<pgrid, PACK_THREADS, 0, ctx.stream>>>(in, (uint32_t)n, (uint32_t)chunk, chunks,
+                                                               hdr.as<uint32_t>(), offs.as<uint32_t>(), out);
+        check_cuda(cudaGetLastError(), "bitpack pack launch");
+    }
+    return out_words;
+}
+
+void bitpack_decompress(device_context& ctx, const uint32_t* data, std::size_t words, std::size_t n,
+                        std::size_t chunk, bool delta, uint32_t* out)
+{
+    using namespace bitpack;
+    check_chunk(chunk);
+    if (n == 0) return;
+    check_size(n);
+    if (data == nullptr || out == nullptr) throw std::invalid_argument("bitpack: null argument");
+    const uint32_t chunks = (uint32_t)((n + chunk - 1) / chunk);
+    if (words < 3 * (std::size_t)chunks) throw std::invalid_argument("bitpack: data shorter than its chunk headers");
+    ctx.activate();
+    uint32_t shift = 0;
+    while ((std::size_t(1) << shift) < chunk) ++shift;
+    const std::size_t groups = (n + 3) / 4;
+    const int grid = (int)std::max<std::size_t>(
+        1, std::min<std::size_t>((groups + THREADS - 1) / THREADS, (std::size_t)ctx.sm_count * 16));
+    {
+        kernel_timer kt(ctx, "bitpack.unpack");
+        if (delta)
+            k_bp_unpack<true><<<grid, THREADS, 0, ctx.stream>>>(data, (uint32_t)n, shift, chunks, out);
+        else
+            k_bp_unpack<false><<<grid, THREADS, 0, ctx.stream>>>(data, (uint32_t)n, shift, chunks, out);
+        check_cuda(cudaGetLastError(), "bitpack unpack launch");
+    }
+    if (delta) {
+        const uint32_t zero = 0;
+        scan(ctx, out, out, n, elem::u32, op_kind::plus, &zero, false, nullptr);
+    }
+}
+
+}  // namespace gbc

@@ -48,6 +48,15 @@ struct clc_kernel_s {
     int unused;
 };
 
+struct clc_map_s {
+    std::shared_ptr<gbc::memory_resource> resource;
+    std::shared_ptr<gbc::stream_holder> holder;
+    void* slots;
+    std::size_t capacity;
+    uint32_t empty_key, empty_value;
+    std::size_t size;
+};
+
 struct clc_graph_s {
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -968,6 +977,19 @@ clc_status clc_context_memory_stats(clc_context ctx, clc_memory_stats* out)
     });
 }
 
+clc_status clc_context_arena_info(clc_context ctx, size_t* held_bytes, size_t* slabs, size_t* slab_allocations,
+                                  size_t* slab_releases)
+{
+    if (ctx == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    return guarded([&] {
+        const gbc::stream_arena::usage u = ctx->ctx->arena->stats();
+        if (held_bytes != nullptr) *held_bytes = u.held_bytes;
+        if (slabs != nullptr) *slabs = u.slabs;
+        if (slab_allocations != nullptr) *slab_allocations = u.slab_allocations;
+        if (slab_releases != nullptr) *slab_releases = u.slab_releases;
+    });
+}
+
 clc_status clc_context_release_cache(clc_context ctx)
 {
     if (ctx == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
@@ -1106,6 +1128,289 @@ clc_status clc_tuning_save(clc_context ctx, const char* path)
         std::string p = path != nullptr && *path ? std::string(path) : ctx->ctx->tuning_path;
         require(!p.empty(), "clc: no tuning table path (pass one, or create the context with a cache dir)");
         ctx->ctx->tuning.save(p);
+    });
+}
+
+// ---- bitpack compression ---------------------------------------------------
+// The reference's compressed_buffer (Compression.hpp, Compression.cpp:
+// 139-278) has no C interface; these entry points carry its operations and
+// its serialized form: an 8-word header {magic "CLBP", version 1, delta,
+// chunk size, element count (2 words, low first), data words (2 words)}
+// followed by the device words, validated on load as the reference does
+// (Compression.cpp:226-275).
+
+namespace {
+constexpr uint32_t BITPACK_MAGIC = 0x50424C43u;  // "CLBP"
+constexpr uint32_t BITPACK_VERSION = 1;
+constexpr std::size_t BITPACK_HEADER_WORDS = 8;
+}  // namespace
+
+size_t clc_bitpack_words_bound(size_t n, size_t chunk_size)
+{
+    try {
+        return gbc::bitpack_words_bound(n, chunk_size);
+    } catch (...) {
+        return 0;
+    }
+}
+
+clc_status clc_bitpack_compress(clc_context ctx, clc_buffer in, size_t n, size_t chunk_size, int delta,
+                                clc_buffer* out, size_t* out_words)
+{
+    if (ctx == nullptr || out == nullptr || out_words == nullptr)
+        return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    *out = nullptr;
+    *out_words = 0;
+    return guarded([&] {
+        require_fits(in, n, CLC_TYPE_U32);
+        require_same_device(ctx, in);
+        std::unique_ptr<clc_buffer_s> b(new clc_buffer_s{ctx->ctx->resource, ctx->ctx->holder, nullptr, 0});
+        const std::size_t words = gbc::bitpack_compress(
+            *ctx->ctx, static_cast<const uint32_t*>(in->ptr), n, chunk_size, delta != 0, [&](std::size_t w) {
+                b->bytes = w * 4;
+                if (b->bytes != 0) b->ptr = b->resource->allocate(b->bytes);
+                return static_cast<uint32_t*>(b->ptr);
+            });
+        if (n == 0) gbc::bitpack_words_bound(0, chunk_size);  // validates chunk_size
+        *out_words = words;
+        *out = b.release();
+    });
+}
+
+clc_status clc_bitpack_decompress(clc_context ctx, clc_buffer data, size_t n, size_t chunk_size, int delta,
+                                  clc_buffer out)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        require(data != nullptr, "clc: null buffer");
+        require_fits(out, n, CLC_TYPE_U32);
+        require_same_device(ctx, data);
+        require_same_device(ctx, out);
+        gbc::bitpack_decompress(*ctx->ctx, static_cast<const uint32_t*>(data->ptr), data->bytes / 4, n, chunk_size,
+                                delta != 0, static_cast<uint32_t*>(out->ptr));
+    });
+}
+
+clc_status clc_bitpack_compress_raw(clc_context ctx, const uint32_t* in, size_t n, size_t chunk_size, int delta,
+                                    uint32_t* out, size_t out_capacity_words, size_t* out_words)
+{
+    if (ctx == nullptr || out_words == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    *out_words = 0;
+    return guarded([&] {
+        require(n == 0 || in != nullptr, "clc: null input");
+        std::size_t words = gbc::bitpack_compress(*ctx->ctx, in, n, chunk_size, delta != 0, [&](std::size_t w) {
+            if (w > out_capacity_words || out == nullptr)
+                throw std::invalid_argument("clc_bitpack_compress_raw: output capacity below the compressed size "
+                                            "(clc_bitpack_words_bound gives a sufficient one)");
+            return out;
+        });
+        if (n == 0) gbc::bitpack_words_bound(0, chunk_size);
+        *out_words = words;
+    });
+}
+
+clc_status clc_bitpack_decompress_raw(clc_context ctx, const uint32_t* data, size_t words, size_t n,
+                                      size_t chunk_size, int delta, uint32_t* out)
+{
+    return guarded([&] {
+        require(ctx != nullptr, "clc: null context");
+        gbc::bitpack_decompress(*ctx->ctx, data, words, n, chunk_size, delta != 0, out);
+    });
+}
+
+clc_status clc_bitpack_serialize(clc_context ctx, clc_buffer data, size_t n, size_t chunk_size, int delta, void* blob,
+                                 size_t blob_bytes, size_t* needed)
+{
+    return guarded([&] {
+        require(ctx != nullptr && data != nullptr, "clc: null argument");
+        gbc::bitpack_words_bound(0, chunk_size);  // validates chunk_size
+        const std::size_t words = data->bytes / 4;
+        const std::size_t bytes = (BITPACK_HEADER_WORDS + words) * 4;
+        if (needed != nullptr) *needed = bytes;
+        if (blob == nullptr) return;
+        require(blob_bytes >= bytes, "clc_bitpack_serialize: blob too small");
+        const uint64_t n64 = n, w64 = words;
+        const uint32_t header[BITPACK_HEADER_WORDS] = {
+            BITPACK_MAGIC, BITPACK_VERSION, delta ? 1u : 0u, (uint32_t)chunk_size,
+            (uint32_t)(n64 & 0xFFFFFFFFu), (uint32_t)(n64 >> 32), (uint32_t)(w64 & 0xFFFFFFFFu), (uint32_t)(w64 >> 32)};
+        std::memcpy(blob, header, sizeof header);
+        if (words != 0) {
+            ctx->ctx->activate();
+            gbc::check_cuda(cudaMemcpyAsync(static_cast<char*>(blob) + sizeof header, data->ptr, words * 4,
+                                            cudaMemcpyDeviceToHost, ctx->ctx->stream),
+                            "cudaMemcpyAsync");
+            gbc::check_cuda(cudaStreamSynchronize(ctx->ctx->stream), "cudaStreamSynchronize");
+        }
+    });
+}
+
+clc_status clc_bitpack_deserialize(clc_context ctx, const void* blob, size_t blob_bytes, clc_buffer* data,
+                                   size_t* n, size_t* chunk_size, int* delta)
+{
+    if (ctx == nullptr || blob == nullptr || data == nullptr || n == nullptr || chunk_size == nullptr ||
+        delta == nullptr)
+        return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    *data = nullptr;
+    return guarded([&] {
+        uint32_t h[BITPACK_HEADER_WORDS];
+        require(blob_bytes >= sizeof h, "bitpack: truncated header");
+        std::memcpy(h, blob, sizeof h);
+        require(h[0] == BITPACK_MAGIC && h[1] == BITPACK_VERSION, "bitpack: not a bitpack stream");
+        const uint64_t count = h[4] | ((uint64_t)h[5] << 32), words = h[6] | ((uint64_t)h[7] << 32);
+        require(blob_bytes == (BITPACK_HEADER_WORDS + words) * 4, "bitpack: size mismatch");
+        const uint64_t chunk = h[3];
+        const bool pow2 = chunk >= 256 && chunk <= 65536 && (chunk & (chunk - 1)) == 0;
+        const uint64_t chunks = pow2 ? (count + chunk - 1) / chunk : 0;
+        require(pow2 && (count == 0 || words >= 3 * chunks), "bitpack: corrupt header");
+        require(count <= 0x7FFFFFFFu, "bitpack: more than 2^31-1 elements");
+        // every chunk header must keep the unpack kernel inside the data
+        const uint32_t* body = reinterpret_cast<const uint32_t*>(static_cast<const char*>(blob) + sizeof h);
+        const uint64_t packed = words - 3 * chunks;
+        for (uint64_t c = 0; c < chunks; ++c) {
+            const uint64_t elems = std::min<uint64_t>(chunk, count - c * chunk);
+            const uint32_t width = body[3 * c + 1];
+            require(width <= 32 && (uint64_t)body[3 * c + 2] + (elems * width + 31) / 32 <= packed,
+                    "bitpack: corrupt chunk header");
+        }
+        std::unique_ptr<clc_buffer_s> b(
+            new clc_buffer_s{ctx->ctx->resource, ctx->ctx->holder, nullptr, (std::size_t)words * 4});
+        ctx->ctx->activate();
+        if (words != 0) {
+            b->ptr = b->resource->allocate(b->bytes);
+            gbc::check_cuda(cudaMemcpyAsync(b->ptr, body, b->bytes, cudaMemcpyHostToDevice, ctx->ctx->stream),
+                            "cudaMemcpyAsync");
+            gbc::check_cuda(cudaStreamSynchronize(ctx->ctx->stream), "cudaStreamSynchronize");
+        }
+        *n = (std::size_t)count;
+        *chunk_size = (std::size_t)chunk;
+        *delta = h[2] != 0 ? 1 : 0;
+        *data = b.release();
+    });
+}
+
+// ---- static_map --------------------------------------------------------------
+// The reference's static_map (HashMap.hpp, HashMap.cpp:16-184) has no C
+// interface; these entry points carry its operations.
+
+clc_status clc_map_create(clc_context ctx, size_t capacity, uint32_t empty_key, uint32_t empty_value, clc_map* out)
+{
+    if (ctx == nullptr || out == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null argument");
+    *out = nullptr;
+    return guarded([&] {
+        const std::size_t slots = gbc::static_map_slots(std::max<std::size_t>(capacity, 2));
+        ctx->ctx->activate();
+        std::unique_ptr<clc_map_s> m(
+            new clc_map_s{ctx->ctx->resource, ctx->ctx->holder, nullptr, slots, empty_key, empty_value, 0});
+        m->slots = m->resource->allocate(slots * 8);
+        try {
+            gbc::static_map_clear(*ctx->ctx, m->slots, slots, empty_key, empty_value);
+        } catch (...) {
+            m->resource->deallocate(m->slots, slots * 8);
+            throw;
+        }
+        *out = m.release();
+    });
+}
+
+void clc_map_release(clc_map map)
+{
+    if (map == nullptr) return;
+    cudaSetDevice(map->holder->device);
+    map->resource->deallocate(map->slots, map->capacity * 8);
+    delete map;
+}
+
+clc_status clc_map_info(clc_map map, size_t* size, size_t* capacity, uint32_t* empty_key, uint32_t* empty_value)
+{
+    if (map == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null map");
+    if (size != nullptr) *size = map->size;
+    if (capacity != nullptr) *capacity = map->capacity;
+    if (empty_key != nullptr) *empty_key = map->empty_key;
+    if (empty_value != nullptr) *empty_value = map->empty_value;
+    return fail(CLC_SUCCESS, "");
+}
+
+clc_status clc_map_clear(clc_context ctx, clc_map map)
+{
+    return guarded([&] {
+        require(ctx != nullptr && map != nullptr, "clc: null argument");
+        require(map->holder->device == ctx->ctx->device, "clc: map belongs to another device");
+        gbc::static_map_clear(*ctx->ctx, map->slots, map->capacity, map->empty_key, map->empty_value);
+        map->size = 0;
+    });
+}
+
+clc_status clc_map_insert_raw(clc_context ctx, clc_map map, const uint32_t* keys, const uint32_t* values, size_t n,
+                              size_t* inserted)
+{
+    if (inserted != nullptr) *inserted = 0;
+    return guarded([&] {
+        require(ctx != nullptr && map != nullptr, "clc: null argument");
+        require(map->holder->device == ctx->ctx->device, "clc: map belongs to another device");
+        std::size_t not_placed = 0;
+        const std::size_t added = gbc::static_map_insert(*ctx->ctx, map->slots, map->capacity, map->empty_key,
+                                                         map->empty_value, keys, values, n, not_placed);
+        map->size += added;
+        if (inserted != nullptr) *inserted = added;
+        if (not_placed != 0)
+            throw std::overflow_error("static_map::insert: table is full (" + std::to_string(not_placed) +
+                                      " keys not inserted)");
+    });
+}
+
+clc_status clc_map_insert(clc_context ctx, clc_map map, clc_buffer keys, clc_buffer values, size_t n,
+                          size_t* inserted)
+{
+    if (keys == nullptr || values == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null buffer");
+    if (n > keys->bytes / 4 || n > values->bytes / 4)
+        return fail(CLC_ERROR_INVALID_ARGUMENT, "static_map::insert: n out of range");
+    return clc_map_insert_raw(ctx, map, static_cast<const uint32_t*>(keys->ptr), static_cast<const uint32_t*>(values->ptr),
+                              n, inserted);
+}
+
+clc_status clc_map_find_raw(clc_context ctx, clc_map map, const uint32_t* keys, size_t n, uint32_t* values)
+{
+    return guarded([&] {
+        require(ctx != nullptr && map != nullptr, "clc: null argument");
+        require(map->holder->device == ctx->ctx->device, "clc: map belongs to another device");
+        gbc::static_map_find(*ctx->ctx, map->slots, map->capacity, map->empty_key, map->empty_value, keys, n, values);
+    });
+}
+
+clc_status clc_map_find(clc_context ctx, clc_map map, clc_buffer keys, size_t n, clc_buffer values)
+{
+    if (keys == nullptr || values == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null buffer");
+    if (n > keys->bytes / 4 || n > values->bytes / 4)
+        return fail(CLC_ERROR_INVALID_ARGUMENT, "static_map::find: output too small");
+    return clc_map_find_raw(ctx, map, static_cast<const uint32_t*>(keys->ptr), n, static_cast<uint32_t*>(values->ptr));
+}
+
+clc_status clc_map_contains_raw(clc_context ctx, clc_map map, const uint32_t* keys, size_t n, uint8_t* found)
+{
+    return guarded([&] {
+        require(ctx != nullptr && map != nullptr, "clc: null argument");
+        require(map->holder->device == ctx->ctx->device, "clc: map belongs to another device");
+        gbc::static_map_contains(*ctx->ctx, map->slots, map->capacity, map->empty_key, keys, n, found);
+    });
+}
+
+clc_status clc_map_contains(clc_context ctx, clc_map map, clc_buffer keys, size_t n, clc_buffer found)
+{
+    if (keys == nullptr || found == nullptr) return fail(CLC_ERROR_INVALID_ARGUMENT, "clc: null buffer");
+    if (n > keys->bytes / 4 || n > found->bytes)
+        return fail(CLC_ERROR_INVALID_ARGUMENT, "static_map::contains: output too small");
+    return clc_map_contains_raw(ctx, map, static_cast<const uint32_t*>(keys->ptr), n, static_cast<uint8_t*>(found->ptr));
+}
+
+clc_status clc_map_slots(clc_context ctx, clc_map map, clc_buffer slot_keys, clc_buffer slot_values)
+{
+    return guarded([&] {
+        require(ctx != nullptr && map != nullptr, "clc: null argument");
+        require(slot_keys == nullptr || slot_keys->bytes >= map->capacity * 4, "clc: slot key buffer too small");
+        require(slot_values == nullptr || slot_values->bytes >= map->capacity * 4, "clc: slot value buffer too small");
+        gbc::static_map_unzip(*ctx->ctx, map->slots, map->capacity,
+                              slot_keys ? static_cast<uint32_t*>(slot_keys->ptr) : nullptr,
+                              slot_values ? static_cast<uint32_t*>(slot_values->ptr) : nullptr);
     });
 }
 

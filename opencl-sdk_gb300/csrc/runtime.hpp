@@ -262,6 +262,34 @@ void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const u
                    void* keys_out, unsigned long long* sums_out, uint32_t* counts_out, uint32_t* hist,
                    uint32_t* num_runs_device);
 
+//! Bitpack compression of n uint32 (the reference's chunk format, see
+//! bitpack.cu): analyzes and scans, then asks make_output for a device
+//! buffer of the exact compressed size in words, packs into it and returns
+//! that size. Synchronises once (to learn the size).
+std::size_t bitpack_compress(device_context& ctx, const uint32_t* in, std::size_t n, std::size_t chunk, bool delta,
+                             const std::function<uint32_t*(std::size_t)>& make_output);
+//! Decodes n elements of compressed data (`words` words) into out. Asynchronous.
+void bitpack_decompress(device_context& ctx, const uint32_t* data, std::size_t words, std::size_t n,
+                        std::size_t chunk, bool delta, uint32_t* out);
+//! Upper bound of the compressed size in words (3 per chunk + n).
+std::size_t bitpack_words_bound(std::size_t n, std::size_t chunk);
+
+//! static_map (static_map.cu): slots are `capacity` 64-bit words (key low,
+//! value high); capacity is a power of two from static_map_slots.
+std::size_t static_map_slots(std::size_t capacity);
+void static_map_clear(device_context& ctx, void* slots, std::size_t capacity, uint32_t empty_key,
+                      uint32_t empty_value);
+//! Blocks; returns the keys newly inserted, the keys it could not place in not_placed.
+std::size_t static_map_insert(device_context& ctx, void* slots, std::size_t capacity, uint32_t empty_key,
+                              uint32_t empty_value, const uint32_t* keys, const uint32_t* values, std::size_t n,
+                              std::size_t& not_placed);
+void static_map_find(device_context& ctx, const void* slots, std::size_t capacity, uint32_t empty_key,
+                     uint32_t empty_value, const uint32_t* keys, std::size_t n, uint32_t* out);
+void static_map_contains(device_context& ctx, const void* slots, std::size_t capacity, uint32_t empty_key,
+                         const uint32_t* keys, std::size_t n, uint8_t* out);
+void static_map_unzip(device_context& ctx, const void* slots, std::size_t capacity, uint32_t* keys,
+                      uint32_t* values);
+
 //! Launches one scan tile whose predecessor never publishes (the failure
 //! path of the bounded look-back wait); the next finish() reports it.
 void selftest_lookback_timeout(device_context& ctx);

@@ -195,10 +195,30 @@ _PROTOS = {
     "clc_context_stream": (_vp, [_vp]),
     "clc_context_memory_stats": (_i, [_vp, C.POINTER(MemoryStats)]),
     "clc_context_release_cache": (_i, [_vp]),
+    "clc_context_arena_info": (_i, [_vp, C.POINTER(_sz), C.POINTER(_sz), C.POINTER(_sz), C.POINTER(_sz)]),
     "clc_sort_keys_raw": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _sz, _i]),
     "clc_scan_raw": (_i, [_vp, _vp, _vp, _sz, _i, _cp, _cp, _i, _vp]),
     "clc_histogram_even_raw": (_i, [_vp, _vp, _sz, _i, _vp, _sz, C.c_double, C.c_double]),
     "clc_reduce_raw": (_i, [_vp, _vp, _sz, _i, _cp, _cp, _vp, _vp]),
+    "clc_bitpack_words_bound": (_sz, [_sz, _sz]),
+    "clc_bitpack_compress": (_i, [_vp, _vp, _sz, _sz, _i, C.POINTER(_vp), C.POINTER(_sz)]),
+    "clc_bitpack_decompress": (_i, [_vp, _vp, _sz, _sz, _i, _vp]),
+    "clc_bitpack_compress_raw": (_i, [_vp, _vp, _sz, _sz, _i, _vp, _sz, C.POINTER(_sz)]),
+    "clc_bitpack_decompress_raw": (_i, [_vp, _vp, _sz, _sz, _sz, _i, _vp]),
+    "clc_bitpack_serialize": (_i, [_vp, _vp, _sz, _sz, _i, _vp, _sz, C.POINTER(_sz)]),
+    "clc_bitpack_deserialize": (_i, [_vp, _vp, _sz, C.POINTER(_vp), C.POINTER(_sz), C.POINTER(_sz),
+                                     C.POINTER(_i)]),
+    "clc_map_create": (_i, [_vp, _sz, C.c_uint32, C.c_uint32, C.POINTER(_vp)]),
+    "clc_map_release": (None, [_vp]),
+    "clc_map_info": (_i, [_vp, C.POINTER(_sz), C.POINTER(_sz), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "clc_map_clear": (_i, [_vp, _vp]),
+    "clc_map_insert": (_i, [_vp, _vp, _vp, _vp, _sz, C.POINTER(_sz)]),
+    "clc_map_find": (_i, [_vp, _vp, _vp, _sz, _vp]),
+    "clc_map_contains": (_i, [_vp, _vp, _vp, _sz, _vp]),
+    "clc_map_slots": (_i, [_vp, _vp, _vp, _vp]),
+    "clc_map_insert_raw": (_i, [_vp, _vp, _vp, _vp, _sz, C.POINTER(_sz)]),
+    "clc_map_find_raw": (_i, [_vp, _vp, _vp, _sz, _vp]),
+    "clc_map_contains_raw": (_i, [_vp, _vp, _vp, _sz, _vp]),
     "clc_scan_i32_noalloc": (_i, [_vp, _vp, _sz, _i, _vp]),
     "clc_scan_i32_noalloc_status": (_i, [_vp]),
     "clc_selftest_noalloc_timeout": (_i, [_vp, _sz, _vp]),
@@ -280,6 +300,12 @@ class Context:
         s = MemoryStats()
         _raise_for(lib.clc_context_memory_stats(self.handle, C.byref(s)))
         return s
+
+    def arena_info(self) -> dict:
+        """held_bytes, slabs, slab_allocations, slab_releases of the context's arena."""
+        v = [C.c_size_t() for _ in range(4)]
+        _raise_for(lib.clc_context_arena_info(self.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("held_bytes", "slabs", "slab_allocations", "slab_releases"), (x.value for x in v)))
 
     def release_cache(self) -> None:
         _raise_for(lib.clc_context_release_cache(self.handle))
@@ -753,3 +779,154 @@ def reduce_by_key_raw(ctx: Context, keys: int, key_dtype, values: int, n: int, k
                                          C.c_void_p(hist16 or None), C.byref(runs) if want_count else None))
     return runs.value if want_count else None
 
+
+# ---- bitpack compression (Compression.hpp) ----------------------------------
+
+class CompressedBuffer:
+    """compressed_buffer: the device words of the reference's chunk format
+    (3 header words per chunk, then the packed words) and how to read them."""
+
+    def __init__(self, data: DeviceBuffer, num_elements: int, chunk_size: int, delta: bool):
+        self.data = data
+        self.num_elements = int(num_elements)
+        self.chunk_size = int(chunk_size)
+        self.delta = bool(delta)
+
+    def num_chunks(self) -> int:
+        return 0 if self.chunk_size == 0 else (self.num_elements + self.chunk_size - 1) // self.chunk_size
+
+    def compressed_bytes(self) -> int:
+        return self.data.nbytes
+
+    def uncompressed_bytes(self) -> int:
+        return 4 * self.num_elements
+
+    def serialize(self) -> bytes:
+        needed = C.c_size_t(0)
+        _raise_for(lib.clc_bitpack_serialize(self.data.ctx.handle, self.data.handle, self.num_elements,
+                                             self.chunk_size, int(self.delta), None, 0, C.byref(needed)))
+        blob = (C.c_ubyte * needed.value)()
+        _raise_for(lib.clc_bitpack_serialize(self.data.ctx.handle, self.data.handle, self.num_elements,
+                                             self.chunk_size, int(self.delta), blob, needed.value, C.byref(needed)))
+        return bytes(blob)
+
+    @classmethod
+    def deserialize(cls, ctx: Context, blob: bytes) -> "CompressedBuffer":
+        h, n, chunk, delta = C.c_void_p(), C.c_size_t(), C.c_size_t(), C.c_int()
+        buf = (C.c_ubyte * len(blob)).from_buffer_copy(blob) if blob else (C.c_ubyte * 1)()
+        _raise_for(lib.clc_bitpack_deserialize(ctx.handle, buf, len(blob), C.byref(h), C.byref(n), C.byref(chunk),
+                                               C.byref(delta)))
+        words = lib.clc_buffer_size(h) // 4
+        return cls(DeviceBuffer(ctx, words, np.uint32, _handle=h), n.value, chunk.value, bool(delta.value))
+
+
+def compress_bitpack(ctx: Context, inp: DeviceBuffer, delta: bool = False, chunk_size: int = 2048) -> CompressedBuffer:
+    h, words = C.c_void_p(), C.c_size_t()
+    _raise_for(lib.clc_bitpack_compress(ctx.handle, inp.handle, inp.size, chunk_size, int(delta), C.byref(h),
+                                        C.byref(words)))
+    return CompressedBuffer(DeviceBuffer(ctx, words.value, np.uint32, _handle=h), inp.size, chunk_size, delta)
+
+
+def decompress_bitpack(ctx: Context, comp: CompressedBuffer, out: DeviceBuffer) -> None:
+    if out.size < comp.num_elements:
+        raise InvalidArgumentError(ERROR_INVALID_ARGUMENT, "decompress_bitpack: output too small", 0)
+    _raise_for(lib.clc_bitpack_decompress(ctx.handle, comp.data.handle, comp.num_elements, comp.chunk_size,
+                                          int(comp.delta), out.handle))
+
+
+def bitpack_words_bound(n: int, chunk_size: int = 2048) -> int:
+    return lib.clc_bitpack_words_bound(n, chunk_size)
+
+
+def compress_bitpack_raw(ctx: Context, inp: int, n: int, out: int, capacity_words: int, delta: bool = False,
+                         chunk_size: int = 2048) -> int:
+    words = C.c_size_t()
+    _raise_for(lib.clc_bitpack_compress_raw(ctx.handle, C.c_void_p(inp), n, chunk_size, int(delta), C.c_void_p(out),
+                                            capacity_words, C.byref(words)))
+    return words.value
+
+
+def decompress_bitpack_raw(ctx: Context, data: int, words: int, n: int, out: int, delta: bool = False,
+                           chunk_size: int = 2048) -> None:
+    _raise_for(lib.clc_bitpack_decompress_raw(ctx.handle, C.c_void_p(data), words, n, chunk_size, int(delta),
+                                              C.c_void_p(out)))
+
+
+# ---- static_map (HashMap.hpp) ----------------------------------------------
+
+class StaticMap:
+    """static_map: fixed-capacity uint32 -> uint32 hash map (linear probing,
+    MurmurHash3 finalizer); insert keeps a key's first value and raises
+    OutOfMemoryError ("table is full") when keys cannot be placed."""
+
+    def __init__(self, ctx: Context, capacity: int, empty_key: int = 0xFFFFFFFF, empty_value: int = 0xFFFFFFFF):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _raise_for(lib.clc_map_create(ctx.handle, capacity, empty_key, empty_value, C.byref(h)))
+        self.handle = h
+
+    def _info(self):
+        size, cap, ek, ev = C.c_size_t(), C.c_size_t(), C.c_uint32(), C.c_uint32()
+        _raise_for(lib.clc_map_info(self.handle, C.byref(size), C.byref(cap), C.byref(ek), C.byref(ev)))
+        return size.value, cap.value, ek.value, ev.value
+
+    def size(self) -> int:
+        return self._info()[0]
+
+    def capacity(self) -> int:
+        return self._info()[1]
+
+    def empty_key(self) -> int:
+        return self._info()[2]
+
+    def empty_value(self) -> int:
+        return self._info()[3]
+
+    def load_factor(self) -> float:
+        s, c, _, _ = self._info()
+        return s / c
+
+    def insert(self, keys: DeviceBuffer, values: DeviceBuffer, n: int | None = None) -> int:
+        n = keys.size if n is None else n
+        added = C.c_size_t()
+        _raise_for(lib.clc_map_insert(self.ctx.handle, self.handle, keys.handle, values.handle, n, C.byref(added)))
+        return added.value
+
+    def find(self, keys: DeviceBuffer, values: DeviceBuffer) -> None:
+        _raise_for(lib.clc_map_find(self.ctx.handle, self.handle, keys.handle, keys.size, values.handle))
+
+    def contains(self, keys: DeviceBuffer, found: DeviceBuffer) -> None:
+        _raise_for(lib.clc_map_contains(self.ctx.handle, self.handle, keys.handle, keys.size, found.handle))
+
+    def clear(self) -> None:
+        _raise_for(lib.clc_map_clear(self.ctx.handle, self.handle))
+
+    def slots(self):
+        """(slot keys, slot values) as host arrays."""
+        cap = self.capacity()
+        k, v = DeviceBuffer(self.ctx, cap, np.uint32), DeviceBuffer(self.ctx, cap, np.uint32)
+        _raise_for(lib.clc_map_slots(self.ctx.handle, self.handle, k.handle, v.handle))
+        return k.to_host(), v.to_host()
+
+    def insert_raw(self, keys: int, values: int, n: int) -> int:
+        added = C.c_size_t()
+        _raise_for(lib.clc_map_insert_raw(self.ctx.handle, self.handle, C.c_void_p(keys), C.c_void_p(values), n,
+                                          C.byref(added)))
+        return added.value
+
+    def find_raw(self, keys: int, n: int, values: int) -> None:
+        _raise_for(lib.clc_map_find_raw(self.ctx.handle, self.handle, C.c_void_p(keys), n, C.c_void_p(values)))
+
+    def contains_raw(self, keys: int, n: int, found: int) -> None:
+        _raise_for(lib.clc_map_contains_raw(self.ctx.handle, self.handle, C.c_void_p(keys), n, C.c_void_p(found)))
+
+    def release(self) -> None:
+        if self.handle:
+            lib.clc_map_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass

@@ -543,3 +543,104 @@ std::size_t orc_std_reduce_by_key(const void* keys, int key_bytes, const uint32_
     return r;
 }
 }
+
+// ---- bitpack compression (restated from lib/src/Compute/Compression.cpp) ----
+// Chunk format of Compression.cpp:19-24, 88-106: for every chunk of `chunk`
+// elements three words {base, width, offset of the packed words relative to
+// the packed area}, then the packed area; a chunk's values are stored as
+// (encoded value - base) in `width` bits each, least significant bits first,
+// element j at bit j * width of the chunk's words. width = 32 - clz(max -
+// min) of the encoded values (0 when they are all equal). Delta mode encodes
+// zigzag(x[i] - x[i-1]) with wrapping 32-bit arithmetic and x[-1] = 0
+// (Compression.cpp:30-37); decoding undoes the zigzag and takes a wrapping
+// inclusive prefix sum over the whole array (Compression.cpp:121-123, 178).
+namespace {
+uint32_t bp_encode(const uint32_t* in, std::size_t i, int delta)
+{
+    if (!delta) return in[i];
+    const uint32_t d = in[i] - (i > 0 ? in[i - 1] : 0u);
+    return (d << 1) ^ (0u - (d >> 31));
+}
+}  // namespace
+
+extern "C" {
+// Writes the compressed words into out (when not null); returns their count.
+std::size_t orc_bitpack_compress(const uint32_t* in, std::size_t n, std::size_t chunk, int delta, uint32_t* out)
+{
+    if (n == 0) return 0;
+    const std::size_t chunks = (n + chunk - 1) / chunk;
+    std::vector<uint32_t> base(chunks), width(chunks), offset(chunks);
+    std::size_t packed = 0;
+    for (std::size_t c = 0; c < chunks; ++c) {
+        const std::size_t b = c * chunk, e = std::min(n, b + chunk);
+        uint32_t lo = 0xFFFFFFFFu, hi = 0;
+        for (std::size_t i = b; i < e; ++i) {
+            const uint32_t v = bp_encode(in, i, delta);
+            lo = std::min(lo, v);
+            hi = std::max(hi, v);
+        }
+        const uint32_t range = hi - lo;
+        uint32_t w = 0;
+        while (w < 32 && (range >> w) != 0) ++w;  // 32 - clz(range), 0 for range 0
+        base[c] = lo;
+        width[c] = w;
+        offset[c] = (uint32_t)packed;
+        packed += ((e - b) * w + 31) / 32;
+    }
+    const std::size_t total = 3 * chunks + packed;
+    if (out == nullptr) return total;
+    std::fill(out, out + total, 0u);
+    for (std::size_t c = 0; c < chunks; ++c) {
+        out[3 * c] = base[c];
+        out[3 * c + 1] = width[c];
+        out[3 * c + 2] = offset[c];
+        const uint32_t w = width[c];
+        if (w == 0) continue;
+        uint32_t* words = out + 3 * chunks + offset[c];
+        const std::size_t b = c * chunk, e = std::min(n, b + chunk);
+        for (std::size_t i = b; i < e; ++i) {
+            const uint64_t v = bp_encode(in, i, delta) - base[c];
+            const uint64_t bit = (uint64_t)(i - b) * w;
+            const uint64_t bits = v << (bit & 31);
+            words[bit >> 5] |= (uint32_t)bits;
+            if ((bit & 31) + w > 32) words[(bit >> 5) + 1] |= (uint32_t)(bits >> 32);
+        }
+    }
+    return total;
+}
+
+// Decodes n elements from data (`words` words); returns 0, or -1 when a
+// chunk header points outside the data.
+int orc_bitpack_decompress(const uint32_t* data, std::size_t words, std::size_t n, std::size_t chunk, int delta,
+                           uint32_t* out)
+{
+    if (n == 0) return 0;
+    const std::size_t chunks = (n + chunk - 1) / chunk;
+    if (words < 3 * chunks) return -1;
+    const std::size_t packed = words - 3 * chunks;
+    uint32_t run = 0;
+    for (std::size_t c = 0; c < chunks; ++c) {
+        const uint32_t base = data[3 * c], w = data[3 * c + 1], off = data[3 * c + 2];
+        const std::size_t b = c * chunk, e = std::min(n, b + chunk);
+        if (w > 32 || (uint64_t)off + ((e - b) * (uint64_t)w + 31) / 32 > packed) return -1;
+        const uint32_t* p = data + 3 * chunks + off;
+        for (std::size_t i = b; i < e; ++i) {
+            uint32_t v = 0;
+            if (w != 0) {
+                const uint64_t bit = (uint64_t)(i - b) * w;
+                uint64_t both = p[bit >> 5];
+                if ((bit & 31) + w > 32) both |= (uint64_t)p[(bit >> 5) + 1] << 32;
+                v = (uint32_t)((both >> (bit & 31)) & (w == 32 ? 0xFFFFFFFFull : ((1ull << w) - 1)));
+            }
+            v += base;
+            if (delta) {
+                run += (v >> 1) ^ (0u - (v & 1u));
+                out[i] = run;
+            } else {
+                out[i] = v;
+            }
+        }
+    }
+    return 0;
+}
+}  // extern "C"

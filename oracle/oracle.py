@@ -65,6 +65,10 @@ def lib():
         L.orc_mlp_grad.argtypes = [vp, vp, C.c_float, vp, vp, sz, i, vp, C.POINTER(C.c_double)]
         L.orc_std_reduce_by_key.argtypes = [vp, i, vp, sz, vp, vp, vp, vp]
         L.orc_std_reduce_by_key.restype = sz
+        L.orc_bitpack_compress.argtypes = [vp, sz, sz, i, vp]
+        L.orc_bitpack_compress.restype = sz
+        L.orc_bitpack_decompress.argtypes = [vp, sz, sz, sz, i, vp]
+        L.orc_bitpack_decompress.restype = i
         _lib = L
     return _lib
 
@@ -245,3 +249,82 @@ def zipf_keys(n: int, s: float, distinct: int, seed: int) -> np.ndarray:
     z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
     z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
     return z ^ (z >> np.uint64(31))
+
+
+# ---- bitpack compression (the reference's chunk format) ---------------------
+
+def bitpack_compress(x: np.ndarray, chunk: int = 2048, delta: bool = False) -> np.ndarray:
+    """The compressed words (3 header words per chunk, then the packed area)."""
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    words = lib().orc_bitpack_compress(_p(x), x.size, chunk, int(delta), None)
+    out = np.zeros(words, dtype=np.uint32)
+    if words:
+        lib().orc_bitpack_compress(_p(x), x.size, chunk, int(delta), _p(out))
+    return out
+
+
+def bitpack_decompress(words: np.ndarray, n: int, chunk: int = 2048, delta: bool = False) -> np.ndarray:
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    out = np.zeros(n, dtype=np.uint32)
+    if lib().orc_bitpack_decompress(_p(w), w.size, n, chunk, int(delta), _p(out)) != 0:
+        raise ValueError("bitpack: corrupt chunk header")
+    return out
+
+
+def bitpack_recipes():
+    """The reference's compression test inputs (lib/test/Compute/main.cpp:
+    392-402) for every size of main.cpp:54, in its order: slowly increasing
+    timestamps (one mt19937(11) shared across the sizes: t += rng() % 50 from
+    1,700,000,000), small-range values (uniform [0, 300] + 5,000,000, seed
+    n + 4) and incompressible noise (uniform 32-bit, seed n + 5)."""
+    sizes = [0, 1, 7, 255, 256, 1000, 4097, 100003, 1 << 20]
+    ts_all = mt19937_words(11, sum(sizes))
+    out, used = [], 0
+    for n in sizes:
+        steps = (ts_all[used:used + n] % 50).astype(np.uint64)
+        used += n
+        ts = ((1700000000 + np.cumsum(steps)) & 0xFFFFFFFF).astype(np.uint32)
+        small = (random_uints(n, 300, n + 4).astype(np.uint64) + 5000000).astype(np.uint32)
+        noise = random_uints(n, 0xFFFFFFFF, n + 5)
+        out.append((n, ts, small, noise))
+    return out
+
+
+def mt19937_words(seed: int, count: int) -> np.ndarray:
+    """The first `count` raw outputs of std::mt19937(seed)."""
+    return random_uints(count, 0xFFFFFFFF, seed)
+
+
+# ---- static_map -----------------------------------------------------------------
+
+def murmur_fmix32(k: np.ndarray) -> np.ndarray:
+    """The MurmurHash3 32-bit finalizer (the hash of the reference's
+    static_map, DeviceHeaders.cpp:136-145)."""
+    k = np.asarray(k, dtype=np.uint64) & 0xFFFFFFFF
+    k ^= k >> 16
+    k = (k * 0x85EBCA6B) & 0xFFFFFFFF
+    k ^= k >> 13
+    k = (k * 0xC2B2AE35) & 0xFFFFFFFF
+    k ^= k >> 16
+    return k.astype(np.uint32)
+
+
+def linear_probe_table_ok(slot_keys: np.ndarray, empty_key: int) -> bool:
+    """True when every stored key is reachable by the linear-probing walk the
+    reference's find makes (HashMap.cpp:45-58): from slot hash(key) & mask
+    forward, no empty slot before the key's slot."""
+    cap = slot_keys.size
+    mask = cap - 1
+    occupied = slot_keys != empty_key
+    idx = np.nonzero(occupied)[0]
+    home = murmur_fmix32(slot_keys[idx]).astype(np.int64) & mask
+    # an empty slot on the cyclic walk home .. idx breaks the chain
+    empty_pos = np.nonzero(~occupied)[0]
+    if empty_pos.size == 0:
+        return True
+    dist = (idx - home) % cap
+    # nearest empty slot at or after home, cyclically
+    nxt = np.searchsorted(empty_pos, home)
+    nearest = np.where(nxt < empty_pos.size, empty_pos[np.minimum(nxt, empty_pos.size - 1)], empty_pos[0] + cap)
+    gap = nearest - home
+    return bool(np.all(dist < gap))

@@ -1,15 +1,19 @@
 // A C++ caller of the reference's algorithm API, compiled against
 // include/gbcompute/compute.hpp and linked with libgbcompute.so. It runs the
 // algorithm cases of the reference's C++ test (lib/test/Compute/
-// main.cpp:184-336) with the same recipes -- sizes {0, 1, 7, 255, 256, 1000,
+// main.cpp:184-451) with the same recipes -- sizes {0, 1, 7, 255, 256, 1000,
 // 4097, 100003, 2^20}, mt19937(seed) + uniform_int_distribution inputs,
 // seeds n (reduce), n+1 (scan), n+2 (sort), n+3 (copy_if and histogram) --
 // and checks every result on the host: sequence/transform/fill, reduce with
 // plus/min/max, inclusive/exclusive/in-place scans with the right projection
 // and the max operator, sort_by_key against std::stable_sort, stability with
 // many duplicates, signed and float keys (descending, with -0 and +-inf),
-// copy_if and a 10-bin histogram; plus the facade's exceptions. Exit status
-// = failed checks.
+// copy_if and a 10-bin histogram; the static_map and bitpack compression
+// cases of main.cpp:337-451 (a 200,000-key map, finds of present and absent
+// keys, the overflow of a 4-slot table; three inputs x delta x two chunk
+// sizes round-tripped through compression and serialization, the > 4x ratio
+// of delta-coded timestamps, a rejected blob); plus the facade's
+// exceptions. Exit status = failed checks.
 #include <gbcompute/compute.hpp>
 
 #include <algorithm>
@@ -233,6 +237,91 @@ void select_and_histogram(cc::compute_context& ctx)
     }
 }
 
+void hash_map(cc::compute_context& ctx)
+{
+    const std::size_t n = 200000;
+    std::vector<cl_uint> keys(n), values(n);
+    for (std::size_t i = 0; i < n; ++i) {
+        keys[i] = cl_uint(uint64_t(i) * 2654435761u % 0xFFFFFFF0u);  // distinct
+        values[i] = cl_uint(i);
+    }
+    cc::static_map map(ctx, n * 2);
+    auto kb = cc::device_buffer<cl_uint>::from_host(ctx, keys);
+    auto vb = cc::device_buffer<cl_uint>::from_host(ctx, values);
+    EXPECT(map.insert(kb, vb) == n);
+    EXPECT(map.size() == n);
+    EXPECT(map.insert(kb, vb) == 0);  // present keys keep their values
+    std::vector<cl_uint> q(keys.begin(), keys.begin() + 1000);
+    for (cl_uint i = 0; i < 1000; ++i) q.push_back(0xFFFFFFF1u + i % 14);
+    auto qb = cc::device_buffer<cl_uint>::from_host(ctx, q);
+    cc::device_buffer<cl_uint> found(ctx, q.size());
+    map.find(qb, found);
+    const auto fv = found.to_host(ctx);
+    bool ok = true;
+    for (std::size_t i = 0; i < q.size(); ++i) ok = ok && fv[i] == (i < 1000 ? values[i] : map.empty_value());
+    EXPECT(ok);
+    cc::device_buffer<cl_uchar> present(ctx, q.size());
+    map.contains(qb, present);
+    const auto pv = present.to_host(ctx);
+    EXPECT(std::count(pv.begin(), pv.end(), cl_uchar(1)) == 1000);
+    EXPECT(map.slot_keys().size() == map.capacity());
+
+    cc::static_map tiny(ctx, 4);
+    bool overflow = false;
+    try {
+        tiny.insert(kb, vb, 10);
+    } catch (const std::overflow_error&) {
+        overflow = true;
+    }
+    EXPECT(overflow && tiny.size() == 4);
+    tiny.clear();
+    EXPECT(tiny.size() == 0);
+}
+
+void compression(cc::compute_context& ctx)
+{
+    std::mt19937 ticks(11);
+    for (std::size_t n : kSizes) {
+        std::vector<cl_uint> ts(n);  // slowly increasing timestamps
+        cl_uint t = 1700000000u;
+        for (auto& x : ts) x = t += ticks() % 50;
+        auto small = uniform(n, 300, unsigned(n) + 4);  // small range
+        for (auto& x : small) x += 5000000u;
+        const auto noise = uniform(n, 0xFFFFFFFFu, unsigned(n) + 5);  // incompressible
+        const std::vector<cl_uint>* inputs[] = {&ts, &small, &noise};
+        for (const auto* input : inputs)
+            for (bool delta : {false, true})
+                for (std::size_t chunk : {std::size_t(256), std::size_t(2048)}) {
+                    auto in = cc::device_buffer<cl_uint>::from_host(ctx, *input);
+                    cc::bitpack_options opt;
+                    opt.delta = delta;
+                    opt.chunk_size = chunk;
+                    const auto packed = cc::compress_bitpack(ctx, in, opt);
+                    cc::device_buffer<cl_uint> out(ctx, n);
+                    cc::decompress_bitpack(ctx, packed, out);
+                    EXPECT(out.to_host(ctx) == *input);
+                    const auto restored = cc::compressed_buffer::deserialize(ctx, packed.serialize(ctx));
+                    cc::device_buffer<cl_uint> out2(ctx, n);
+                    cc::decompress_bitpack(ctx, restored, out2);
+                    EXPECT(out2.to_host(ctx) == *input);
+                }
+        if (n == (std::size_t(1) << 20)) {
+            auto in = cc::device_buffer<cl_uint>::from_host(ctx, ts);
+            cc::bitpack_options opt;
+            opt.delta = true;
+            const auto packed = cc::compress_bitpack(ctx, in, opt);
+            EXPECT(double(packed.uncompressed_bytes()) / double(packed.compressed_bytes()) > 4.0);
+        }
+    }
+    bool rejected = false;
+    try {
+        cc::compressed_buffer::deserialize(ctx, std::vector<unsigned char>(64, 0));
+    } catch (const std::invalid_argument&) {
+        rejected = true;
+    }
+    EXPECT(rejected);
+}
+
 void facade_errors(cc::compute_context& ctx)
 {
     cc::device_buffer<cl_uint> small(ctx, 10), large(ctx, 20);
@@ -279,6 +368,8 @@ int main()
         scans(ctx);
         sorts(ctx);
         select_and_histogram(ctx);
+        hash_map(ctx);
+        compression(ctx);
         facade_errors(ctx);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "unexpected exception: %s\n", e.what());

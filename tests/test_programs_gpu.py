@@ -1,7 +1,8 @@
 """Programs written against the public headers, run on the GPU: a C99 caller
 of the C interface doing what the reference's capi.c checks for the hot path
 (lib/test/Compute/capi.c:52-157), and a C++ caller of the cl::compute facade
-running the algorithm cases of the reference's main.cpp:184-336 with its own
+running the algorithm, static_map and compression cases of the reference's
+main.cpp:184-451 with its own
 host checks. Each exits with its number of failed checks."""
 import subprocess
 

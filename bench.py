@@ -226,6 +226,94 @@ def cpu_baseline_block(seconds: float = 12.0) -> dict:
             "std_floor": cs.std_floor(STD_FLOOR_N)}
 
 
+def cpu_table() -> dict:
+    """The CPU side of every configuration on this host, on bounded samples:
+    A = the oracle's restatement of the reference's algorithm on all host
+    threads, B = the std:: floor on one thread (std::stable_sort, a sequential
+    scan, a histogram loop). Each entry names its sample; rates are in the
+    configuration's unit."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    threads = oracle.hardware_threads()
+    rng = np.random.default_rng(7)
+    out = {"threads": threads}
+
+    def best(fn, reps=3):
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    # 1: keys-only u32 sort, 2^24 (and the std floor on the same keys)
+    k24 = rng.integers(0, 2**32, size=1 << 24, dtype=np.uint32)
+    out["keys_sort_u32_n2^24"] = {
+        "A_gkeys": (1 << 24) / best(lambda: oracle.ref_radix_sort(k24, threads=threads)) / 1e9,
+        "B_gkeys": (1 << 24) / best(lambda: oracle.std_sort(k24), 1) / 1e9, "sample": "full 2^24"}
+    # 2a: key-value u32 sort 2^28: A on the full workload, B on 2^24 pairs
+    cs = CpuSort(N_MAIN)
+    out["kv_sort_u32_n2^28"] = {"A_gkeys": N_MAIN / min(cs.time_lsd() for _ in range(2)) / 1e9,
+                                "B_gkeys": cs.std_floor(STD_FLOOR_N)["value"],
+                                "sample": "A: full 2^28; B: 2^24 pairs"}
+    del cs
+    # 2b: exclusive scan of 2^30 int32 in [-1000, 1000]
+    x = rng.integers(-1000, 1001, size=1 << 30, dtype=np.int32)
+    out["exclusive_scan_i32_n2^30"] = {
+        "A_gelem": (1 << 30) / best(lambda: oracle.ref_scan(x, exclusive=True, threads=threads), 2) / 1e9,
+        "B_gelem": (1 << 30) / best(lambda: oracle.std_scan(x, exclusive=True), 1) / 1e9, "sample": "full 2^30"}
+    del x
+    # 2c: 256-bin histogram of 2^30 bytes
+    u8 = rng.integers(0, 256, size=1 << 30, dtype=np.uint8)
+    out["histogram256_u8_n2^30"] = {
+        "A_gelem": (1 << 30) / best(lambda: oracle.histogram_even(u8, 256, 0.0, 256.0, threads=threads), 2) / 1e9,
+        "B_gelem": (1 << 30) / best(lambda: oracle.histogram_even(u8, 256, 0.0, 256.0, threads=1), 1) / 1e9,
+        "sample": "full 2^30"}
+    del u8
+    # 3: segmented sort of u64 keys + u32 values, lognormal segments: per-segment
+    # std::stable_sort (A: segments spread over all threads, B: one thread) on
+    # the first 20,000 of the 200,000 segments
+    lens = np.clip(np.rint(np.random.default_rng(4).lognormal(np.log(256), 2.0, 200000)), 1, 1 << 20).astype(np.int64)
+    sl = lens[:20000]
+    off = np.zeros(sl.size + 1, dtype=np.int64)
+    np.cumsum(sl, out=off[1:])
+    m = int(off[-1])
+    sk = rng.integers(0, 2**63, size=m, dtype=np.uint64)
+    sv = np.arange(m, dtype=np.uint32)
+    off32 = off.astype(np.uint32)
+    out["segmented_sort_u64kv_lognormal"] = {
+        "A_gkeys": m / best(lambda: oracle.std_segmented_sort(sk, off32, sv, threads=threads), 2) / 1e9,
+        "B_gkeys": m / best(lambda: oracle.std_segmented_sort(sk, off32, sv, threads=1), 1) / 1e9,
+        "sample": f"the first 20,000 segments ({m} pairs)"}
+    del sk, sv
+    # 4: the learned-CDF configuration's float keys: the reference's sort (A,
+    # 2^28) and std::stable_sort (B, 2^24); the reference has no learned sort
+    fk = rng.standard_normal(1 << 28).astype(np.float32) * 300.0
+    out["float_sort_f32_n2^28"] = {
+        "A_gkeys": (1 << 28) / best(lambda: oracle.ref_radix_sort(fk, threads=threads), 1) / 1e9,
+        "B_gkeys": (1 << 24) / best(lambda: oracle.std_sort(fk[: 1 << 24]), 1) / 1e9,
+        "sample": "A: 2^28 normal floats (the sort does not depend on the distribution); B: 2^24 of them"}
+    del fk
+    # 5: sort -> reduce_by_key -> 65,536-bin histogram of u64 Zipf keys: the
+    # reference's sort of 2^26 pairs (A) and std::stable_sort of 2^24 (B), then
+    # the single-thread run-length reduction and histogram of the sorted keys
+    zk = oracle.zipf_keys(1 << 26, 1.1, 1 << 24, 6)
+    zv = rng.integers(0, 1 << 16, size=zk.size, dtype=np.uint32)
+    ta = best(lambda: oracle.ref_radix_sort(zk, zv, threads=threads), 1)
+    skz, svz = oracle.ref_radix_sort(zk, zv, threads=threads)
+    tr = best(lambda: oracle.std_reduce_by_key(skz, svz), 1)
+    tb = best(lambda: oracle.std_sort(zk[: 1 << 24], zv[: 1 << 24]), 1)
+    out["pipeline_u64_zipf"] = {"A_gkeys": zk.size / (ta + tr) / 1e9,
+                                "B_gkeys": (1 << 24) / (tb + tr * (1 << 24) / zk.size) / 1e9,
+                                "sample": "A: 2^26 pairs (reference sort + reduce_by_key/histogram); "
+                                          "B: 2^24 pairs (std::stable_sort + the same reduction, scaled)"}
+    return out
+
+
 def run_reference(args) -> None:
     """The reference arm: the reference's sort algorithm on the host cores,
     on the headline workload itself (2^28 uniform uint32 keys with their
@@ -269,8 +357,13 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="only the headline workload")
     ap.add_argument("--n", type=int, default=N_MAIN, help="keys per step (default 2^28)")
+    ap.add_argument("--cpu-table", action="store_true",
+                    help="print the CPU baselines of every configuration (host only) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.cpu_table:
+        print(json.dumps(cpu_table()), flush=True)
+        return
 
     if args.impl == "reference":
         run_reference(args)
@@ -676,13 +769,16 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ms_plain, prof_p = timed(lambda: gbc.sort_raw(ctx, lk.data_ptr(), pout.data_ptr(), np.float32, n), steps, warmup,
                              ("sort.",))
     stats = []
+    arena0 = ctx.arena_info()
     ms_learn, prof_l = timed(lambda: stats.append(gbc.sort_learned(ctx, lk.data_ptr(), lout.data_ptr(), np.float32, n)),
                              steps, warmup, ("learned.", "segsort.", "sort."))
+    arena1 = ctx.arena_info()
     ok = bool(torch.equal(lout, pout))
     st = stats[-1].as_dict() if stats else {}
     entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 36 * n, ok, prof_l,
           {"plain_sort_ms": ms_plain, "plain_sort_gkeys": n / (ms_plain * 1e-3) / 1e9,
            "speedup_vs_plain": ms_plain / ms_learn, "stats": st,
+           "arena": {"before": arena0, "after": arena1},
            "note": "includes sampling, the sample sort and the MLP fit; bytes = 36n: count (key read, u16 bucket "
                    "write), group level (key + bucket read and write), bucket level (key + bucket read, key "
                    "write), finish (read + write); oversized buckets move more"})
@@ -717,6 +813,14 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     # the autotuner picks the one-CTA capacity for this size / segment-length class
     seg_cap, _ = gbc.autotune_segmented_sort(ctx, sk.data_ptr(), sko.data_ptr(), np.uint64, total, off_d.data_ptr(),
                                              lens.size, sv.data_ptr(), svo.data_ptr(), repetitions=1)
+
+    def size_class(v):
+        k = 0
+        while (1 << k) < v and k < 63:
+            k += 1
+        return f"2^{k}"
+
+    msd_cap = ctx.tuning_get(f"segsort:u64kv:{size_class(total)}:avg{size_class(total // lens.size)}:msd")
     batch()
     ctx.finish()
     graph = gbc.capture(ctx, batch)
@@ -729,8 +833,31 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
                                                          svo.data_ptr() + 4 * int(offs[i]))
                                             for i in range(sample_segs)], 1, 1, ("sort.",))
     per_array_est_ms = ms_per_array_sample * lens.size / sample_segs
+    # the plain LSD over the whole concatenation: a stable sort of all pairs by
+    # key (the library's plain sort, values = positions), then a stable sort
+    # of the segment ids in that order (plain sort, values = positions), then
+    # the gathers of keys and values into segment-major order
+    seg_of = torch.repeat_interleave(torch.arange(lens.size, device="cuda", dtype=torch.int32),
+                                     torch.from_numpy(lens).cuda())
+    pos = torch.arange(total, dtype=torch.int32, device="cuda")
+    k1, p1 = torch.empty_like(sk), torch.empty_like(pos)
+    s2, p2 = torch.empty_like(pos), torch.empty_like(pos)
+    plain_k, plain_v = torch.empty_like(sk), torch.empty_like(sv)
+
+    def plain_lsd():
+        gbc.sort_raw(ctx, sk.data_ptr(), k1.data_ptr(), np.uint64, total, pos.data_ptr(), p1.data_ptr())
+        with torch.cuda.stream(stream):
+            torch.index_select(seg_of, 0, p1, out=s2)
+        gbc.sort_raw(ctx, s2.data_ptr(), s2.data_ptr(), np.uint32, total, pos.data_ptr(), p2.data_ptr())
+        with torch.cuda.stream(stream):
+            torch.index_select(k1, 0, p2, out=plain_k)
+            torch.index_select(sv, 0, torch.index_select(p1, 0, p2), out=plain_v)
+
+    ms_plain_lsd, _ = timed(plain_lsd, max(3, steps // 2), warmup, ("sort.",))
     graph.launch()
     ctx.finish()
+    plain_ok = bool(torch.equal(plain_k, sko)) and bool(torch.equal(plain_v, svo))
+    del seg_of, pos, k1, p1, s2, p2, plain_k, plain_v
     # parity: each segment sorted stably (torch's stable sort on (segment, key) as the independent check)
     seg_id = torch.repeat_interleave(torch.arange(lens.size, device="cuda"), torch.from_numpy(lens).cuda())
     ku = sk.view(torch.int64) ^ (-2**63)  # unsigned order as signed
@@ -750,10 +877,15 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     seg_bytes = 24 * (total - large_keys) + (8 + 8 * 24) * large_keys + 8 * total
     entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, seg_bytes, ok, prof_s,
           {"segments": int(lens.size), "total_keys": total, "graph": True, "autotuned_cta_capacity": seg_cap,
+           "autotuned_msd_capacity": msd_cap,
            "keys_in_large_segments": large_keys,
            "includes": "segmented sort (u64 keys + u32 values) and segmented exclusive int32 scan",
            "plain_per_array_estimate_ms": per_array_est_ms,
            "speedup_vs_per_array": per_array_est_ms / ms_seg,
+           "plain_lsd_ms": ms_plain_lsd, "plain_lsd_bitexact": plain_ok,
+           "speedup_vs_plain_lsd": ms_plain_lsd / ms_seg,
+           "plain_lsd": "stable plain sort of all pairs by key, stable plain sort of the segment ids in that order, "
+                        "gathers of keys and values (sort only: the segmented figure also includes the scan)",
            "hbm_frac_one_pass": 32 * total / (ms_seg * 1e-3) / 1e9 / peak,
            "note": "bytes: 24 B/pair in segments <= the one-CTA capacity, 200 B/pair above it (8 B histogram "
                    "+ 8 digit passes x 24 B), 8 B/elem scan; hbm_frac_one_pass counts 32 B/key"})
@@ -850,6 +982,64 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ok = bool(torch.equal(torch.bincount(u8.to(torch.int64), minlength=256).to(torch.int32), hist))
     entry("histogram256_u8_n2^30", m, "Gelem/s", ms, m, ok, prof)
     del u8
+    torch.cuda.empty_cache()
+
+    # bitpack compression of 2^28 slowly increasing uint32 timestamps (the
+    # reference's compression recipe: t += uniform [0, 50)), delta coding,
+    # 2,048-element chunks; then decompression of the result
+    nb = n
+    steps_ = torch.randint(0, 50, (nb,), dtype=torch.int64, device="cuda", generator=gen)
+    ts = ((1700000000 + torch.cumsum(steps_, 0)) & 0xFFFFFFFF).to(torch.int32)
+    del steps_
+    cap = gbc.bitpack_words_bound(nb, 2048)
+    packed = torch.empty(cap, dtype=torch.int32, device="cuda")
+    back = torch.empty_like(ts)
+    words = []
+    ms_c, prof_c = timed(lambda: words.append(gbc.compress_bitpack_raw(ctx, ts.data_ptr(), nb, packed.data_ptr(), cap,
+                                                                      delta=True)), steps, warmup, ("bitpack.", "scan."))
+    w = words[-1]
+    ms_d, prof_d = timed(lambda: gbc.decompress_bitpack_raw(ctx, packed.data_ptr(), w, nb, back.data_ptr(), delta=True),
+                         steps, warmup, ("bitpack.", "scan."))
+    ok = bool(torch.equal(back, ts))
+    # compress reads the input twice (analyze, pack) and writes the packed
+    # words; decompress reads them, writes the deltas and scans them in place
+    entry("bitpack_compress_u32_timestamps_n2^28", nb, "Gelem/s", ms_c, 8 * nb + 4 * w, ok, prof_c,
+          {"ratio": 4 * nb / (4 * w), "words": int(w), "delta": True, "chunk": 2048,
+           "note": "includes the blocking read of the compressed size"})
+    entry("bitpack_decompress_u32_timestamps_n2^28", nb, "Gelem/s", ms_d, 4 * w + 4 * nb + 8 * nb, ok, prof_d,
+          {"note": "unpack (packed words in, deltas out) + in-place inclusive scan"})
+    del ts, packed, back
+    torch.cuda.empty_cache()
+
+    # static_map: 2^26 distinct keys (odd multiples of a constant: distinct
+    # 32-bit values) inserted into 2^27 slots (load factor 0.5), then found
+    # (every other query absent)
+    nm = 1 << 26
+    mk = ((torch.arange(nm, dtype=torch.int64, device="cuda") * 2654435761 + 12345) & 0xFFFFFFFE).to(torch.int32)
+    mv = torch.arange(nm, dtype=torch.int32, device="cuda")
+    qk = mk.clone()
+    qk[1::2] |= 1  # odd keys were never inserted
+    got = torch.empty_like(mv)
+    smap = gbc.StaticMap(ctx, 2 * nm)
+    added = []
+
+    def map_insert():
+        smap.clear()
+        added.append(smap.insert_raw(mk.data_ptr(), mv.data_ptr(), nm))
+
+    ms_i, prof_i = timed(map_insert, steps, warmup, ("static_map.",))
+    ms_f, prof_f = timed(lambda: smap.find_raw(qk.data_ptr(), nm, got.data_ptr()), steps, warmup, ("static_map.",))
+    want = torch.where(torch.arange(nm, device="cuda") % 2 == 0, mv, torch.full_like(mv, -1))
+    ok = added[-1] == nm and bool(torch.equal(got, want))
+    # random 8-byte slot accesses move whole 32-byte sectors: insert reads 8 B
+    # of input per key and touches >= one sector; find reads 4 B and one sector
+    entry("static_map_insert_u32_n2^26", nm, "Gkeys/s", ms_i, nm * (8 + 32) + 2 * nm * 8, ok, prof_i,
+          {"load_factor": 0.5, "note": "includes clearing the 2^27 slots and the blocking count read; bytes: "
+                                       "input + one 32-byte sector per key + the slot clear"})
+    entry("static_map_find_u32_n2^26", nm, "Gkeys/s", ms_f, nm * (4 + 32 + 4), ok, prof_f,
+          {"present_fraction": 0.5, "note": "bytes: query + one 32-byte sector + result per key"})
+    smap.release()
+    del mk, mv, qk, got, want
     torch.cuda.empty_cache()
     return out
 

@@ -111,12 +111,31 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
     for (int c : r.candidates) {
         seg_options o;
         o.cta_cap = c;
+        o.msd_cap = 0;
         r.ms.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);
         }));
     }
     pick(r, ctx);
+    // Then, with that capacity, the MSD route's bucket capacity (0: off),
+    // stored under its own key.
+    autotune_result m;
+    m.key = segsort_msd_tuning_key(key_bytes, kv, n, num_segments);
+    m.candidates.push_back(0);
+    for (int c = 2048; c < cap; c += 1024) m.candidates.push_back(c);
+    m.candidates.push_back(cap);
+    for (int c : m.candidates) {
+        seg_options o;
+        o.cta_cap = r.best;
+        o.msd_cap = c;
+        m.ms.push_back(ev.time(ctx, repetitions, [&] {
+            segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
+                           false, o);
+        }));
+    }
+    pick(m, ctx);
+    r.best_ms = std::min(r.best_ms, m.best_ms);
     return r;
 }
 

@@ -16,6 +16,8 @@
 // look back like the scan. The tile holding a run's last element knows the
 // run's index (c - 1), sum, start and hence length, and writes the run.
 #include <cstring>
+#include <string>
+#include <type_traits>
 
 #include "device_common.cuh"
 #include "runtime.hpp"
@@ -25,9 +27,7 @@ namespace gbc {
 namespace {
 
 using dev::FULL_MASK;
-constexpr int THREADS = 256;
 constexpr int ITEMS = 16;
-constexpr int TILE = THREADS * ITEMS;
 constexpr int LB_PER_LANE = 4;  // look-back window: 32 x 4 tiles per round trip
 constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
 constexpr uint64_t TAG_MASK = (1ull << 29) - 1;
@@ -121,8 +121,13 @@ template <typename K> struct RbkArgs {
     int* err;
 };
 
-template <typename K> __global__ void __launch_bounds__(THREADS, 2) k_reduce_by_key(RbkArgs<K> a)
+// THREADS: 256, 128 or 64 per CTA. Every CTA's warps wait at a barrier while
+// its first warp looks back, so smaller CTAs (more of them per SM, each with
+// its own look-back in flight) keep more warps busy; registers cap any shape
+// at 16 warps per SM.
+template <typename K, int THREADS> __global__ void __launch_bounds__(THREADS) k_reduce_by_key(RbkArgs<K> a)
 {
+    constexpr int TILE = THREADS * ITEMS;
     __shared__ State s_warp[THREADS / 32];
     __shared__ State s_prefix;
     __shared__ uint32_t s_tile;
@@ -318,11 +323,17 @@ void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const u
     }
     if (keys == nullptr || vals == nullptr || keys_out == nullptr || sums_out == nullptr)
         throw std::invalid_argument("reduce_by_key: null argument");
-    const uint32_t num_tiles = (uint32_t)((n + TILE - 1) / TILE);
+    // CTA size from the tuning table (variant 0: 256 threads, 1: 128, 2: 64)
+    launch_shape shape;
+    const std::string key = std::string("reduce_by_key:") + (key_bytes == 4 ? "u32" : "u64");
+    const int threads = ctx.tuning.lookup(key, shape) ? (shape.variant == 1 ? 128 : shape.variant == 2 ? 64 : 256)
+                                                      : 128;
+    const uint32_t num_tiles = (uint32_t)((n + (std::size_t)threads * ITEMS - 1) / ((std::size_t)threads * ITEMS));
     unsigned char* ctl = ctx.d_small + 512;
     check_cuda(cudaMemsetAsync(ctl, 0, 64, ctx.stream), "cudaMemsetAsync");
-    auto launch = [&](auto tag) {
+    auto launch = [&](auto tag, auto threads_tag) {
         using K = decltype(tag);
+        constexpr int THREADS = decltype(threads_tag)::value;
         RbkArgs<K> a;
         a.keys = static_cast<const K*>(keys);
         a.vals = vals;
@@ -338,15 +349,20 @@ void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const u
         a.tile_ctr = reinterpret_cast<uint32_t*>(ctl);
         a.err = ctx.d_error;
         int per_sm = 0;
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, &k_reduce_by_key<K>, THREADS, 0),
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, &k_reduce_by_key<K, THREADS>, THREADS, 0),
                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         const int grid = (int)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * std::max(per_sm, 1));
         kernel_timer kt(ctx, "reduce_by_key.lookback");
-        k_reduce_by_key<K><<<grid, THREADS, 0, ctx.stream>>>(a);
+        k_reduce_by_key<K, THREADS><<<grid, THREADS, 0, ctx.stream>>>(a);
         check_cuda(cudaGetLastError(), "reduce_by_key launch");
     };
-    if (key_bytes == 4) launch(uint32_t{});
-    else launch(uint64_t{});
+    auto by_threads = [&](auto tag) {
+        if (threads == 64) launch(tag, std::integral_constant<int, 64>{});
+        else if (threads == 128) launch(tag, std::integral_constant<int, 128>{});
+        else launch(tag, std::integral_constant<int, 256>{});
+    };
+    if (key_bytes == 4) by_threads(uint32_t{});
+    else by_threads(uint64_t{});
 }
 
 }  // namespace gbc

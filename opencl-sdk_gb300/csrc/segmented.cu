@@ -64,7 +64,9 @@ struct SegControl {
     uint32_t large_tiles;             // tiles of all large segments
     uint32_t warp_next, cta_next;     // work queue heads
     uint32_t tile_ctr[8];
-    uint32_t pad[6];
+    uint32_t n_sub_warp, n_sub_cta;      // sub-bucket list lengths (MSD route)
+    uint32_t sub_warp_next, sub_cta_next;
+    uint32_t pad[2];
 };
 
 template <typename K> struct SegArgs {
@@ -91,7 +93,18 @@ template <typename K> struct SegArgs {
     uint64_t* ring;
     uint64_t seq0;
     int* err;
+    // MSD route of large segments: route[j] = the digit position of large
+    // segment j's single pass, or NO_ROUTE for the full LSD passes; its
+    // sub-buckets (begin, end pairs) are finished from alt into out by the
+    // warp (<= WARP_CAP) and CTA (<= sub_cap) sorts.
+    uint8_t* route;
+    uint32_t* sub_warp_list;
+    uint32_t* sub_cta_list;
+    uint32_t max_sub;
+    uint32_t sub_cap;
 };
+
+constexpr uint8_t NO_ROUTE = 0xFF;
 
 // ---------------------------------------------------------------------------
 // Classification
@@ -170,9 +183,14 @@ template <int GW> __device__ __forceinline__ void group_sync()
     else __syncthreads();
 }
 
+// Ranking is by shared-memory peer masks, as in the digit pass: each lane ORs
+// its bit into its digit's mask word (GW x 256 words in `masks`, all zero
+// between rows), reads the word back (its peers) and the warp's count of the
+// digit so far; the lowest peer stores the new count and clears the mask.
+// (__match_any_sync ranked the same rows about 1.7x slower on this GPU.)
 template <typename K, bool HAS_V, int GW>
 __device__ void group_sort(K* k0, K* k1, uint32_t* v0, uint32_t* v1, uint32_t* rd, uint32_t* hist,
-                           uint32_t* scratch, uint32_t len, dev::KeyXform<K> xf, int gw, int lane,
+                           uint32_t* masks, uint32_t* scratch, uint32_t len, dev::KeyXform<K> xf, int gw, int lane,
                            bool& in_k1)
 {
     constexpr int P = Traits<K>::PASSES;
@@ -203,20 +221,25 @@ __device__ void group_sort(K* k0, K* k1, uint32_t* v0, uint32_t* v1, uint32_t* r
         for (int i = (GW > 1 ? threadIdx.x : lane); i < GW * RADIX; i += GW * 32) hist[i] = 0;
         group_sync<GW>();
         uint32_t* wh = hist + gw * RADIX;
+        uint32_t* wm = masks + gw * RADIX;
+        const uint32_t lt = dev::lanemask_lt();
         for (uint32_t r = 0; r < rows; ++r) {
             const uint32_t idx = gw * chunk + r * 32 + lane;
             const bool valid = idx < len;
+            // padding ranks in bin 255 (counted there, never placed)
             const uint32_t d = valid ? (uint32_t)(xf(k0[idx]) >> shift) & 0xFFu : 0xFFu;
-            const uint32_t peers = __match_any_sync(FULL_MASK, d);
-            const int leader = 31 - __clz(peers);
-            uint32_t before = 0;
-            if (lane == leader) {
-                before = wh[d];
-                wh[d] = before + __popc(peers);
-            }
-            before = __shfl_sync(FULL_MASK, before, leader);
-            if (valid) rd[idx] = ((before + __popc(peers & dev::lanemask_lt())) << 8) | d;
+            atomicOr(&wm[d], 1u << lane);
             __syncwarp();
+            const uint32_t peers = wm[d];
+            const uint32_t before = wh[d];
+            __syncwarp();
+            const uint32_t lower = peers & lt;
+            if (lower == 0) {
+                wh[d] = before + __popc(peers);
+                wm[d] = 0;
+            }
+            __syncwarp();
+            if (valid) rd[idx] = ((before + __popc(lower)) << 8) | d;
         }
         group_sync<GW>();
         // digit starts and per-warp offsets
@@ -268,12 +291,15 @@ __device__ void group_sort(K* k0, K* k1, uint32_t* v0, uint32_t* v1, uint32_t* r
     }
 }
 
-template <typename K, bool HAS_V>
+// SUB: the MSD route's sub-buckets (begin, end pairs, read from alt) instead
+// of whole segments (read from the input).
+template <typename K, bool HAS_V, bool SUB>
 __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr std::size_t per_warp = 2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + RADIX * 4;
+    constexpr std::size_t per_warp =
+        2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
     unsigned char* base = smem + warp * per_warp;
     K* k0 = reinterpret_cast<K*>(base);
     K* k1 = k0 + WARP_CAP;
@@ -281,21 +307,33 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
     uint32_t* v1 = v0 + (HAS_V ? WARP_CAP : 0);
     uint32_t* rd = v1 + (HAS_V ? WARP_CAP : 0);
     uint32_t* hist = rd + WARP_CAP;
-    const uint32_t total = a.ctl->n_warp;
+    uint32_t* masks = hist + RADIX;
+    for (int i = lane; i < RADIX; i += 32) masks[i] = 0;
+    __syncwarp();
+    const uint32_t total = SUB ? min(a.ctl->n_sub_warp, a.max_sub) : a.ctl->n_warp;
+    const K* src_k = SUB ? a.alt_k : a.in_k;
+    const uint32_t* src_v = SUB ? a.alt_v : a.in_v;
     for (;;) {
         uint32_t w = 0;
-        if (lane == 0) w = atomicAdd(&a.ctl->warp_next, 1u);
+        if (lane == 0) w = atomicAdd(SUB ? &a.ctl->sub_warp_next : &a.ctl->warp_next, 1u);
         w = __shfl_sync(FULL_MASK, w, 0);
         if (w >= total) break;
-        const uint32_t s = a.warp_list[w];
-        const uint32_t b = a.off[s], len = a.off[s + 1] - b;
+        uint32_t b, len;
+        if (SUB) {
+            b = a.sub_warp_list[2 * w];
+            len = a.sub_warp_list[2 * w + 1] - b;
+        } else {
+            const uint32_t s = a.warp_list[w];
+            b = a.off[s];
+            len = a.off[s + 1] - b;
+        }
         for (uint32_t i = lane; i < len; i += 32) {
-            k0[i] = a.in_k[b + i];
-            if (HAS_V) v0[i] = a.in_v[b + i];
+            k0[i] = src_k[b + i];
+            if (HAS_V) v0[i] = src_v[b + i];
         }
         __syncwarp();
         bool flipped = false;
-        if (len > 1) group_sort<K, HAS_V, 1>(k0, k1, v0, v1, rd, hist, nullptr, len, a.xf, 0, lane, flipped);
+        if (len > 1) group_sort<K, HAS_V, 1>(k0, k1, v0, v1, rd, hist, masks, nullptr, len, a.xf, 0, lane, flipped);
         const K* rk = flipped ? k1 : k0;
         const uint32_t* rv = flipped ? v1 : v0;
         for (uint32_t i = lane; i < len; i += 32) {
@@ -306,35 +344,46 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
     }
 }
 
-template <typename K, bool HAS_V>
+template <typename K, bool HAS_V, bool SUB>
 __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t cap = a.cta_cap;
+    const uint32_t cap = SUB ? a.sub_cap : a.cta_cap;
     K* k0 = reinterpret_cast<K*>(smem);
     K* k1 = k0 + cap;
     uint32_t* v0 = reinterpret_cast<uint32_t*>(k1 + cap);
     uint32_t* v1 = v0 + (HAS_V ? cap : 0);
     uint32_t* rd = v1 + (HAS_V ? cap : 0);
     uint32_t* hist = rd + cap;
+    uint32_t* masks = hist + SMALL_WARPS * RADIX;
+    for (int i = threadIdx.x; i < SMALL_WARPS * RADIX; i += SMALL_THREADS) masks[i] = 0;
     __shared__ uint32_t scratch[64 + 8];
     __shared__ uint32_t s_work;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t total = a.ctl->n_cta;
+    const uint32_t total = SUB ? min(a.ctl->n_sub_cta, a.max_sub) : a.ctl->n_cta;
+    const K* src_k = SUB ? a.alt_k : a.in_k;
+    const uint32_t* src_v = SUB ? a.alt_v : a.in_v;
     for (;;) {
-        if (threadIdx.x == 0) s_work = atomicAdd(&a.ctl->cta_next, 1u);
+        if (threadIdx.x == 0) s_work = atomicAdd(SUB ? &a.ctl->sub_cta_next : &a.ctl->cta_next, 1u);
         __syncthreads();
         const uint32_t w = s_work;
         if (w >= total) break;
-        const uint32_t s = a.cta_list[w];
-        const uint32_t b = a.off[s], len = a.off[s + 1] - b;
+        uint32_t b, len;
+        if (SUB) {
+            b = a.sub_cta_list[2 * w];
+            len = a.sub_cta_list[2 * w + 1] - b;
+        } else {
+            const uint32_t s = a.cta_list[w];
+            b = a.off[s];
+            len = a.off[s + 1] - b;
+        }
         for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
-            k0[i] = a.in_k[b + i];
-            if (HAS_V) v0[i] = a.in_v[b + i];
+            k0[i] = src_k[b + i];
+            if (HAS_V) v0[i] = src_v[b + i];
         }
         __syncthreads();
         bool flipped = false;
-        group_sort<K, HAS_V, SMALL_WARPS>(k0, k1, v0, v1, rd, hist, scratch, len, a.xf, warp, lane, flipped);
+        group_sort<K, HAS_V, SMALL_WARPS>(k0, k1, v0, v1, rd, hist, masks, scratch, len, a.xf, warp, lane, flipped);
         const K* rk = flipped ? k1 : k0;
         const uint32_t* rv = flipped ? v1 : v0;
         for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
@@ -432,6 +481,63 @@ template <typename K> __global__ void __launch_bounds__(256) k_seg_large_starts(
     }
 }
 
+// Per large segment (one CTA, thread d = bin d): the highest digit position
+// that varies inside the segment (its bins are not all in one) and, when
+// every bin there holds at most sub_cap keys, the MSD route: one pass on that
+// digit partitions the segment into its bins (stable), which become
+// sub-buckets for the warp and CTA sorts; else the full LSD passes. The bin
+// starts in seg_hist are absolute, from k_seg_large_starts.
+template <typename K> __global__ void __launch_bounds__(256) k_seg_route(SegArgs<K> a)
+{
+    constexpr int P = Traits<K>::PASSES;
+    __shared__ uint32_t s_max[8];
+    __shared__ int s_top;
+    const uint32_t nl = min(a.ctl->n_large, a.max_large);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t j = blockIdx.x; j < nl; j += gridDim.x) {
+        const uint32_t s = a.large_list[j];
+        const uint32_t segb = a.off[s], sege = a.off[s + 1], len = sege - segb;
+        auto bin_size = [&](int p, uint32_t d) {
+            const uint32_t* row = a.seg_hist + ((size_t)j * P + p) * RADIX;
+            return (d == RADIX - 1 ? sege : row[d + 1]) - row[d];
+        };
+        if (threadIdx.x == 0) s_top = -1;
+        __syncthreads();
+        for (int p = P - 1; p >= 0; --p) {
+            // a position varies when no bin holds the whole segment
+            const bool whole = bin_size(p, threadIdx.x) == len;
+            if (__syncthreads_or(whole) == 0) {
+                if (threadIdx.x == 0) s_top = p;
+                break;
+            }
+        }
+        __syncthreads();
+        const int top = s_top;
+        uint32_t size = top >= 0 ? bin_size(top, threadIdx.x) : len;
+        uint32_t m = size;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL_MASK, m, o));
+        if (lane == 0) s_max[warp] = m;
+        __syncthreads();
+        uint32_t biggest = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) biggest = max(biggest, s_max[w]);
+        const bool msd = top >= 0 && biggest <= a.sub_cap;
+        if (threadIdx.x == 0) a.route[j] = msd ? (uint8_t)top : NO_ROUTE;
+        if (msd && size != 0) {  // a one-key bucket goes to the warp sort, which copies it
+            const uint32_t b = a.seg_hist[((size_t)j * P + top) * RADIX + threadIdx.x];
+            if (size <= (uint32_t)WARP_CAP) {
+                const uint32_t q = atomicAdd(&a.ctl->n_sub_warp, 1u);
+                if (q < a.max_sub) a.sub_warp_list[2 * q] = b, a.sub_warp_list[2 * q + 1] = b + size;
+            } else {
+                const uint32_t q = atomicAdd(&a.ctl->n_sub_cta, 1u);
+                if (q < a.max_sub) a.sub_cta_list[2 * q] = b, a.sub_cta_list[2 * q + 1] = b + size;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // One digit pass over every large segment's tiles (cf. onesweep::k_pass2:
 // shared-memory peer-mask ranking, place offsets folded into the per-warp
 // counts, a look-back reading LBW predecessors per round trip, which stops at
@@ -475,14 +581,18 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
         if (tid == 0) {
             s_tile = atomicAdd(&a.ctl->tile_ctr[slot], 1u);
             // L2 prefetch of the tile a grid further on in the tile sequence
+            // (from where this pass reads it, if it takes part)
             const uint32_t ahead = s_tile + gridDim.x;
             if (aligned_src && ahead < num_tiles) {
                 const uint32_t ja = a.tile_seg[ahead];
+                const uint8_t ra = a.route[ja];
                 const uint32_t sa = a.large_list[ja];
                 const uint32_t ba = a.off[sa] + (ahead - a.tile_begin[ja]) * TILE;
-                if (ba + TILE <= a.off[sa + 1] && (ba % (16 / sizeof(K))) == 0) {
-                    dev::prefetch_l2(src_k + ba, TILE * sizeof(K));
-                    if (HAS_V && (ba & 3) == 0) dev::prefetch_l2(src_v + ba, TILE * 4);
+                const K* pk = ra == NO_ROUTE ? src_k : a.in_k;
+                const uint32_t* pv = ra == NO_ROUTE ? src_v : a.in_v;
+                if ((ra == NO_ROUTE || ra == slot) && ba + TILE <= a.off[sa + 1] && (ba % (16 / sizeof(K))) == 0) {
+                    dev::prefetch_l2(pk + ba, TILE * sizeof(K));
+                    if (HAS_V && (ba & 3) == 0) dev::prefetch_l2(pv + ba, TILE * 4);
                 }
             }
         }
@@ -491,6 +601,19 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
         const uint32_t t = s_tile;
         if (t >= num_tiles) break;
         const uint32_t j = a.tile_seg[t];
+        // a segment on the MSD route takes part in its one pass only, reading
+        // the input and writing the scratch buffer (its sub-buckets are then
+        // finished from there); its tiles publish nothing in the other passes,
+        // and no tile of another segment looks back into it
+        const uint8_t rt = a.route[j];
+        if (rt != NO_ROUTE && rt != slot) {
+            __syncthreads();  // every thread has read s_tile before thread 0 takes the next tile
+            continue;
+        }
+        const K* tsrc_k = rt == NO_ROUTE ? src_k : a.in_k;
+        const uint32_t* tsrc_v = rt == NO_ROUTE ? src_v : a.in_v;
+        K* tdst_k = rt == NO_ROUTE ? dst_k : a.alt_k;
+        uint32_t* tdst_v = rt == NO_ROUTE ? dst_v : a.alt_v;
         const uint32_t s = a.large_list[j];
         const uint32_t segb = a.off[s], sege = a.off[s + 1];
         const uint32_t lt = t - a.tile_begin[j];
@@ -504,10 +627,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
         uint32_t val[HAS_V ? ITEMS : 1];
         if (valid == (uint32_t)TILE) {
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * 32];
+            for (int i = 0; i < ITEMS; ++i) key[i] = tsrc_k[wbase + i * 32];
             if (HAS_V) {
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) val[i] = src_v[wbase + i * 32];
+                for (int i = 0; i < ITEMS; ++i) val[i] = tsrc_v[wbase + i * 32];
             }
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
@@ -516,8 +639,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
             for (int i = 0; i < ITEMS; ++i) {
                 const uint32_t idx = wbase + i * 32;
                 const bool in = idx < sege;
-                key[i] = in ? src_k[idx] : K(0);
-                if (HAS_V) val[i] = in ? src_v[idx] : 0u;
+                key[i] = in ? tsrc_k[idx] : K(0);
+                if (HAS_V) val[i] = in ? tsrc_v[idx] : 0u;
                 rd[i] = in ? digit(key[i]) : 0xFFu;  // padding ranks last
             }
         }
@@ -626,8 +749,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 if (o[i] >= segb && o[i] < sege) {
-                    dst_k[o[i]] = key[i];
-                    if (HAS_V) dst_v[o[i]] = val[i];
+                    tdst_k[o[i]] = key[i];
+                    if (HAS_V) tdst_v[o[i]] = val[i];
                 }
             }
         } else {
@@ -635,8 +758,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
                 const K kk = s_keys[q];
                 const uint32_t o = s_bin_off[digit(kk)] + q;
                 if (o >= segb && o < sege) {
-                    dst_k[o] = kk;
-                    if (HAS_V) dst_v[o] = s_vals[q];
+                    tdst_k[o] = kk;
+                    if (HAS_V) tdst_v[o] = s_vals[q];
                 }
             }
         }
@@ -678,9 +801,9 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     using LS = LargeShape<K, HAS_V>;
     constexpr int TILE = LS::THREADS * LS::ITEMS;
     // Largest segment one CTA sorts in shared memory: two copies of keys (and
-    // values) plus a packed rank per element, and 8 KiB of warp histograms,
-    // must fit the 227 KiB opt-in (u32: 12 B/elem keys-only, 20 B/elem with
-    // values; u64: 20 and 28 B/elem).
+    // values) plus a packed rank per element, and 16 KiB of warp histograms
+    // and peer masks, must fit the 227 KiB opt-in (u32: 12 B/elem keys-only,
+    // 20 B/elem with values; u64: 20 and 28 B/elem).
     constexpr int MAX_CAP = sizeof(K) == 4 ? (HAS_V ? 10240 : 16384) : (HAS_V ? 7168 : 10240);
     const uint32_t cta_cap =
         (uint32_t)std::max<int>(WARP_CAP + 1, std::min<int>(opt.cta_cap > 0 ? opt.cta_cap : MAX_CAP, MAX_CAP));
@@ -694,7 +817,16 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     const bool maybe_large = n > cta_cap;
     temp_buffer alt_k(ctx.resource, maybe_large ? n * sizeof(K) : 0);
     temp_buffer alt_v(ctx.resource, maybe_large && HAS_V ? n * sizeof(uint32_t) : 0);
+    // MSD route: per large segment its pass (or none), and at most 256
+    // sub-buckets per large segment (never more than n)
+    const uint32_t msd_cap = opt.msd_cap <= 0 ? 0u : (uint32_t)std::max<int>(WARP_CAP + 1, std::min(opt.msd_cap, MAX_CAP));
+    const bool msd = maybe_large && msd_cap > 0;
+    const uint32_t max_sub = msd ? (uint32_t)std::min<std::size_t>((std::size_t)max_large * RADIX, n) : 0;
+    temp_buffer route(ctx.resource, maybe_large ? max_large : 0);
+    temp_buffer sub_lists(ctx.resource, (std::size_t)max_sub * 4 * sizeof(uint32_t));
     check_cuda(cudaMemsetAsync(ctl.get(), 0, sizeof(SegControl), ctx.stream), "cudaMemsetAsync");
+    if (maybe_large && !msd)
+        check_cuda(cudaMemsetAsync(route.get(), NO_ROUTE, max_large, ctx.stream), "cudaMemsetAsync");
 
     SegArgs<K> a;
     a.in_k = in_k;
@@ -721,6 +853,11 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     a.ring = ctx.lookback_ring;
     a.seq0 = maybe_large ? ctx.reserve_seq((uint64_t)P * max_tiles) : 0;
     a.err = ctx.d_error;
+    a.route = route.as<uint8_t>();
+    a.sub_warp_list = sub_lists.as<uint32_t>();
+    a.sub_cta_list = sub_lists.as<uint32_t>() + 2 * (std::size_t)max_sub;
+    a.max_sub = max_sub;
+    a.sub_cap = msd_cap;
 
     {
         kernel_timer kt(ctx, "segsort.classify");
@@ -735,9 +872,10 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
 
     {
         kernel_timer kt(ctx, "segsort.small_warp");
-        constexpr std::size_t per_warp = 2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + RADIX * 4;
+        constexpr std::size_t per_warp =
+            2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
         const std::size_t smem = per_warp * SMALL_WARPS;
-        auto kern = &k_seg_small_warp<K, HAS_V>;
+        auto kern = &k_seg_small_warp<K, HAS_V, false>;
         set_smem(kern, smem);
         const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
         kern<<<grid, SMALL_THREADS, smem, ctx.stream>>>(a);
@@ -745,8 +883,8 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     }
     {
         kernel_timer kt(ctx, "segsort.small_cta");
-        const std::size_t smem = (std::size_t)cta_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + SMALL_WARPS * RADIX * 4;
-        auto kern = &k_seg_small_cta<K, HAS_V>;
+        const std::size_t smem = (std::size_t)cta_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * SMALL_WARPS * RADIX * 4;
+        auto kern = &k_seg_small_cta<K, HAS_V, false>;
         set_smem(kern, smem);
         const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
         kern<<<grid, SMALL_THREADS, smem, ctx.stream>>>(a);
@@ -760,6 +898,10 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
         hk<<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
         k_seg_large_starts<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
         check_cuda(cudaGetLastError(), "segmented sort histogram launch");
+        if (msd) {
+            k_seg_route<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
+            check_cuda(cudaGetLastError(), "segmented sort route launch");
+        }
         auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS, LS::MINB, LS::LBW>;
         const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +
                                   (HAS_V ? (std::size_t)TILE * 4 : 0);
@@ -768,6 +910,21 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
         for (int s = 0; s < P; ++s) {
             pk<<<pgrid, LS::THREADS, psmem, aux>>>(a, s);
             check_cuda(cudaGetLastError(), "segmented sort pass launch");
+        }
+        if (msd) {
+            // the MSD route's sub-buckets: from the scratch buffer into the output
+            constexpr std::size_t per_warp =
+                2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
+            auto wk = &k_seg_small_warp<K, HAS_V, true>;
+            set_smem(wk, per_warp * SMALL_WARPS);
+            wk<<<ctx.sm_count * occupancy(wk, SMALL_THREADS, per_warp * SMALL_WARPS), SMALL_THREADS,
+                 per_warp * SMALL_WARPS, aux>>>(a);
+            const std::size_t csmem = (std::size_t)msd_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) +
+                                      2 * SMALL_WARPS * RADIX * 4;
+            auto ck = &k_seg_small_cta<K, HAS_V, true>;
+            set_smem(ck, csmem);
+            ck<<<ctx.sm_count * occupancy(ck, SMALL_THREADS, csmem), SMALL_THREADS, csmem, aux>>>(a);
+            check_cuda(cudaGetLastError(), "segmented sort sub-bucket launch");
         }
     }
     // Join.
@@ -780,6 +937,11 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
 uint32_t segsort_cta_cap(int key_bytes, bool has_values)
 {
     return key_bytes == 4 ? (has_values ? 10240u : 16384u) : (has_values ? 7168u : 10240u);
+}
+
+std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
+{
+    return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":msd";
 }
 
 std::string segsort_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
@@ -806,22 +968,29 @@ void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, in
     if (opt.skip != nullptr && (keys_in != keys_out || vals_in != vals_out))
         throw std::invalid_argument("segmented_sort: skipped segments need an in-place call");
     ctx.activate();
+    seg_options o = opt;
+    if (o.msd_cap < 0) {
+        launch_shape shape;
+        o.msd_cap = ctx.tuning.lookup(segsort_msd_tuning_key(key_bytes, vals_in != nullptr, n, num_segments), shape)
+                        ? shape.variant
+                        : 0;
+    }
     if (key_bytes == 4) {
         const auto xf = dev::make_xform<uint32_t>(key_kind, descending);
         if (vals_in)
             seg::run<uint32_t, true>(ctx, static_cast<const uint32_t*>(keys_in), static_cast<uint32_t*>(keys_out),
-                                     vals_in, vals_out, n, offsets, num_segments, xf, opt);
+                                     vals_in, vals_out, n, offsets, num_segments, xf, o);
         else
             seg::run<uint32_t, false>(ctx, static_cast<const uint32_t*>(keys_in), static_cast<uint32_t*>(keys_out),
-                                      nullptr, nullptr, n, offsets, num_segments, xf, opt);
+                                      nullptr, nullptr, n, offsets, num_segments, xf, o);
     } else {
         const auto xf = dev::make_xform<uint64_t>(key_kind, descending);
         if (vals_in)
             seg::run<uint64_t, true>(ctx, static_cast<const uint64_t*>(keys_in), static_cast<uint64_t*>(keys_out),
-                                     vals_in, vals_out, n, offsets, num_segments, xf, opt);
+                                     vals_in, vals_out, n, offsets, num_segments, xf, o);
         else
             seg::run<uint64_t, false>(ctx, static_cast<const uint64_t*>(keys_in), static_cast<uint64_t*>(keys_out),
-                                      nullptr, nullptr, n, offsets, num_segments, xf, opt);
+                                      nullptr, nullptr, n, offsets, num_segments, xf, o);
     }
 }
 

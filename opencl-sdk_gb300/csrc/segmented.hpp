@@ -14,6 +14,11 @@ struct seg_options {
     // device, one byte per segment or null: nonzero marks a segment already in
     // order (every key equal), left untouched; only for in-place calls
     const uint8_t* skip = nullptr;
+    // MSD route: a large segment whose highest varying digit splits it into
+    // buckets of at most msd_cap keys takes one pass on that digit, then the
+    // shared-memory sorts finish the buckets; 0: every large segment takes
+    // all digit passes; -1: the default (the tuning table's entry, else off)
+    int msd_cap = -1;
 };
 
 //! Sorts every segment [offsets[i], offsets[i+1]) independently and stably.
@@ -31,6 +36,8 @@ void segmented_scan(device_context& ctx, const void* in, void* out, std::size_t 
                     const void* identity, bool exclusive, const uint32_t* offsets, std::size_t num_segments);
 
 std::string segsort_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
+//! The tuning-table key of the MSD route's bucket capacity (0: off).
+std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
 
 //! Largest segment the segmented sort finishes in one CTA's shared memory.
 uint32_t segsort_cta_cap(int key_bytes, bool has_values);

@@ -124,3 +124,52 @@ def test_graph_capture_replays_segmented_sort_and_scan(ctx, gbc, orc):
         g2.launch()
         assert np.array_equal(k2o.to_host(), np.sort(keys[:100000]))
     g2.release()
+
+
+@pytest.mark.parametrize("key_dtype", [np.uint64, np.uint32, np.float32])
+@pytest.mark.parametrize("with_values", [True, False])
+def test_msd_and_lsd_routes_mixed(ctx, gbc, orc, key_dtype, with_values):
+    """Large segments go one of two ways: when the highest digit position
+    that varies inside the segment splits it into buckets that one CTA can
+    sort, one pass on that digit and a shared-memory sort per bucket (the MSD
+    route); otherwise every digit pass (the LSD route). One call mixes both,
+    plus segments whose varying digits lie low (small key ranges), a segment
+    of equal keys and small segments, and checks the result bit for bit."""
+    rng = np.random.default_rng(31)
+    lens = [200000, 150000, 90000, 60000, 40000, 5000, 300, 17, 70000, 120000]
+    off = offsets_from_lengths(lens)
+    n = int(off[-1])
+    bits = 64 if np.dtype(key_dtype).itemsize == 8 else 32
+    keys = rng.integers(0, 2**63, size=n, dtype=np.uint64)
+    if bits == 32:
+        keys &= np.uint64(0xFFFFFFFF)
+    b = [int(x) for x in off]
+    # segment 1: one dominant value of the top digit (a bucket of ~90% -> LSD)
+    seg = slice(b[1], b[2])
+    keys[seg] = np.where(rng.random(lens[1]) < 0.9, keys[seg] & np.uint64((1 << (bits - 8)) - 1), keys[seg])
+    # segment 2: keys below 2^20 (the top varying digit is low; buckets fit -> MSD there)
+    keys[b[2]:b[3]] &= np.uint64((1 << 20) - 1)
+    # segment 3: all keys equal (no digit varies -> LSD, every pass a copy)
+    keys[b[3]:b[4]] = keys[b[3]]
+    # segment 4: duplicates inside buckets (stability)
+    keys[b[4]:b[5]:3] = keys[b[4]]
+    # segment 9: two values only
+    keys[b[9]:b[10]] = np.where(rng.random(lens[9]) < 0.5, 5, 7).astype(np.uint64)
+    if np.dtype(key_dtype).kind == "f":
+        k = rng.standard_normal(n).astype(np.float32)
+        k[b[3]:b[4]] = 1.5
+        k[b[1]:b[2]] = np.where(rng.random(lens[1]) < 0.9, np.float32(2.0) + k[b[1]:b[2]] * 1e-6, k[b[1]:b[2]])
+        k[::97] = -0.0
+        keys = k
+    else:
+        keys = keys.astype(key_dtype)
+    vals = np.arange(n, dtype=np.uint32)
+    for descending in (False, True):
+        kb = gbc.DeviceBuffer.from_host(ctx, keys)
+        vb = gbc.DeviceBuffer.from_host(ctx, vals) if with_values else None
+        ob = gbc.DeviceBuffer.from_host(ctx, off)
+        gbc.segmented_sort(ctx, kb, ob, vb, descending=descending)
+        ek, ev = orc.std_segmented_sort(keys, off, vals if with_values else None, descending=descending)
+        assert np.array_equal(kb.to_host().view(np.uint8), ek.view(np.uint8))
+        if with_values:
+            assert np.array_equal(vb.to_host(), ev)

@@ -1,7 +1,7 @@
 """Profiling harness: runs one named workload a fixed number of times so that
 an ncu capture has a short, deterministic launch sequence.
 
-  python opencl-sdk_gb300/profile_cases.py CASE [--n N] [--iters K]
+  python profile_cases.py CASE [--n N] [--iters K]
 
 Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
 (u64 keys + u32 values), scan-i32 (exclusive, int64 total), reduce-i32,
@@ -11,7 +11,10 @@ n = total keys), rbk-u64 (reduce_by_key over sorted keys with runs, fused
 32.0f", uint -> float), transform2-u32 ("x + y"), learned-f32 (learned-CDF
 sort of float32 keys: 75% from 8 Gaussians with means in [-1e3, 1e3] and
 sigmas log-uniform in [1e-2, 1e2], 20% lognormal(0, 2), 5% copies of 1,000 of
-those values, shuffled). Inputs are seeded synthetic
+those values, shuffled), bitpack-u32 (delta-coded compression of slowly
+increasing timestamps, then decompression), map-u32 (static_map: clear,
+insert n distinct keys into 2n slots, find n keys of which half are
+absent). Inputs are seeded synthetic
 data generated on the device; every call goes through the C ABI on the
 library's stream.
 """
@@ -22,7 +25,7 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "opencl-sdk_gb300"))
 
 
 def main() -> None:
@@ -144,6 +147,31 @@ def main() -> None:
 
         def step():
             gbc.sort_learned(ctx, k.data_ptr(), ko.data_ptr(), np.float32, n)
+    elif args.case == "bitpack-u32":
+        # slowly increasing timestamps, delta coding, 2,048-element chunks:
+        # compress, then decompress the result
+        steps = torch.randint(0, 50, (n,), dtype=torch.int64, device="cuda", generator=g)
+        ts = ((1700000000 + torch.cumsum(steps, 0)) & 0xFFFFFFFF).to(torch.int32)
+        cap = gbc.bitpack_words_bound(n, 2048)
+        packed = torch.empty(cap, dtype=torch.int32, device="cuda")
+        back = torch.empty_like(ts)
+
+        def step():
+            w = gbc.compress_bitpack_raw(ctx, ts.data_ptr(), n, packed.data_ptr(), cap, delta=True)
+            gbc.decompress_bitpack_raw(ctx, packed.data_ptr(), w, n, back.data_ptr(), delta=True)
+    elif args.case == "map-u32":
+        # n distinct keys into 2n slots, then n finds (half absent)
+        mk = ((torch.arange(n, dtype=torch.int64, device="cuda") * 2654435761 + 12345) & 0xFFFFFFFE).to(torch.int32)
+        mv = torch.arange(n, dtype=torch.int32, device="cuda")
+        qk = mk.clone()
+        qk[1::2] |= 1
+        got = torch.empty_like(mv)
+        smap = gbc.StaticMap(ctx, 2 * n)
+
+        def step():
+            smap.clear()
+            smap.insert_raw(mk.data_ptr(), mv.data_ptr(), n)
+            smap.find_raw(qk.data_ptr(), n, got.data_ptr())
     else:
         raise SystemExit(f"unknown case {args.case}")
 

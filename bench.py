@@ -820,11 +820,36 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
             k += 1
         return f"2^{k}"
 
-    msd_cap = ctx.tuning_get(f"segsort:u64kv:{size_class(total)}:avg{size_class(total // lens.size)}:msd")
+    seg_key = f"segsort:u64kv:{size_class(total)}:avg{size_class(total // lens.size)}"
+    msd_cap = ctx.tuning_get(seg_key + ":msd")
+    seg_form = ctx.tuning_get(seg_key + ":batch")
     batch()
     ctx.finish()
     graph = gbc.capture(ctx, batch)
     ms_seg, prof_s = timed(graph.launch, steps, warmup, ("segsort.", "segscan.", "sort."))
+    graph.release()
+    # the sort in one persistent launch (grid barriers between its phases),
+    # every split of its CTAs between the small and the large segments, each
+    # captured in a graph with the scan; checked like the autotuned form below
+    one_launch = {}
+    for form in (1, 2, 3, 4):
+        ctx.tuning_set(seg_key, 2048)
+        ctx.tuning_set(seg_key + ":batch", form)
+        batch()
+        ctx.finish()
+        g1 = gbc.capture(ctx, batch)
+        one_launch[form] = timed(g1.launch, max(3, steps // 2), warmup, ("segsort.",))
+        g1.launch()
+        ctx.finish()
+        g1.release()
+    one_form = min(one_launch, key=lambda f: one_launch[f][0])
+    ms_one, prof_one = one_launch[one_form]
+    one_launch_out = (sko.clone(), svo.clone())  # the output of the last one-launch replay
+    ctx.tuning_set(seg_key, int(seg_cap))
+    ctx.tuning_set(seg_key + ":batch", int(seg_form))
+    batch()
+    ctx.finish()
+    graph = gbc.capture(ctx, batch)
     # the plain per-array method: the plain sort called once per segment, timed on a bounded sample
     sample_segs = 2000
     ms_per_array_sample, _ = timed(lambda: [gbc.sort_raw(ctx, sk.data_ptr() + 8 * int(offs[i]),
@@ -864,6 +889,8 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     order = torch.sort(ku, stable=True).indices
     order = order[torch.sort(seg_id[order], stable=True).indices]
     ok = bool(torch.equal(sko, sk[order])) and bool(torch.equal(svo, sv[order]))
+    one_ok = bool(torch.equal(one_launch_out[0], sk[order])) and bool(torch.equal(one_launch_out[1], sv[order]))
+    del one_launch_out
     csum = torch.cumsum(sx.to(torch.int64), 0)
     base = torch.repeat_interleave(torch.cat([torch.zeros(1, device="cuda", dtype=torch.int64), csum[off_d[1:-1].long() - 1]]),
                                    torch.from_numpy(lens).cuda())
@@ -878,12 +905,19 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, seg_bytes, ok, prof_s,
           {"segments": int(lens.size), "total_keys": total, "graph": True, "autotuned_cta_capacity": seg_cap,
            "autotuned_msd_capacity": msd_cap,
+           "autotuned_form": {0: "launch sequence on two streams", 1: "one persistent launch"}.get(
+               seg_form, f"one persistent launch, {seg_form - 1}/8 of its CTAs on the small segments"),
+           "one_launch": {"ms": ms_one, "gkeys": total / (ms_one * 1e-3) / 1e9, "bitexact": one_ok,
+                          "form": f"one cooperative launch, cta capacity 2048, {one_form - 1}/8 of its CTAs on the "
+                                  f"small segments, in a CUDA graph with the scan",
+                          "all_forms_ms": {str(f): v[0] for f, v in one_launch.items()}},
            "keys_in_large_segments": large_keys,
            "includes": "segmented sort (u64 keys + u32 values) and segmented exclusive int32 scan",
            "plain_per_array_estimate_ms": per_array_est_ms,
            "speedup_vs_per_array": per_array_est_ms / ms_seg,
            "plain_lsd_ms": ms_plain_lsd, "plain_lsd_bitexact": plain_ok,
            "speedup_vs_plain_lsd": ms_plain_lsd / ms_seg,
+           "one_launch_speedup_vs_plain_lsd": ms_plain_lsd / ms_one,
            "plain_lsd": "stable plain sort of all pairs by key, stable plain sort of the segment ids in that order, "
                         "gathers of keys and values (sort only: the segmented figure also includes the scan)",
            "hbm_frac_one_pass": 32 * total / (ms_seg * 1e-3) / 1e9 / peak,

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <stdexcept>
+#include <vector>
 
 #include "segmented.hpp"
 #include "sort_internal.hpp"
@@ -112,6 +113,7 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         seg_options o;
         o.cta_cap = c;
         o.msd_cap = 0;
+        o.persistent = 0;
         r.ms.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);
@@ -129,13 +131,43 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         seg_options o;
         o.cta_cap = r.best;
         o.msd_cap = c;
+        o.persistent = 0;
         m.ms.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);
         }));
     }
     pick(m, ctx);
-    r.best_ms = std::min(r.best_ms, m.best_ms);
+    // Last, the launch form: the launch sequence at that capacity against the
+    // one persistent launch (every CTA on both paths, or 1/8 .. 3/8 of them
+    // on the small and medium segments), at capacities whose shared memory
+    // leaves two CTAs per SM; the winner's capacity replaces the first pick.
+    struct form {
+        int persistent, cap;
+    };
+    std::vector<form> forms{{0, r.best}};
+    std::vector<double> times{std::min(r.best_ms, m.best_ms)};
+    for (int mode = 1; mode <= 4; ++mode)
+        for (int c : {1024, 2048}) forms.push_back({mode, std::min(c, cap)});
+    for (std::size_t f = 1; f < forms.size(); ++f) {
+        seg_options o;
+        o.cta_cap = forms[f].cap;
+        o.msd_cap = m.best;
+        o.persistent = forms[f].persistent;
+        times.push_back(ev.time(ctx, repetitions, [&] {
+            segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
+                           false, o);
+        }));
+    }
+    const std::size_t best = std::min_element(times.begin(), times.end()) - times.begin();
+    launch_shape sh;
+    sh.variant = forms[best].persistent;
+    ctx.tuning.store(segsort_batch_tuning_key(key_bytes, kv, n, num_segments), sh);
+    sh.variant = forms[best].cap;
+    ctx.tuning.store(r.key, sh);
+    r.best = forms[best].cap;
+    r.best_ms = times[best];
+    r.persistent_ms = *std::min_element(times.begin() + 1, times.end());
     return r;
 }
 

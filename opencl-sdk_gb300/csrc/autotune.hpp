@@ -17,6 +17,7 @@ struct autotune_result {
     double best_ms = 0;       // its mean time per call
     std::vector<int> candidates;
     std::vector<double> ms;   // mean time per call of every candidate
+    double persistent_ms = 0;  // segmented: the fastest one-launch form's time
 };
 
 //! Plain radix sort: every compiled digit-pass variant (tile shape, CTAs per

@@ -66,7 +66,8 @@ struct SegControl {
     uint32_t tile_ctr[8];
     uint32_t n_sub_warp, n_sub_cta;      // sub-bucket list lengths (MSD route)
     uint32_t sub_warp_next, sub_cta_next;
-    uint32_t pad[2];
+    uint32_t barrier;                    // arrivals at the persistent batch's first grid barrier
+    uint32_t large_barrier;              // ... and at those among its large-segment CTAs
 };
 
 template <typename K> struct SegArgs {
@@ -109,7 +110,7 @@ constexpr uint8_t NO_ROUTE = 0xFF;
 // ---------------------------------------------------------------------------
 // Classification
 // ---------------------------------------------------------------------------
-template <typename K> __global__ void k_seg_classify(SegArgs<K> a)
+template <typename K> __device__ __forceinline__ void seg_classify(const SegArgs<K>& a)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nseg; i += stride) {
@@ -132,17 +133,18 @@ template <typename K> __global__ void k_seg_classify(SegArgs<K> a)
     }
 }
 
-// One CTA: exclusive scan of the large segments' tile counts, then the
-// tile -> segment map.
-template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_plan(SegArgs<K> a)
+template <typename K> __global__ void k_seg_classify(SegArgs<K> a) { seg_classify(a); }
+
+// One CTA of NT threads: exclusive scan of the large segments' tile counts.
+template <typename K, int TILE, int NT> __device__ __forceinline__ void seg_plan_scan(const SegArgs<K>& a)
 {
-    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_warp[NT / 32];
     __shared__ uint32_t s_carry;
     const uint32_t nl = min(a.ctl->n_large, a.max_large);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
-    for (uint32_t base = 0; base < nl; base += 1024) {
+    for (uint32_t base = 0; base < nl; base += NT) {
         const uint32_t j = base + threadIdx.x;
         uint32_t cnt = 0;
         if (j < nl) {
@@ -156,7 +158,7 @@ template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_pl
         for (int w = 0; w < warp; ++w) before += s_warp[w];
         if (j < nl) a.tile_begin[j] = before + x - cnt;
         __syncthreads();
-        if (threadIdx.x == 1023) s_carry = before + x;
+        if (threadIdx.x == NT - 1) s_carry = before + x;
         __syncthreads();
     }
     const uint32_t total = min(s_carry, a.max_tiles);
@@ -165,11 +167,26 @@ template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_pl
         a.ctl->large_tiles = total;
     }
     __syncthreads();
-    // tile -> segment: warp w fills the tiles of segments w, w + 32, ...
-    for (uint32_t j = warp; j < nl; j += 32) {
+}
+
+// The tile -> segment map: the warps of the first `ctas` CTAs fill the tiles
+// of one large segment at a time.
+template <typename K> __device__ __forceinline__ void seg_plan_map(const SegArgs<K>& a, uint32_t ctas)
+{
+    const uint32_t nl = min(a.ctl->n_large, a.max_large);
+    const uint32_t total = a.ctl->large_tiles;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = ctas * (blockDim.x / 32);
+    for (uint32_t j = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); j < nl; j += warps) {
         const uint32_t t0 = a.tile_begin[j], t1 = min(a.tile_begin[j + 1], total);
         for (uint32_t t = t0 + lane; t < t1; t += 32) a.tile_seg[t] = j;
     }
+}
+
+template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_plan(SegArgs<K> a)
+{
+    seg_plan_scan<K, TILE, 1024>(a);
+    seg_plan_map(a, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -293,8 +310,7 @@ __device__ void group_sort(K* k0, K* k1, uint32_t* v0, uint32_t* v1, uint32_t* r
 
 // SUB: the MSD route's sub-buckets (begin, end pairs, read from alt) instead
 // of whole segments (read from the input).
-template <typename K, bool HAS_V, bool SUB>
-__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
+template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_small_warp(const SegArgs<K>& a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -345,7 +361,12 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
 }
 
 template <typename K, bool HAS_V, bool SUB>
-__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
+__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
+{
+    seg_small_warp<K, HAS_V, SUB>(a);
+}
+
+template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_small_cta(const SegArgs<K>& a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t cap = SUB ? a.sub_cap : a.cta_cap;
@@ -394,6 +415,12 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
     }
 }
 
+template <typename K, bool HAS_V, bool SUB>
+__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
+{
+    seg_small_cta<K, HAS_V, SUB>(a);
+}
+
 // ---------------------------------------------------------------------------
 // Large segments: per-segment digit histograms -> absolute bin starts, in
 // three steps over the large-segment tile sequence that the passes use (so
@@ -404,16 +431,19 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
 // ---------------------------------------------------------------------------
 constexpr uint32_t HIST_TILES = 8;
 
-template <typename K> __global__ void k_seg_large_zero(SegArgs<K> a)
+template <typename K> __device__ __forceinline__ void seg_large_zero(const SegArgs<K>& a, uint32_t ctas)
 {
     constexpr int P = Traits<K>::PASSES;
     const uint32_t nl = min(a.ctl->n_large, a.max_large);
     const std::size_t words = (std::size_t)nl * P * RADIX;
-    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    const std::size_t stride = (std::size_t)ctas * blockDim.x;
     for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) a.seg_hist[i] = 0;
 }
 
-template <typename K, int TILE> __global__ void __launch_bounds__(256) k_seg_large_count(SegArgs<K> a)
+template <typename K> __global__ void k_seg_large_zero(SegArgs<K> a) { seg_large_zero(a, gridDim.x); }
+
+
+template <typename K, int TILE> __device__ __forceinline__ void seg_large_count(const SegArgs<K>& a, uint32_t ctas)
 {
     constexpr int P = Traits<K>::PASSES;
     constexpr int BATCH = 8;  // keys in flight per thread
@@ -434,7 +464,7 @@ template <typename K, int TILE> __global__ void __launch_bounds__(256) k_seg_lar
     };
     for (int i = threadIdx.x; i < 2 * P * RADIX; i += 256) (&sh[0][0])[i] = 0;
     __syncthreads();
-    for (uint32_t r = blockIdx.x; r < runs; r += gridDim.x) {
+    for (uint32_t r = blockIdx.x; r < runs; r += ctas) {
         const uint32_t t0 = r * HIST_TILES, t1 = min(total, t0 + HIST_TILES);
         uint32_t j = a.tile_seg[t0];
         for (uint32_t t = t0; t < t1; ++t) {
@@ -466,12 +496,18 @@ template <typename K, int TILE> __global__ void __launch_bounds__(256) k_seg_lar
     }
 }
 
-template <typename K> __global__ void __launch_bounds__(256) k_seg_large_starts(SegArgs<K> a)
+template <typename K, int TILE> __global__ void __launch_bounds__(256) k_seg_large_count(SegArgs<K> a)
+{
+    seg_large_count<K, TILE>(a, gridDim.x);
+}
+
+
+template <typename K> __device__ __forceinline__ void seg_large_starts(const SegArgs<K>& a, uint32_t ctas)
 {
     constexpr int P = Traits<K>::PASSES;
     __shared__ uint32_t s_scratch[8];
     const uint32_t nl = min(a.ctl->n_large, a.max_large);
-    for (uint32_t j = blockIdx.x; j < nl; j += gridDim.x) {
+    for (uint32_t j = blockIdx.x; j < nl; j += ctas) {
         const uint32_t b = a.off[a.large_list[j]];
         for (int p = 0; p < P; ++p) {
             uint32_t* row = a.seg_hist + ((std::size_t)j * P + p) * RADIX;
@@ -481,20 +517,26 @@ template <typename K> __global__ void __launch_bounds__(256) k_seg_large_starts(
     }
 }
 
+template <typename K> __global__ void __launch_bounds__(256) k_seg_large_starts(SegArgs<K> a)
+{
+    seg_large_starts(a, gridDim.x);
+}
+
+
 // Per large segment (one CTA, thread d = bin d): the highest digit position
 // that varies inside the segment (its bins are not all in one) and, when
 // every bin there holds at most sub_cap keys, the MSD route: one pass on that
 // digit partitions the segment into its bins (stable), which become
 // sub-buckets for the warp and CTA sorts; else the full LSD passes. The bin
 // starts in seg_hist are absolute, from k_seg_large_starts.
-template <typename K> __global__ void __launch_bounds__(256) k_seg_route(SegArgs<K> a)
+template <typename K> __device__ __forceinline__ void seg_route(const SegArgs<K>& a, uint32_t ctas)
 {
     constexpr int P = Traits<K>::PASSES;
     __shared__ uint32_t s_max[8];
     __shared__ int s_top;
     const uint32_t nl = min(a.ctl->n_large, a.max_large);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t j = blockIdx.x; j < nl; j += gridDim.x) {
+    for (uint32_t j = blockIdx.x; j < nl; j += ctas) {
         const uint32_t s = a.large_list[j];
         const uint32_t segb = a.off[s], sege = a.off[s + 1], len = sege - segb;
         auto bin_size = [&](int p, uint32_t d) {
@@ -538,13 +580,16 @@ template <typename K> __global__ void __launch_bounds__(256) k_seg_route(SegArgs
     }
 }
 
+template <typename K> __global__ void __launch_bounds__(256) k_seg_route(SegArgs<K> a) { seg_route(a, gridDim.x); }
+
+
 // One digit pass over every large segment's tiles (cf. onesweep::k_pass2:
 // shared-memory peer-mask ranking, place offsets folded into the per-warp
 // counts, a look-back reading LBW predecessors per round trip, which stops at
 // the segment's first tile (it publishes an inclusive count), an L2 prefetch
 // of the tile a grid ahead and an unrolled write-out of full tiles).
-template <typename K, bool HAS_V, int THREADS, int ITEMS, int MINB, int LBW>
-__global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, int slot)
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int LBW>
+__device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, uint32_t ctas)
 {
     constexpr int P = Traits<K>::PASSES;
     constexpr int WARPS = THREADS / 32;
@@ -582,7 +627,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
             s_tile = atomicAdd(&a.ctl->tile_ctr[slot], 1u);
             // L2 prefetch of the tile a grid further on in the tile sequence
             // (from where this pass reads it, if it takes part)
-            const uint32_t ahead = s_tile + gridDim.x;
+            const uint32_t ahead = s_tile + ctas;
             if (aligned_src && ahead < num_tiles) {
                 const uint32_t ja = a.tile_seg[ahead];
                 const uint8_t ra = a.route[ja];
@@ -767,6 +812,98 @@ __global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, 
     }
 }
 
+template <typename K, bool HAS_V, int THREADS, int ITEMS, int MINB, int LBW>
+__global__ void __launch_bounds__(THREADS, MINB) k_seg_large_pass(SegArgs<K> a, int slot)
+{
+    seg_large_pass<K, HAS_V, THREADS, ITEMS, LBW>(a, slot, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// The whole batch in one persistent launch: every phase above in order, with
+// a grid barrier wherever a phase reads what an earlier one wrote (the launch
+// is cooperative, so every CTA is resident). After classification the first
+// large_ctas CTAs take the large-segment phases -- the plan's scan (CTA 0)
+// while they zero the histogram rows; the tile map; the histogram count; the
+// bin starts; [the MSD route]; each digit pass; [the MSD route's bucket
+// sorts] -- with barriers among themselves, and the other CTAs sort the
+// small and medium segments meanwhile (the two paths share nothing). With
+// large_ctas equal to the grid, every CTA takes both, the small and medium
+// sorts after the histogram count. A barrier wait is bounded (about one
+// second): a CTA that gives up records ERR_LOOKBACK_TIMEOUT and returns, so
+// no later phase runs on incomplete data, and the others give up at their
+// next barrier in turn.
+// ---------------------------------------------------------------------------
+// The first `parties` CTAs of the grid take part; `generation` counts the
+// barriers passed (kept by thread 0).
+__device__ __forceinline__ bool grid_barrier(uint32_t* arrivals, uint32_t& generation, uint32_t parties, int* err)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_ok = 1;
+        __threadfence();
+        atomicAdd(arrivals, 1u);
+        const uint32_t target = ++generation * parties;
+        const unsigned long long t0 = dev::globaltimer();
+        for (uint32_t spin = 1; dev::ld_acquire(arrivals) < target; ++spin) {
+            if ((spin & 63) == 0 && dev::globaltimer() - t0 > dev::SPIN_LIMIT_NS) {
+                dev::raise_error(err, dev::ERR_LOOKBACK_TIMEOUT);
+                s_ok = 0;
+                break;
+            }
+            if (spin > 16) __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename K, bool HAS_V, int ITEMS, int LBW>
+__global__ void __launch_bounds__(256, 2) k_seg_batch(SegArgs<K> a, int msd, uint32_t large_ctas)
+{
+    constexpr int P = Traits<K>::PASSES;
+    constexpr int TILE = 256 * ITEMS;
+    uint32_t gen = 0, lgen = 0;
+    seg_classify(a);
+    if (!grid_barrier(&a.ctl->barrier, gen, gridDim.x, a.err)) return;
+    const bool split = large_ctas < gridDim.x;
+    if (blockIdx.x >= large_ctas) {
+        seg_small_warp<K, HAS_V, false>(a);
+        __syncthreads();
+        seg_small_cta<K, HAS_V, false>(a);
+        return;
+    }
+    uint32_t* arrivals = &a.ctl->large_barrier;
+    if (blockIdx.x == 0) seg_plan_scan<K, TILE, 256>(a);
+    seg_large_zero(a, large_ctas);
+    if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    seg_plan_map(a, large_ctas);
+    if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    seg_large_count<K, TILE>(a, large_ctas);
+    if (!split) {
+        seg_small_warp<K, HAS_V, false>(a);
+        __syncthreads();
+        seg_small_cta<K, HAS_V, false>(a);
+    }
+    if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    seg_large_starts(a, large_ctas);
+    if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    if (msd) {
+        seg_route(a, large_ctas);
+        if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    }
+    for (int slot = 0; slot < P; ++slot) {
+        seg_large_pass<K, HAS_V, 256, ITEMS, LBW>(a, slot, large_ctas);
+        if (!grid_barrier(arrivals, lgen, large_ctas, a.err)) return;
+    }
+    if (msd) {
+        seg_small_warp<K, HAS_V, true>(a);
+        __syncthreads();
+        seg_small_cta<K, HAS_V, true>(a);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host
 // ---------------------------------------------------------------------------
@@ -859,6 +996,48 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     a.max_sub = max_sub;
     a.sub_cap = msd_cap;
 
+    constexpr std::size_t per_warp_smem =
+        2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
+    auto cta_smem = [](uint32_t cap) {
+        return (std::size_t)cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * SMALL_WARPS * RADIX * 4;
+    };
+    if (opt.persistent > 0) {
+        // One cooperative launch of every phase; its shared memory is the
+        // largest any phase needs. Falls through to the launch sequence below
+        // when not even one CTA per SM fits.
+        const std::size_t pass_smem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +
+                                      (HAS_V ? (std::size_t)TILE * 4 : 0);
+        const std::size_t smem = std::max({per_warp_smem * SMALL_WARPS, cta_smem(cta_cap), pass_smem,
+                                           msd ? cta_smem(msd_cap) : std::size_t(0)});
+        auto kern = &k_seg_batch<K, HAS_V, LS::ITEMS, LS::LBW>;
+        int per_sm = 0;
+        if (smem + 32 * 1024 <= ctx.smem_optin) {
+            set_smem(kern, smem);
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem),
+                       "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        }
+        if (per_sm > 0) {
+            const uint32_t grid = (uint32_t)(ctx.sm_count * per_sm);
+            // persistent >= 2: that many eighths (less one) of the grid sort
+            // the small and medium segments while the rest take the large ones
+            const uint32_t small_ctas = opt.persistent >= 2 ? grid * (uint32_t)std::min(opt.persistent - 1, 6) / 8 : 0;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = ctx.stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            kernel_timer kt(ctx, "segsort.batch");
+            check_cuda(cudaLaunchKernelEx(&cfg, kern, a, msd ? 1 : 0, grid - small_ctas),
+                       "segmented sort batch launch");
+            return;
+        }
+    }
+
     {
         kernel_timer kt(ctx, "segsort.classify");
         const int grid = (int)std::max<std::size_t>(1, std::min<std::size_t>((nseg + 255) / 256, (std::size_t)ctx.sm_count * 4));
@@ -872,9 +1051,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
 
     {
         kernel_timer kt(ctx, "segsort.small_warp");
-        constexpr std::size_t per_warp =
-            2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
-        const std::size_t smem = per_warp * SMALL_WARPS;
+        const std::size_t smem = per_warp_smem * SMALL_WARPS;
         auto kern = &k_seg_small_warp<K, HAS_V, false>;
         set_smem(kern, smem);
         const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
@@ -939,6 +1116,11 @@ uint32_t segsort_cta_cap(int key_bytes, bool has_values)
     return key_bytes == 4 ? (has_values ? 10240u : 16384u) : (has_values ? 7168u : 10240u);
 }
 
+std::string segsort_batch_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
+{
+    return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":batch";
+}
+
 std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
 {
     return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":msd";
@@ -974,6 +1156,12 @@ void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, in
         o.msd_cap = ctx.tuning.lookup(segsort_msd_tuning_key(key_bytes, vals_in != nullptr, n, num_segments), shape)
                         ? shape.variant
                         : 0;
+    }
+    if (o.persistent < 0) {
+        launch_shape shape;
+        o.persistent = ctx.tuning.lookup(segsort_batch_tuning_key(key_bytes, vals_in != nullptr, n, num_segments), shape)
+                           ? shape.variant
+                           : 0;
     }
     if (key_bytes == 4) {
         const auto xf = dev::make_xform<uint32_t>(key_kind, descending);

@@ -19,6 +19,12 @@ struct seg_options {
     // shared-memory sorts finish the buckets; 0: every large segment takes
     // all digit passes; -1: the default (the tuning table's entry, else off)
     int msd_cap = -1;
+    // 0: a launch per phase, the small/medium and large paths on two
+    // streams; 1: the whole batch in one persistent (cooperative) launch with
+    // grid barriers between its phases; 2..7: the same with (persistent - 1)
+    // eighths of its CTAs sorting the small and medium segments while the
+    // others take the large ones; -1: the tuning table's entry, else 0
+    int persistent = -1;
 };
 
 //! Sorts every segment [offsets[i], offsets[i+1]) independently and stably.
@@ -36,6 +42,8 @@ void segmented_scan(device_context& ctx, const void* in, void* out, std::size_t 
                     const void* identity, bool exclusive, const uint32_t* offsets, std::size_t num_segments);
 
 std::string segsort_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
+//! The tuning-table key of the batch's launch form (seg_options::persistent).
+std::string segsort_batch_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
 //! The tuning-table key of the MSD route's bucket capacity (0: off).
 std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
 

@@ -173,3 +173,62 @@ def test_msd_and_lsd_routes_mixed(ctx, gbc, orc, key_dtype, with_values):
         assert np.array_equal(kb.to_host().view(np.uint8), ek.view(np.uint8))
         if with_values:
             assert np.array_equal(vb.to_host(), ev)
+
+
+def _size_class(v):
+    k = 0
+    while (1 << k) < v and k < 63:
+        k += 1
+    return f"2^{k}"
+
+
+@pytest.mark.parametrize("form", [1, 3])
+@pytest.mark.parametrize("key_dtype,with_values", [(np.uint64, True), (np.uint32, False), (np.float32, True)])
+def test_one_persistent_launch(ctx, gbc, orc, form, key_dtype, with_values):
+    """The whole batch in one cooperative launch (form 1: every CTA takes the
+    small and the large segments in turn; form 3: a quarter of the CTAs sort
+    the small and medium segments while the rest take the large ones),
+    selected through the tuning table, directly and replayed from a CUDA
+    graph: bit for bit the per-segment std::stable_sort."""
+    off = orc.lognormal_segments(4000, 256, 2.0, 1, 1 << 17, seed=12)
+    n = int(off[-1])
+    rng = np.random.default_rng(13)
+    if np.dtype(key_dtype).kind == "f":
+        keys = rng.standard_normal(n).astype(key_dtype)
+        keys[::17] = -0.0
+    else:
+        keys = rng.integers(0, 2**63, size=n, dtype=np.uint64).astype(key_dtype)
+        keys[::9] = keys[0]
+    vals = np.arange(n, dtype=np.uint32)
+    tag = {np.dtype(np.uint64): "u64", np.dtype(np.uint32): "u32", np.dtype(np.float32): "u32"}[np.dtype(key_dtype)]
+    key = f"segsort:{tag}{'kv' if with_values else 'k'}:{_size_class(n)}:avg{_size_class(n // (off.size - 1))}"
+    ctx.tuning_set(key, 2048)
+    ctx.tuning_set(key + ":batch", form)
+    try:
+        ek, ev = orc.std_segmented_sort(keys, off, vals if with_values else None)
+        ob = gbc.DeviceBuffer.from_host(ctx, off)
+        kin = gbc.DeviceBuffer.from_host(ctx, keys)
+        vin = gbc.DeviceBuffer.from_host(ctx, vals)
+        kout = gbc.DeviceBuffer(ctx, n, key_dtype)
+        vout = gbc.DeviceBuffer(ctx, n, np.uint32)
+
+        def call():
+            gbc.segmented_sort_raw(ctx, kin.device_pointer, kout.device_pointer, key_dtype, n, ob.device_pointer,
+                                   off.size - 1, vin.device_pointer if with_values else 0,
+                                   vout.device_pointer if with_values else 0)
+
+        call()
+        assert np.array_equal(kout.to_host().view(np.uint8), ek.view(np.uint8))
+        if with_values:
+            assert np.array_equal(vout.to_host(), ev)
+        # replayed from a graph, after the outputs are overwritten
+        graph = gbc.capture(ctx, call)
+        gbc.fill(ctx, kout, np.zeros(1, dtype=key_dtype)[0])
+        graph.launch()
+        ctx.finish()
+        graph.release()
+        assert np.array_equal(kout.to_host().view(np.uint8), ek.view(np.uint8))
+        if with_values:
+            assert np.array_equal(vout.to_host(), ev)
+    finally:
+        ctx.tuning_set(key + ":batch", 0)

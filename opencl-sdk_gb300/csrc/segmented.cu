@@ -588,6 +588,8 @@ template <typename K> __global__ void __launch_bounds__(256) k_seg_route(SegArgs
 // counts, a look-back reading LBW predecessors per round trip, which stops at
 // the segment's first tile (it publishes an inclusive count), an L2 prefetch
 // of the tile a grid ahead and an unrolled write-out of full tiles).
+constexpr int LARGE_PAD = 1;  // words between the half-warp count arrays of the large pass
+
 template <typename K, bool HAS_V, int THREADS, int ITEMS, int LBW>
 __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, uint32_t ctas)
 {
@@ -607,17 +609,22 @@ __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, ui
         ((reinterpret_cast<uintptr_t>(src_k) | (HAS_V ? reinterpret_cast<uintptr_t>(src_v) : 0)) & 15) == 0;
 
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256: counts, then place offsets
-    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256 peer masks
-    K* s_keys = reinterpret_cast<K*>(warp_mask + WARPS * RADIX);
+    // Keys are ranked by half-warps (rows of 16, each half-warp a contiguous
+    // run of the tile): one word per half-warp and digit holds the count
+    // (high 16 bits) and the current row's peer mask (low 16 bits).
+    // A half-warp's words sit LARGE_PAD banks from its partner's, so equal
+    // digits in the two halves of a row do not meet in one bank.
+    constexpr int GROUPS = 2 * WARPS, GSTRIDE = RADIX + LARGE_PAD;
+    static_assert(16 * ITEMS < (1 << 16), "half-warp counts are 16-bit");
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // GROUPS x GSTRIDE: counts, then place offsets
+    K* s_keys = reinterpret_cast<K*>(warp_hist + GROUPS * GSTRIDE);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
     __shared__ uint32_t s_bin_off[RADIX], s_local[RADIX];
     __shared__ uint32_t s_scratch[8];
     __shared__ uint32_t s_tile;
     __shared__ int s_abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t lt_mask = dev::lanemask_lt();
-    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
+    const int grp = 2 * warp + (lane >> 4), gl = lane & 15;
     if (tid == 0) s_abort = 0;
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.max_tiles;
     auto digit = [&](K k) -> uint32_t { return (uint32_t)(a.xf(k) >> shift) & 0xFFu; };
@@ -641,7 +648,7 @@ __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, ui
                 }
             }
         }
-        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
+        for (int i = tid; i < GROUPS * GSTRIDE; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= num_tiles) break;
@@ -666,23 +673,23 @@ __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, ui
         const uint32_t valid = min((uint32_t)TILE, sege - tile_base);
         const bool first = lt == 0;
 
-        const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
+        const uint32_t wbase = tile_base + grp * 16 * ITEMS + gl;
         K key[ITEMS];
         uint32_t rd[ITEMS];
         uint32_t val[HAS_V ? ITEMS : 1];
         if (valid == (uint32_t)TILE) {
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) key[i] = tsrc_k[wbase + i * 32];
+            for (int i = 0; i < ITEMS; ++i) key[i] = tsrc_k[wbase + i * 16];
             if (HAS_V) {
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) val[i] = tsrc_v[wbase + i * 32];
+                for (int i = 0; i < ITEMS; ++i) val[i] = tsrc_v[wbase + i * 16];
             }
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
         } else {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t idx = wbase + i * 32;
+                const uint32_t idx = wbase + i * 16;
                 const bool in = idx < sege;
                 key[i] = in ? tsrc_k[idx] : K(0);
                 if (HAS_V) val[i] = in ? tsrc_v[idx] : 0u;
@@ -690,32 +697,28 @@ __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, ui
             }
         }
 
-        uint32_t* wh = warp_hist + warp * RADIX;
-        uint32_t* wm = warp_mask + warp * RADIX;
+        uint32_t* wh = warp_hist + grp * GSTRIDE;
+        const uint32_t hbit = 1u << gl, hlt = hbit - 1u;
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t d = rd[i];
-            atomicOr(&wm[d], 1u << lane);
+            atomicOr(&wh[d], hbit);
             __syncwarp();
-            const uint32_t peers = wm[d];
-            const uint32_t before = wh[d];
+            const uint32_t x = wh[d];
             __syncwarp();
-            const uint32_t lower = peers & lt_mask;
-            if (lower == 0) {
-                wh[d] = before + __popc(peers);
-                wm[d] = 0;
-            }
+            const uint32_t peers = x & 0xFFFFu, before = x >> 16;
+            if ((peers & hlt) == 0) wh[d] = (before + __popc(peers)) << 16;  // the new count; the mask cleared
             __syncwarp();
-            rd[i] = ((before + __popc(lower)) << 8) | d;
+            rd[i] = ((before + __popc(peers & hlt)) << 8) | d;
         }
         __syncthreads();
 
         uint32_t count = 0;
         if (tid < RADIX) {
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) {
-                const uint32_t c = warp_hist[w * RADIX + tid];
-                warp_hist[w * RADIX + tid] = count;
+            for (int w = 0; w < GROUPS; ++w) {
+                const uint32_t c = warp_hist[w * GSTRIDE + tid] >> 16;
+                warp_hist[w * GSTRIDE + tid] = count;
                 count += c;
             }
         }
@@ -727,12 +730,12 @@ __device__ __forceinline__ void seg_large_pass(const SegArgs<K>& a, int slot, ui
         if (tid < RADIX) {
             s_local[tid] = local;
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) warp_hist[w * RADIX + tid] += local;
+            for (int w = 0; w < GROUPS; ++w) warp_hist[w * GSTRIDE + tid] += local;
         }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t pos = warp_hist[warp * RADIX + (rd[i] & 0xFFu)] + (rd[i] >> 8);
+            const uint32_t pos = warp_hist[grp * GSTRIDE + (rd[i] & 0xFFu)] + (rd[i] >> 8);
             s_keys[pos] = key[i];
             if (HAS_V) s_vals[pos] = val[i];
         }
@@ -1001,12 +1004,14 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     auto cta_smem = [](uint32_t cap) {
         return (std::size_t)cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * SMALL_WARPS * RADIX * 4;
     };
+    // the large pass: two half-warp count arrays of RADIX + LARGE_PAD words per warp, and a tile
+    constexpr std::size_t large_pass_smem = (std::size_t)(LS::THREADS / 32) * (RADIX + LARGE_PAD) * 8 +
+                                            (std::size_t)TILE * sizeof(K) + (HAS_V ? (std::size_t)TILE * 4 : 0);
     if (opt.persistent > 0) {
         // One cooperative launch of every phase; its shared memory is the
         // largest any phase needs. Falls through to the launch sequence below
         // when not even one CTA per SM fits.
-        const std::size_t pass_smem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +
-                                      (HAS_V ? (std::size_t)TILE * 4 : 0);
+        const std::size_t pass_smem = large_pass_smem;
         const std::size_t smem = std::max({per_warp_smem * SMALL_WARPS, cta_smem(cta_cap), pass_smem,
                                            msd ? cta_smem(msd_cap) : std::size_t(0)});
         auto kern = &k_seg_batch<K, HAS_V, LS::ITEMS, LS::LBW>;
@@ -1080,8 +1085,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
             check_cuda(cudaGetLastError(), "segmented sort route launch");
         }
         auto pk = &k_seg_large_pass<K, HAS_V, LS::THREADS, LS::ITEMS, LS::MINB, LS::LBW>;
-        const std::size_t psmem = (std::size_t)(LS::THREADS / 32) * RADIX * 8 + (std::size_t)TILE * sizeof(K) +
-                                  (HAS_V ? (std::size_t)TILE * 4 : 0);
+        const std::size_t psmem = large_pass_smem;
         set_smem(pk, psmem);
         const int pgrid = ctx.sm_count * occupancy(pk, LS::THREADS, psmem);
         for (int s = 0; s < P; ++s) {

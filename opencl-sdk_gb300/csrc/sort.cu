@@ -1,7 +1,8 @@
 // Onesweep LSD radix sort for sm_103a: 8-bit digits, one upfront pass that
 // builds every digit histogram, then one kernel per digit that ranks a tile of
-// keys with warp match/ballot votes and finds the tile's global offsets by a
-// decoupled look-back over per-(tile, digit) status words.
+// keys by peer-mask words in shared memory (or warp votes) and finds the
+// tile's global offsets by a decoupled look-back over per-(tile, digit) status
+// words.
 //
 // Reference path replaced: detail::radix_sort (lib/src/Compute/
 // Algorithm.cpp:453-527) with its kernels clc_radix_histogram (153-171) and
@@ -433,15 +434,35 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     one warp, 8 digits per lane with 16-byte status loads, made the sort
 //     twice as slow, and so did taking the next tile's index early: a tile
 //     taken before the CTA can work on it publishes its counts late);
-//   * IDENT: the key transform is the identity (unsigned ascending keys).
+//   * IDENT: the key transform is the identity (unsigned ascending keys);
+//   * HALF: rows of 16 keys, one per half-warp, ranked in one 32-bit word per
+//     half-warp and digit that holds the count (high 16 bits) and the row's
+//     peer mask (low 16 bits): an OR, one read and the lowest peer's store
+//     of the new count (which also clears the mask), three shared-memory
+//     instructions per 32 keys instead of five. Each half-warp takes a
+//     contiguous run of the tile, so ranks stay in input order.
 // ---------------------------------------------------------------------------
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH, int BR>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH, int BR,
+          bool HALF, int PAD>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
+    constexpr int GROUPS = HALF ? 2 * WARPS : WARPS;  // ranking groups: warps or half-warps
+    constexpr int GW = HALF ? 16 : 32;                // keys per row of a group
+    // PAD > 0: a half-warp's words sit PAD banks from its partner's, so equal
+    // digits in the two halves of a row do not meet in one bank (skewed keys:
+    // 2^28 pairs whose keys are the AND of 4 uniform words, 7.9 ms with PAD 0,
+    // 6.8 ms with PAD 1). Uniform keys measure fastest with PAD 0 (6.07 ms
+    // against 6.27 for any PAD tried: 1, 8, 16), so both are compiled. (The
+    // same choice made per pass on the device from the upfront histogram, a
+    // stride known only at run time, was slower for both: 6.52 and 7.06 ms.)
+    static_assert(PAD >= 0 && PAD <= 16, "the shared-memory size allows 16 words of padding per group");
+    constexpr int GSTRIDE = HALF ? RADIX + PAD : RADIX;
+    constexpr int TILE_AT = HALF ? GROUPS * GSTRIDE : 2 * WARPS * RADIX;  // words
     static_assert(THREADS >= RADIX, "one thread per bin");
     static_assert(TILE < (1 << 24), "rank and digit share a word");
+    static_assert(!HALF || (BR == 0 && GW * ITEMS < (1 << 16)), "half-warp counts are 16-bit");
 
     const uint32_t act = a.ctl->plan.num_active;
     if (slot >= (int)act) return;
@@ -462,13 +483,13 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 
     extern __shared__ __align__(16) unsigned char smem[];
-    // Per warp and digit: the running count (then the place offset) and the
-    // current row's peer mask.
-    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // WARPS x 256
-    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256
+    // Per group and digit: the running count (then the place offset) and the
+    // current row's peer mask: two words per warp, or one word per half-warp.
+    uint32_t* warp_hist = reinterpret_cast<uint32_t*>(smem);  // GROUPS x GSTRIDE
+    uint32_t* warp_mask = warp_hist + WARPS * RADIX;          // WARPS x 256 (not HALF)
     // One tile of keys (+ values); STAGED: two, the next tile's bulk copy
     // landing in one while the current tile is worked on in the other.
-    unsigned char* tiles = reinterpret_cast<unsigned char*>(warp_mask + WARPS * RADIX);
+    unsigned char* tiles = reinterpret_cast<unsigned char*>(warp_hist + TILE_AT);
     constexpr uint32_t KEY_BYTES = TILE * sizeof(K), VAL_BYTES = HAS_V ? TILE * 4 : 0;
     constexpr uint32_t STAGE_BYTES = KEY_BYTES + VAL_BYTES;
     __shared__ uint32_t s_bin_start[RADIX], s_bin_off[RADIX], s_local[RADIX];
@@ -479,9 +500,12 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     __shared__ __align__(8) uint64_t s_bar[2];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int grp = HALF ? 2 * warp + (lane >> 4) : warp;  // ranking group
+    const int gl = HALF ? lane & 15 : lane;                // lane within the group
     const uint32_t lt_mask = dev::lanemask_lt();
     auto digit = [&](K k) -> uint32_t { return (uint32_t)((IDENT ? k : a.xf(k)) >> shift) & 0xFFu; };
-    for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
+    if (!HALF)
+        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_mask[i] = 0;
     if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
     uint32_t* ctr = &a.ctl->tile_ctr[slot];
@@ -526,7 +550,7 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
                 if (HAS_V) dev::prefetch_l2(src_v + ahead * TILE, TILE * 4);
             }
         }
-        for (int i = tid; i < WARPS * RADIX; i += THREADS) warp_hist[i] = 0;
+        for (int i = tid; i < GROUPS * GSTRIDE; i += THREADS) warp_hist[i] = 0;
         __syncthreads();
         const uint32_t t = s_stage_tile[st];
         if (t >= a.num_tiles) break;
@@ -543,35 +567,36 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             parity ^= 1u << st;
         }
 
-        // Load: row i of warp w is keys tile_base + w*32*ITEMS + 32*i + lane.
-        // Past the end the digit is 255, so padding ranks last.
-        const uint32_t wbase = tile_base + warp * 32 * ITEMS + lane;
+        // Load: row i of group g is keys tile_base + g*GW*ITEMS + GW*i + gl
+        // (groups in input order). Past the end the digit is 255, so padding
+        // ranks last.
+        const uint32_t wbase = tile_base + grp * GW * ITEMS + gl;
         K key[ITEMS];
         uint32_t rd[ITEMS];
         uint32_t val[HAS_V ? ITEMS : 1];
         if (staged) {
-            const uint32_t lb = warp * 32 * ITEMS + lane;
+            const uint32_t lb = grp * GW * ITEMS + gl;
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[lb + i * 32];
+            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[lb + i * GW];
             if (HAS_V) {
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[lb + i * 32];
+                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[lb + i * GW];
             }
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
         } else if (valid == (uint32_t)TILE) {
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * 32];
+            for (int i = 0; i < ITEMS; ++i) key[i] = src_k[wbase + i * GW];
             if (HAS_V) {
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) val[i] = src_v[wbase + i * 32];
+                for (int i = 0; i < ITEMS; ++i) val[i] = src_v[wbase + i * GW];
             }
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) rd[i] = digit(key[i]);
         } else {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t idx = wbase + i * 32;
+                const uint32_t idx = wbase + i * GW;
                 const bool in = idx < n;
                 key[i] = in ? src_k[idx] : K(0);
                 if (HAS_V) val[i] = in ? src_v[idx] : 0u;
@@ -583,10 +608,25 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         // bit into its digit's mask word and reads the word back (its peers)
         // and the warp's count of the digit in earlier rows; the lowest peer
         // stores the new count and clears the mask.
-        uint32_t* wh = warp_hist + warp * RADIX;
+        uint32_t* wh = warp_hist + grp * GSTRIDE;
         uint32_t* wm = warp_mask + warp * RADIX;
+        if (HALF) {
+            const uint32_t hbit = 1u << gl, hlt = hbit - 1u;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t d = rd[i];
+                atomicOr(&wh[d], hbit);
+                __syncwarp();
+                const uint32_t x = wh[d];
+                __syncwarp();
+                const uint32_t peers = x & 0xFFFFu, before = x >> 16;
+                if ((peers & hlt) == 0) wh[d] = (before + __popc(peers)) << 16;
+                __syncwarp();
+                rd[i] = ((before + __popc(peers & hlt)) << 8) | d;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < (HALF ? 0 : ITEMS); ++i) {
             const uint32_t d = rd[i];
             // BR of every 4 rows find their peers with 8 ballots (ALU pipe)
             // instead of the mask word (shared-memory pipe)
@@ -622,9 +662,9 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         uint32_t count = 0;
         if (tid < RADIX) {
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) {
-                const uint32_t c = warp_hist[w * RADIX + tid];
-                warp_hist[w * RADIX + tid] = count;
+            for (int w = 0; w < GROUPS; ++w) {
+                const uint32_t c = HALF ? warp_hist[w * GSTRIDE + tid] >> 16 : warp_hist[w * GSTRIDE + tid];
+                warp_hist[w * GSTRIDE + tid] = count;
                 count += c;
             }
         }
@@ -637,14 +677,14 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         if (tid < RADIX) {
             s_local[tid] = local;
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) warp_hist[w * RADIX + tid] += local;
+            for (int w = 0; w < GROUPS; ++w) warp_hist[w * GSTRIDE + tid] += local;
         }
         __syncthreads();
 
         // Local sort of the tile into shared memory.
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t pos = warp_hist[warp * RADIX + (rd[i] & 0xFFu)] + (rd[i] >> 8);
+            const uint32_t pos = warp_hist[grp * GSTRIDE + (rd[i] & 0xFFu)] + (rd[i] >> 8);
             s_keys[pos] = key[i];
             if (HAS_V) s_vals[pos] = val[i];
         }
@@ -741,10 +781,11 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     }
 }
 
-template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF, int BR>
+template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF, int BR,
+          bool HALF, int PAD>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR, HALF, PAD>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -766,15 +807,20 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_P1(K, HV, T, I, M) PassVariant<K>{T, I, false, false, &k_pass<K, HV, T, I, M>, &k_pass<K, HV, T, I, M>}
 #define GBC_P1B(K, HV, T, I, B) \
     PassVariant<K>{T, I, false, false, &k_pass_mb<K, HV, T, I, false, B>, &k_pass_mb<K, HV, T, I, false, B>}
-#define GBC_P2(K, HV, T, I, B, W, S, PF) GBC_P2R(K, HV, T, I, B, W, S, PF, 0)
-#define GBC_P2R(K, HV, T, I, B, W, S, PF, BR)                                                  \
-    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR>,              \
-                   &k_pass2<K, HV, T, I, true, B, W, S, PF, BR>}
+#define GBC_P2(K, HV, T, I, B, W, S, PF) GBC_P2XP(K, HV, T, I, B, W, S, PF, 0, false, 0)
+#define GBC_P2R(K, HV, T, I, B, W, S, PF, BR) GBC_P2XP(K, HV, T, I, B, W, S, PF, BR, false, 0)
+#define GBC_P2H(K, HV, T, I, B, W, S, PF, PD) GBC_P2XP(K, HV, T, I, B, W, S, PF, 0, true, PD)
+#define GBC_P2XP(K, HV, T, I, B, W, S, PF, BR, HF, PD)                                                  \
+    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR, HF, PD>,              \
+                   &k_pass2<K, HV, T, I, true, B, W, S, PF, BR, HF, PD>}
 template <bool HV> struct Variants<uint32_t, HV> {
-    static constexpr int count = 8;
+    static constexpr int count = 11;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
+            GBC_P2H(uint32_t, HV, 256, 24, 2, 4, false, true, 1),
+            GBC_P2H(uint32_t, HV, 256, 24, 2, 4, false, true, 0),
+            GBC_P2H(uint32_t, HV, 256, 24, 2, 4, true, true, 1),
             HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, true),
             HV ? GBC_P2R(uint32_t, HV, 256, 24, 2, 4, false, true, 1) : GBC_P2R(uint32_t, HV, 256, 24, 2, 4, true, true, 1),
             HV ? GBC_P2R(uint32_t, HV, 256, 24, 2, 4, false, true, 2) : GBC_P2R(uint32_t, HV, 256, 24, 2, 4, true, true, 2),
@@ -788,10 +834,12 @@ template <bool HV> struct Variants<uint32_t, HV> {
     }
 };
 template <bool HV> struct Variants<uint64_t, HV> {
-    static constexpr int count = 7;
+    static constexpr int count = 9;
     static PassVariant<uint64_t> get(int i)
     {
         static const PassVariant<uint64_t> v[count] = {
+            HV ? GBC_P2H(uint64_t, HV, 256, 20, 2, 4, false, true, 1) : GBC_P2H(uint64_t, HV, 256, 24, 2, 4, false, true, 1),
+            HV ? GBC_P2H(uint64_t, HV, 256, 20, 2, 4, false, true, 0) : GBC_P2H(uint64_t, HV, 256, 24, 2, 4, false, true, 0),
             HV ? GBC_P2(uint64_t, HV, 256, 20, 2, 4, false, true) : GBC_P2(uint64_t, HV, 256, 24, 2, 4, false, true),
             HV ? GBC_P2(uint64_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint64_t, HV, 256, 20, 2, 4, false, true),
             GBC_P2(uint64_t, HV, 256, 16, 2, 4, false, true),
@@ -807,12 +855,15 @@ template <bool HV> struct Variants<uint64_t, HV> {
 #undef GBC_P1B
 #undef GBC_P2
 #undef GBC_P2R
+#undef GBC_P2H
+#undef GBC_P2XP
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {
     const std::size_t tile = (std::size_t)pv.threads * pv.items;
     const std::size_t one = tile * sizeof(K) + (has_v ? tile * 4 : 0);  // a tile of keys (+ values)
-    const std::size_t per_warp = pv.second ? RADIX * 8 : RADIX * 4;  // counts and peer masks, or counts
+    // counts and peer masks (+ 32 words of bank offset for half-warp ranking), or counts
+    const std::size_t per_warp = pv.second ? RADIX * 8 + 128 : RADIX * 4;
     return (std::size_t)(pv.threads / 32) * per_warp + one * (pv.staged ? 2 : 1);
 }
 

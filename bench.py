@@ -775,13 +775,30 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     arena1 = ctx.arena_info()
     ok = bool(torch.equal(lout, pout))
     st = stats[-1].as_dict() if stats else {}
+
+    # the same sort at equal settings with the network trained by 32 Adam
+    # steps on the GPU, and with the root network alone (no second level)
+    def variant(**kw):
+        o = gbc.learned_options(**kw)
+        vs = []
+        ms_v, prof_v = timed(lambda: vs.append(gbc.sort_learned(ctx, lk.data_ptr(), lout.data_ptr(), np.float32, n,
+                                                                o)), max(3, steps // 5), warmup, ("learned.",))
+        return {"ms": ms_v, "speedup_vs_plain": ms_plain / ms_v, "bitexact": bool(torch.equal(lout, pout)),
+                "stats": vs[-1].as_dict(), "kernels": prof_v, "options": kw}
+
+    trained = variant(steps=32)
+    root_only = variant(refine=0)
     entry("learned_sort_f32_mixture_n2^28", n, "Gkeys/s", ms_learn, 36 * n, ok, prof_l,
           {"plain_sort_ms": ms_plain, "plain_sort_gkeys": n / (ms_plain * 1e-3) / 1e9,
            "speedup_vs_plain": ms_plain / ms_learn, "stats": st,
            "arena": {"before": arena0, "after": arena1},
-           "note": "includes sampling, the sample sort and the MLP fit; bytes = 36n: count (key read, u16 bucket "
-                   "write), group level (key + bucket read and write), bucket level (key + bucket read, key "
-                   "write), finish (read + write); oversized buckets move more"})
+           "trained_32_steps": trained, "root_network_only": root_only,
+           "training_pays": trained["ms"] < ms_learn,
+           "note": "default options: the data-driven initial network (no Adam steps) and the second level "
+                   "(1/3 of the buckets split oversized root buckets at sample quantiles); includes sampling, "
+                   "the sample sort and the splitters; bytes = 36n: count (key read, u16 bucket write), group "
+                   "level (key + bucket read and write), bucket level (key + bucket read, key write), finish "
+                   "(read + write); oversized buckets move more"})
     del lk, lout, pout
     torch.cuda.empty_cache()
 

@@ -262,12 +262,14 @@ typedef struct clc_learned_options {
     int sample;   /* sampled keys (0: 2^20) */
     int points;   /* training points from the sorted sample (0: 8192) */
     int buckets;  /* partition buckets (0: about n / 8192, at least 4096, as many as shared memory holds) */
-    int steps;    /* Adam steps (-1: 32) */
+    int steps;    /* Adam steps (-1: none, the data-driven initial network as fitted) */
     float lr;     /* Adam learning rate (0: 0.01) */
     int use_model;                 /* 0: equal-width buckets over the sampled key range (no network) */
     const float* params_in;        /* host, clc_learned_param_count() floats, or NULL (data-driven init) */
     float* params_out;             /* host, receives the fitted parameters, or NULL */
     const unsigned* splitters_in;  /* host, buckets - 1 order-preserving keys replacing the compiled ones, or NULL */
+    int refine; /* second model level: 1/refine of the buckets split the network's buckets that the sample predicts
+                   oversized, at the sample's quantiles (-1: 3, the default; 0: off) */
 } clc_learned_options;
 typedef struct clc_learned_stats {
     unsigned buckets, nonempty_buckets, largest_bucket;
@@ -277,6 +279,7 @@ typedef struct clc_learned_stats {
     unsigned violation;                         /* the boundary check failed */
     unsigned fallback;                          /* the plain radix sort produced the output */
     float first_loss, last_loss;                /* training loss at the first and last step */
+    unsigned refined_splitters;                 /* splitters added by the second model level */
 } clc_learned_stats;
 GBC_EXPORT void clc_learned_default_options(clc_learned_options* options);
 GBC_EXPORT clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,

@@ -818,7 +818,7 @@ clc_status clc_reduce_by_key_raw(clc_context ctx, const void* keys, clc_type key
 void clc_learned_default_options(clc_learned_options* o)
 {
     if (o == nullptr) return;
-    *o = clc_learned_options{0, 0, 0, -1, 0.f, 1, nullptr, nullptr, nullptr};
+    *o = clc_learned_options{0, 0, 0, -1, 0.f, 1, nullptr, nullptr, nullptr, -1};
 }
 
 int clc_learned_param_count(void) { return gbc::learned::NPARAM; }
@@ -843,6 +843,7 @@ clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out
             o.params_in = options->params_in;
             o.params_out = options->params_out;
             o.splitters_in = options->splitters_in;
+            o.refine = options->refine;
         }
         gbc::learned_stats s;
         gbc::learned_sort(*ctx->ctx, keys_in, keys_out, kind, n, o, &s);
@@ -850,7 +851,7 @@ clc_status clc_sort_learned(clc_context ctx, const void* keys_in, void* keys_out
             *stats = clc_learned_stats{s.buckets,       s.nonempty_buckets,         s.largest_bucket,
                                        s.oversized_buckets, s.oversized_keys,      s.constant_keys,
                                        s.estimated_oversized_keys, s.violation,    s.fallback,
-                                       s.first_loss,    s.last_loss};
+                                       s.first_loss,    s.last_loss,               s.refined_splitters};
     });
 }
 
@@ -876,6 +877,7 @@ clc_status clc_sort_learned_pairs(clc_context ctx, const void* keys_in, void* ke
             o.params_in = options->params_in;
             o.params_out = options->params_out;
             o.splitters_in = options->splitters_in;
+            o.refine = options->refine;
         }
         gbc::learned_stats s;
         gbc::learned_sort_pairs(*ctx->ctx, keys_in, keys_out, bytes, kind, vals_in, vals_out, n, o, &s);
@@ -883,7 +885,7 @@ clc_status clc_sort_learned_pairs(clc_context ctx, const void* keys_in, void* ke
             *stats = clc_learned_stats{s.buckets,       s.nonempty_buckets,         s.largest_bucket,
                                        s.oversized_buckets, s.oversized_keys,      s.constant_keys,
                                        s.estimated_oversized_keys, s.violation,    s.fallback,
-                                       s.first_loss,    s.last_loss};
+                                       s.first_loss,    s.last_loss,               s.refined_splitters};
     });
 }
 

@@ -447,6 +447,108 @@ __global__ void k_lut(const uint32_t* __restrict__ sp, uint32_t buckets, const F
     lut[c] = (uint16_t)lo;
 }
 
+// ---- 4b. second model level: oversized root buckets split at sample quantiles
+// The root model's bm - 1 splitters spm partition the sorted sample. A root
+// bucket whose expected size (its sample count scaled to n) exceeds cap and
+// whose sample keys are not all equal asks for ceil(size / target) - 1 more
+// splitters, placed at equally spaced positions of its own sample keys: a
+// piecewise model of the bucket's CDF, the leaf level of a recursive model
+// index whose root is the network. At most buckets - bm are added (scaled
+// down in proportion when more are asked); the final buckets - 1 splitters
+// are non-decreasing, the unused tail set to 2^32 - 1 (empty buckets).
+
+// want[b] = splitters root bucket b asks for; lo[b] = its first sample index.
+__global__ void k_refine_want(const uint32_t* __restrict__ sorted, uint32_t s, const uint32_t* __restrict__ spm,
+                              uint32_t bm, uint32_t n, uint32_t cap, uint32_t target, uint32_t* __restrict__ lo_out,
+                              uint32_t* __restrict__ want)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bm) return;
+    auto lower = [&](uint32_t v) {
+        uint32_t lo = 0, hi = s;
+        while (lo < hi) {
+            const uint32_t m = (lo + hi) >> 1;
+            if (sorted[m] < v) lo = m + 1;
+            else hi = m;
+        }
+        return lo;
+    };
+    const uint32_t lo = b == 0 ? 0u : lower(spm[b - 1]);
+    const uint32_t hi = b + 1 == bm ? s : lower(spm[b]);
+    uint32_t r = 0;
+    if (hi > lo + 1 && sorted[lo] != sorted[hi - 1]) {
+        const uint64_t size = (uint64_t)(hi - lo) * n / s;
+        if (size > cap) {
+            const uint64_t ask = (size + target - 1) / target - 1;
+            r = (uint32_t)(ask < (uint64_t)(hi - lo - 1) ? ask : (uint64_t)(hi - lo - 1));
+        }
+    }
+    lo_out[b] = lo;
+    want[b] = r;
+}
+
+constexpr int REFINE_THREADS = 1024;
+
+// One CTA: the granted count of every root bucket (want scaled to the budget)
+// replaced in place by its exclusive prefix; *added = the total granted.
+__global__ void __launch_bounds__(REFINE_THREADS) k_refine_plan(uint32_t* __restrict__ want, uint32_t bm,
+                                                                uint32_t budget, uint32_t* __restrict__ added)
+{
+    __shared__ uint32_t s_part[REFINE_THREADS];
+    __shared__ unsigned long long s_total;
+    const uint32_t per = (bm + REFINE_THREADS - 1) / REFINE_THREADS;
+    const uint32_t b0 = min(bm, threadIdx.x * per), b1 = min(bm, b0 + per);
+    if (threadIdx.x == 0) s_total = 0;
+    __syncthreads();
+    unsigned long long mine = 0;
+    for (uint32_t b = b0; b < b1; ++b) mine += want[b];
+    atomicAdd(&s_total, mine);
+    __syncthreads();
+    const unsigned long long total = s_total;
+    auto grant = [&](uint32_t w) -> uint32_t {
+        return total <= budget ? w : (uint32_t)(((unsigned long long)w * budget) / total);
+    };
+    uint32_t sum = 0;
+    for (uint32_t b = b0; b < b1; ++b) sum += grant(want[b]);
+    // exclusive scan of the per-thread sums (Hillis-Steele over 1024 words)
+    s_part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int d = 1; d < REFINE_THREADS; d <<= 1) {
+        const uint32_t v = threadIdx.x >= (uint32_t)d ? s_part[threadIdx.x - d] : 0u;
+        __syncthreads();
+        s_part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = s_part[threadIdx.x] - sum;
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t g = grant(want[b]);
+        want[b] = run;
+        run += g;
+    }
+    if (threadIdx.x == REFINE_THREADS - 1) *added = s_part[REFINE_THREADS - 1];
+}
+
+// The final splitters: root bucket b's granted splitters (offset off[b],
+// count off[b + 1] - off[b], or *added - off[b] for the last), then spm[b].
+__global__ void k_refine_write(const uint32_t* __restrict__ sorted, uint32_t s, const uint32_t* __restrict__ spm,
+                               uint32_t bm, uint32_t buckets, const uint32_t* __restrict__ lo_in,
+                               const uint32_t* __restrict__ off, const uint32_t* __restrict__ added,
+                               uint32_t* __restrict__ sp)
+{
+    const uint32_t total = *added;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < bm; b += stride) {
+        const uint32_t first = off[b], r = (b + 1 < bm ? off[b + 1] : total) - first;
+        const uint32_t lo = lo_in[b], hi = b + 1 < bm ? lo_in[b + 1] : s;
+        const uint32_t c = hi - lo;
+        const uint32_t base = b + first;  // b root splitters and `first` added ones come before
+        for (uint32_t j = 1; j <= r; ++j) sp[base + j - 1] = sorted[lo + (uint32_t)(((uint64_t)j * c) / (r + 1))];
+        if (b + 1 < bm) sp[base + r] = spm[b];
+    }
+    for (uint32_t i = bm - 1 + total + blockIdx.x * blockDim.x + threadIdx.x; i + 1 < buckets; i += stride)
+        sp[i] = 0xFFFFFFFFu;
+}
+
 // ---- 5. partition ----------------------------------------------------------
 struct PartArgs {
     const uint32_t* keys;
@@ -1052,12 +1154,13 @@ struct model_scratch {
     float* ys;
     uint32_t* sp;
     uint16_t* lut;
-    uint32_t* est;
+    uint32_t* est;     // [0] the sample estimate, [1] splitters added by the second level
+    uint32_t* refine;  // 3 x buckets words: root splitters, first sample index and grants per root bucket
 };
 
 uint32_t build_model(device_context& ctx, const uint32_t* sorted, uint32_t S, uint32_t M, uint32_t G,
                      uint32_t buckets, uint32_t n, uint32_t cap, bool skip_constant, const learned_options& opt,
-                     int steps, float lr, const model_scratch& m)
+                     int steps, float lr, const model_scratch& m, uint32_t* refined)
 {
     const bool own_init = opt.params_in == nullptr;
     if (!own_init)
@@ -1074,13 +1177,28 @@ uint32_t build_model(device_context& ctx, const uint32_t* sorted, uint32_t S, ui
     }
     {
         kernel_timer kt(ctx, "learned.splitters");
-        if (opt.splitters_in != nullptr)
+        // second level: a share 1/refine of the buckets splits oversized root buckets
+        const int refine = opt.refine < 0 ? 3 : opt.refine;
+        const uint32_t budget = opt.splitters_in == nullptr && refine > 0 ? buckets / (uint32_t)refine : 0u;
+        const uint32_t bm = buckets - budget;
+        if (opt.splitters_in != nullptr) {
             check_cuda(cudaMemcpyAsync(m.sp, opt.splitters_in, (std::size_t)(buckets - 1) * 4,
                                        cudaMemcpyHostToDevice, ctx.stream),
                        "cudaMemcpyAsync");
-        else
+        } else if (budget == 0) {
             k_splitters<<<(buckets + 127) / 128, 128, 0, ctx.stream>>>(m.params, m.frame, buckets, m.sp,
                                                                        opt.use_model ? 1 : 0);
+        } else {
+            uint32_t* spm = m.refine;      // bm - 1 root splitters
+            uint32_t* lo = spm + buckets;  // bm words
+            uint32_t* want = lo + buckets; // bm words
+            k_splitters<<<(bm + 127) / 128, 128, 0, ctx.stream>>>(m.params, m.frame, bm, spm, opt.use_model ? 1 : 0);
+            k_refine_want<<<(bm + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, spm, bm, n, cap, std::max(1u, cap / 2),
+                                                                     lo, want);
+            k_refine_plan<<<1, REFINE_THREADS, 0, ctx.stream>>>(want, bm, budget, m.est + 1);
+            k_refine_write<<<(bm + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, spm, bm, buckets, lo, want, m.est + 1,
+                                                                      m.sp);
+        }
         k_lut<<<(NCELLS + 1 + 255) / 256, 256, 0, ctx.stream>>>(m.sp, buckets, m.frame, m.lut);
         check_cuda(cudaGetLastError(), "learned splitter launch");
     }
@@ -1089,10 +1207,11 @@ uint32_t build_model(device_context& ctx, const uint32_t* sorted, uint32_t S, ui
     k_estimate<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, m.sp, buckets, n, cap,
                                                                skip_constant ? 1 : 0, m.est);
     check_cuda(cudaGetLastError(), "learned estimate launch");
-    uint32_t est = 0;
-    check_cuda(cudaMemcpyAsync(&est, m.est, 4, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
+    uint32_t est[2] = {0, 0};  // the estimate, the splitters the second level added
+    check_cuda(cudaMemcpyAsync(est, m.est, 8, cudaMemcpyDeviceToHost, ctx.stream), "cudaMemcpyAsync");
     ctx.finish();
-    return est;
+    if (refined != nullptr) *refined = est[1];
+    return est[0];
 }
 
 // Training losses (and the parameters, when asked) back to the host.
@@ -1134,7 +1253,12 @@ learned_shape shape_for(const device_context& ctx, std::size_t n, const learned_
         const uint32_t want = (uint32_t)((n / 8192 + 1023) / 1024 * 1024);
         sh.buckets = std::max<uint32_t>(4096, std::min<uint32_t>(want, max_buckets / 1024 * 1024));
     }
-    sh.steps = opt.steps >= 0 ? opt.steps : 32;
+    // Adam steps: none by default. The data-driven initial network (ramps
+    // between sample quantiles) is already a fit of the sample's CDF, and on
+    // the 2^28-key mixture gradient steps cost more than they save downstream
+    // (0, 8, 16, 32, 64 steps: 8.2, 8.4, 8.6, 8.9, 9.5 ms without the second
+    // level; 7.8 against 8.5 ms with it at 32 steps).
+    sh.steps = opt.steps >= 0 ? opt.steps : 0;
     sh.lr = opt.lr > 0 ? opt.lr : 0.01f;
     sh.G = train_grid(ctx, sh.M);
     return sh;
@@ -1143,15 +1267,16 @@ learned_shape shape_for(const device_context& ctx, std::size_t n, const learned_
 // The model stages' scratch: points, parameters and frame, training
 // partials, splitters and table, small words (barrier, statistics, losses).
 struct model_buffers {
-    temp_buffer pts, prm, partial, spl, misc;
+    temp_buffer pts, prm, partial, spl, misc, refine;
     model_scratch m;
-    uint32_t* dstats;  // [0..5] k_check statistics, [6] estimate
+    uint32_t* dstats;  // [0..5] k_check statistics, [6] estimate, [7] splitters added by the second level
     model_buffers(device_context& ctx, const learned_shape& sh)
         : pts(ctx.resource, (std::size_t)2 * sh.M * 4),
           prm(ctx.resource, (std::size_t)NPARAM * 4 + sizeof(Frame) + 16),
           partial(ctx.resource, (std::size_t)2 * sh.G * PSTR * 4),
           spl(ctx.resource, (std::size_t)sh.buckets * 4 + (std::size_t)(NCELLS + 1) * 2 + 16),
-          misc(ctx.resource, 64 + (std::size_t)std::max(sh.steps, 1) * 4)
+          misc(ctx.resource, 64 + (std::size_t)std::max(sh.steps, 1) * 4),
+          refine(ctx.resource, (std::size_t)3 * sh.buckets * 4)
     {
         check_cuda(cudaMemsetAsync(misc.get(), 0, 64 + (std::size_t)std::max(sh.steps, 1) * 4, ctx.stream),
                    "cudaMemsetAsync");
@@ -1167,6 +1292,7 @@ struct model_buffers {
         m.sp = spl.as<uint32_t>();
         m.lut = reinterpret_cast<uint16_t*>(m.sp + sh.buckets);
         m.est = dstats + 6;
+        m.refine = refine.as<uint32_t>();
     }
 };
 
@@ -1219,8 +1345,10 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     radix_sort(ctx, sample.get(), sample.get(), 4, 0, nullptr, nullptr, S, false);
     const bool train = opt.use_model && steps > 0;
     const uint32_t cap = segsort_cta_cap(4, false);
-    const uint32_t est =
-        build_model(ctx, sample.as<uint32_t>(), S, sh.M, sh.G, buckets, nn, cap, false, opt, steps, sh.lr, mb.m);
+    // buckets holding one key value need no sort, so they do not count
+    // against the model
+    const uint32_t est = build_model(ctx, sample.as<uint32_t>(), S, sh.M, sh.G, buckets, nn, cap, true, opt, steps,
+                                     sh.lr, mb.m, &st.refined_splitters);
     auto read_losses = [&] {
         if (train) read_training(ctx, opt, steps, mb.m.losses, mb.m.params, st);
     };
@@ -1379,7 +1507,7 @@ void learned_sort_pairs(device_context& ctx, const void* keys_in, void* keys_out
     // buckets holding one key value are left as the stable partition leaves
     // them (already in order), so they do not count against the model
     const uint32_t est = build_model(ctx, sample32.as<uint32_t>(), S, sh.M, sh.G, buckets, nn, cap, true, opt, steps,
-                                     sh.lr, mb.m);
+                                     sh.lr, mb.m, &st.refined_splitters);
     st.buckets = buckets;
     st.estimated_oversized_keys = (uint32_t)std::min<uint64_t>(n, (uint64_t)est * n / S);
     auto plain = [&] {

@@ -16,12 +16,14 @@ struct learned_options {
     int sample = 0;     // sampled keys (0: 2^20)
     int points = 0;     // training points taken from the sorted sample (0: 8192)
     int buckets = 0;    // partition buckets (0: from n, up to what shared memory holds)
-    int steps = -1;     // Adam steps (-1: 32)
+    int steps = -1;     // Adam steps (-1: none; the data-driven initial network is used as fitted)
     float lr = 0.f;     // Adam learning rate (0: 0.01)
     bool use_model = true;  // false: equal-width buckets over the sampled key range (no network)
     const float* params_in = nullptr;       // host: start from these parameters instead of the data-driven init
     float* params_out = nullptr;            // host: receives the fitted parameters
     const uint32_t* splitters_in = nullptr; // host: replaces the compiled splitters (buckets - 1 values)
+    int refine = -1;    // second level: 1/refine of the buckets split the root buckets the sample predicts
+                        // oversized, at sample quantiles (-1: 3; 0: off)
 };
 
 struct learned_stats {
@@ -35,6 +37,7 @@ struct learned_stats {
     uint32_t violation = 0;          // bucket order was not monotone
     uint32_t fallback = 0;           // the plain radix sort produced the output
     float first_loss = 0.f, last_loss = 0.f;
+    uint32_t refined_splitters = 0;  // splitters the second level added
 };
 
 //! Out-of-place sort of 32-bit keys (kind 0 unsigned, 1 signed, 2 float) by a

@@ -334,9 +334,14 @@ profiler::~profiler()
     for (auto e : free_) cudaEventDestroy(e);
 }
 
-kernel_timer::kernel_timer(device_context& ctx, const char* name) : ctx_(ctx), slot_(ctx.prof.start(ctx.stream, name)) {}
+kernel_timer::kernel_timer(device_context& ctx, const char* name) : kernel_timer(ctx, name, ctx.stream) {}
 
-kernel_timer::~kernel_timer() { ctx_.prof.stop(ctx_.stream, slot_); }
+kernel_timer::kernel_timer(device_context& ctx, const char* name, cudaStream_t stream)
+    : ctx_(ctx), stream_(stream), slot_(ctx.prof.start(stream, name))
+{
+}
+
+kernel_timer::~kernel_timer() { ctx_.prof.stop(stream_, slot_); }
 
 // ---- tuning table ---------------------------------------------------------
 

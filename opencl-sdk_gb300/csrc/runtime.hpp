@@ -156,13 +156,15 @@ struct device_context;
 //! Brackets one kernel launch for the context's profiler.
 class kernel_timer {
 public:
-    kernel_timer(device_context& ctx, const char* name);
+    kernel_timer(device_context& ctx, const char* name);                       // on the context's stream
+    kernel_timer(device_context& ctx, const char* name, cudaStream_t stream);  // on another stream of it
     ~kernel_timer();
     kernel_timer(const kernel_timer&) = delete;
     kernel_timer& operator=(const kernel_timer&) = delete;
 
 private:
     device_context& ctx_;
+    cudaStream_t stream_;
     int slot_;
 };
 

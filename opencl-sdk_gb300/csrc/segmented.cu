@@ -1073,13 +1073,16 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
         check_cuda(cudaGetLastError(), "segmented sort cta launch");
     }
     if (maybe_large) {
-        k_seg_plan<K, TILE><<<1, 1024, 0, aux>>>(a);
-        check_cuda(cudaGetLastError(), "segmented sort plan launch");
-        k_seg_large_zero<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
-        auto hk = &k_seg_large_count<K, TILE>;
-        hk<<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
-        k_seg_large_starts<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
-        check_cuda(cudaGetLastError(), "segmented sort histogram launch");
+        {
+            kernel_timer kt(ctx, "segsort.large_histogram", aux);
+            k_seg_plan<K, TILE><<<1, 1024, 0, aux>>>(a);
+            check_cuda(cudaGetLastError(), "segmented sort plan launch");
+            k_seg_large_zero<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
+            auto hk = &k_seg_large_count<K, TILE>;
+            hk<<<ctx.sm_count * occupancy(hk, 256, 0), 256, 0, aux>>>(a);
+            k_seg_large_starts<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
+            check_cuda(cudaGetLastError(), "segmented sort histogram launch");
+        }
         if (msd) {
             k_seg_route<K><<<ctx.sm_count * 4, 256, 0, aux>>>(a);
             check_cuda(cudaGetLastError(), "segmented sort route launch");
@@ -1089,6 +1092,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
         set_smem(pk, psmem);
         const int pgrid = ctx.sm_count * occupancy(pk, LS::THREADS, psmem);
         for (int s = 0; s < P; ++s) {
+            kernel_timer kt(ctx, "segsort.large_pass", aux);
             pk<<<pgrid, LS::THREADS, psmem, aux>>>(a, s);
             check_cuda(cudaGetLastError(), "segmented sort pass launch");
         }

@@ -687,14 +687,14 @@ def capture(ctx: Context, fn) -> Graph:
 class LearnedOptions(C.Structure):
     _fields_ = [("sample", C.c_int), ("points", C.c_int), ("buckets", C.c_int), ("steps", C.c_int),
                 ("lr", C.c_float), ("use_model", C.c_int), ("params_in", C.c_void_p), ("params_out", C.c_void_p),
-                ("splitters_in", C.c_void_p)]
+                ("splitters_in", C.c_void_p), ("refine", C.c_int)]
 
 
 class LearnedStats(C.Structure):
     _fields_ = [("buckets", C.c_uint), ("nonempty_buckets", C.c_uint), ("largest_bucket", C.c_uint),
                 ("oversized_buckets", C.c_uint), ("oversized_keys", C.c_uint), ("constant_keys", C.c_uint),
                 ("estimated_oversized_keys", C.c_uint), ("violation", C.c_uint), ("fallback", C.c_uint),
-                ("first_loss", C.c_float), ("last_loss", C.c_float)]
+                ("first_loss", C.c_float), ("last_loss", C.c_float), ("refined_splitters", C.c_uint)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

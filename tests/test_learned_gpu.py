@@ -1,6 +1,7 @@
 """Learned-CDF sort on the GPU: the network's gradients against the CPU
 oracle, output bit-identical to the plain radix sort, the gain of the trained
-network over bucketing without it, and the fallback to the plain radix sort
+network over bucketing without it, the second model level (oversized root
+buckets split at sample quantiles), and the fallback to the plain radix sort
 for a deliberately bad network."""
 import numpy as np
 import pytest
@@ -62,7 +63,7 @@ def learned(ctx, gbc, keys, **kw):
 def test_learned_sort_is_bit_identical_to_plain(ctx, gbc, n):
     keys = learned_mixture(n, seed=5)
     keys[:7] = np.array([-0.0, 0.0, np.inf, -np.inf, -0.0, 1e-45, -1e-45], dtype=np.float32)
-    out, st = learned(ctx, gbc, keys)
+    out, st = learned(ctx, gbc, keys, steps=32)
     ref = plain_sort(ctx, gbc, keys)
     assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
     assert st.violation == 0 and st.fallback == 0
@@ -74,8 +75,8 @@ def test_trained_network_beats_bucketing_without_it(ctx, gbc):
     # key domain; the mixture's narrow clusters then fill a few buckets far
     # beyond one CTA's shared-memory sort. The fitted CDF spreads them.
     keys = learned_mixture(1 << 22, seed=11)
-    opts = dict(buckets=4096)
-    out_l, st_l = learned(ctx, gbc, keys, **opts)
+    opts = dict(buckets=4096, refine=0)  # the root models alone
+    out_l, st_l = learned(ctx, gbc, keys, steps=32, **opts)
     out_u, st_u = learned(ctx, gbc, keys, use_model=0, **opts)
     out_0, st_0 = learned(ctx, gbc, keys, steps=0, **opts)  # initialised, not trained
     ref = plain_sort(ctx, gbc, keys).view(np.uint32)
@@ -125,9 +126,41 @@ def test_bad_network_falls_back_to_plain_sort(ctx, gbc):
     bad[0:H] = -30.0
     bad[2 * H:2 * H + H * H] = -30.0
     bad[3 * H + H * H:4 * H + H * H] = -30.0
-    out, st = learned(ctx, gbc, keys, steps=0, params_in=bad.ctypes.data)
+    out, st = learned(ctx, gbc, keys, steps=0, params_in=bad.ctypes.data, refine=0)
     assert st.fallback == 1 and st.estimated_oversized_keys > keys.size // 2
     assert np.array_equal(out.view(np.uint32), plain_sort(ctx, gbc, keys).view(np.uint32))
+
+
+def test_second_level_splits_oversized_buckets(ctx, gbc):
+    # The mixture's narrow clusters fill root buckets far beyond one CTA's
+    # shared-memory sort; the second level splits them at the sample's
+    # quantiles, which also isolates the clusters' repeated values in buckets
+    # of one key value (left unsorted). Output stays bit-identical.
+    keys = learned_mixture(1 << 22, seed=11)
+    ref = plain_sort(ctx, gbc, keys).view(np.uint32)
+    out_0, st_0 = learned(ctx, gbc, keys, steps=0, refine=0)
+    out_r, st_r = learned(ctx, gbc, keys, steps=0)
+    for out in (out_0, out_r):
+        assert np.array_equal(out.view(np.uint32), ref)
+    assert st_0.refined_splitters == 0 and st_r.refined_splitters > 0
+    assert st_r.refined_splitters <= st_r.buckets // 3
+    assert st_r.fallback == 0 and st_r.violation == 0
+    sorted_0 = st_0.oversized_keys - st_0.constant_keys  # keys the onesweep path sorts
+    sorted_r = st_r.oversized_keys - st_r.constant_keys
+    assert sorted_r * 2 < sorted_0
+
+
+def test_second_level_rescues_a_flat_network_exactly(ctx, gbc):
+    # With the root model flat (all keys in one root bucket) the second level
+    # alone partitions the keys; the bucketing stays monotone and exact.
+    keys = learned_mixture(1 << 20, seed=2)
+    bad = np.zeros(gbc.learned_param_count(), dtype=np.float32)
+    bad[0:H] = -30.0
+    bad[2 * H:2 * H + H * H] = -30.0
+    bad[3 * H + H * H:4 * H + H * H] = -30.0
+    out, st = learned(ctx, gbc, keys, steps=0, params_in=bad.ctypes.data)
+    assert np.array_equal(out.view(np.uint32), plain_sort(ctx, gbc, keys).view(np.uint32))
+    assert st.violation == 0 and st.refined_splitters > 0
 
 
 def ordered_u32(keys):
@@ -223,7 +256,7 @@ def test_learned_pairs_key_types_and_small_sizes(ctx, gbc, dtype):
 def test_learned_pairs_mixture_trains_and_partitions(ctx, gbc):
     keys = learned_mixture(1 << 22, seed=13)
     vals = np.arange(keys.size, dtype=np.uint32)
-    k, v, st = learned_pairs(ctx, gbc, keys, vals)
+    k, v, st = learned_pairs(ctx, gbc, keys, vals, steps=32)
     rk, rv = plain_pairs(ctx, gbc, keys, vals)
     assert np.array_equal(k.view(np.uint32), rk.view(np.uint32)) and np.array_equal(v, rv)
     assert st.fallback == 0 and st.violation == 0 and st.last_loss < st.first_loss
@@ -237,7 +270,7 @@ def test_learned_pairs_bad_network_falls_back(ctx, gbc):
     bad[0:H] = -30.0
     bad[2 * H:2 * H + H * H] = -30.0
     bad[3 * H + H * H:4 * H + H * H] = -30.0
-    k, v, st = learned_pairs(ctx, gbc, keys, vals, steps=0, params_in=bad.ctypes.data)
+    k, v, st = learned_pairs(ctx, gbc, keys, vals, steps=0, params_in=bad.ctypes.data, refine=0)
     rk, rv = plain_pairs(ctx, gbc, keys, vals)
     assert st.fallback == 1
     assert np.array_equal(k, rk) and np.array_equal(v, rv)

@@ -12,8 +12,9 @@ Printed (rank 0, one JSON line): Gkeys/s over the timed steps (CUDA events on
 the library's stream, max over ranks), the digit-pass kernel's achieved
 HBM bandwidth against MEASURED_PEAKS.json, an end-to-end figure through
 clc_buffer_write -> clc_sort -> clc_buffer_read from pinned host memory
-(double-buffered over two contexts and two host threads, with the one-step-
-at-a-time figure beside it), the
+(pipelined over three contexts and three host threads, one lane at a time
+per copy direction, with the one-step-at-a-time figure and its phases
+beside it), the
 CPU baseline (the oracle's restatement of the reference's 4-bit LSD sort on
 all host cores, on the same 2^28 pairs, with std::stable_sort on one thread
 beside it), SM clocks sampled during the run, and
@@ -496,41 +497,61 @@ def main() -> None:
     kb, vb = gbc.DeviceBuffer(ctx, n, np.uint32), gbc.DeviceBuffer(ctx, n, np.uint32)
     import ctypes as C
 
+    phases = {"write_ms": [], "sort_ms": [], "read_ms": []}
+
     def e2e_step():
+        t = time.perf_counter()
         gbc._raise_for(gbc.lib.clc_buffer_write(ctx.handle, kb.handle, 0, 4 * n, C.c_void_p(h_keys.data_ptr())))
         gbc._raise_for(gbc.lib.clc_buffer_write(ctx.handle, vb.handle, 0, 4 * n, C.c_void_p(h_vals.data_ptr())))
+        t1 = time.perf_counter()
         gbc._raise_for(gbc.lib.clc_sort(ctx.handle, kb.handle, gbc.TYPE_U32, vb.handle, n, 0))
         gbc._raise_for(gbc.lib.clc_buffer_read(ctx.handle, kb.handle, 0, 4 * n, C.c_void_p(h_keys_out.data_ptr())))
+        t2 = time.perf_counter()
         gbc._raise_for(gbc.lib.clc_buffer_read(ctx.handle, vb.handle, 0, 4 * n, C.c_void_p(h_vals_out.data_ptr())))
+        t3 = time.perf_counter()
+        # the blocking read of the keys waits for the sort: the sort's share is
+        # that read's time minus the values' read (same size)
+        phases["write_ms"].append((t1 - t) * 1e3)
+        phases["sort_ms"].append(((t2 - t1) - (t3 - t2)) * 1e3)
+        phases["read_ms"].append(2 * (t3 - t2) * 1e3)
 
     e2e_step()
     e2e_steps = max(3, min(args.steps, 10))
+    for v in phases.values():
+        v.clear()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     e2e_s = max_over_ranks(time.perf_counter() - t0) / e2e_steps
+    serial_phases = {k: round(statistics.median(v), 3) for k, v in phases.items()}
     e2e_ok = bool(torch.equal(h_keys_out, keys_out.cpu())) and bool(torch.equal(h_vals_out, vals_out.cpu()))
 
-    # The same steps double-buffered: a second context (its own stream and
-    # pool) on the device, two host threads taking alternate steps, so one
-    # step's transfers overlap the other's sort and opposite-direction copy.
-    # Every step still writes its keys and values from pinned host memory,
-    # sorts and reads both back (the calls block, as in the reference).
+    # The same steps pipelined over three lanes: three contexts on the device
+    # (each with its own stream and arena), three host threads taking
+    # alternate steps. A lane writes its inputs only while no other lane is
+    # writing, and reads its results only while no other lane is reading, so
+    # the two copy directions and the sorts overlap by construction: while
+    # one lane uploads, another sorts and a third downloads. Every step still
+    # writes its keys and values from pinned host memory, sorts and reads both
+    # back, through blocking calls as in the reference.
     import threading
 
-    ctx2 = gbc.Context(local)
-    kb2, vb2 = gbc.DeviceBuffer(ctx2, n, np.uint32), gbc.DeviceBuffer(ctx2, n, np.uint32)
-    h_keys_out2 = torch.empty_like(h_keys).pin_memory()
-    h_vals_out2 = torch.empty_like(h_vals).pin_memory()
-    lanes = [(ctx, kb, vb, h_keys_out, h_vals_out), (ctx2, kb2, vb2, h_keys_out2, h_vals_out2)]
+    extra = [gbc.Context(local) for _ in range(2)]
+    lanes = [(ctx, kb, vb, h_keys_out, h_vals_out)]
+    for c in extra:
+        lanes.append((c, gbc.DeviceBuffer(c, n, np.uint32), gbc.DeviceBuffer(c, n, np.uint32),
+                      torch.empty_like(h_keys).pin_memory(), torch.empty_like(h_vals).pin_memory()))
+    h2d_turn, d2h_turn = threading.Lock(), threading.Lock()
 
     def lane_step(c, kbuf, vbuf, ko, vo):
-        gbc._raise_for(gbc.lib.clc_buffer_write(c.handle, kbuf.handle, 0, 4 * n, C.c_void_p(h_keys.data_ptr())))
-        gbc._raise_for(gbc.lib.clc_buffer_write(c.handle, vbuf.handle, 0, 4 * n, C.c_void_p(h_vals.data_ptr())))
+        with h2d_turn:
+            gbc._raise_for(gbc.lib.clc_buffer_write(c.handle, kbuf.handle, 0, 4 * n, C.c_void_p(h_keys.data_ptr())))
+            gbc._raise_for(gbc.lib.clc_buffer_write(c.handle, vbuf.handle, 0, 4 * n, C.c_void_p(h_vals.data_ptr())))
         gbc._raise_for(gbc.lib.clc_sort(c.handle, kbuf.handle, gbc.TYPE_U32, vbuf.handle, n, 0))
-        gbc._raise_for(gbc.lib.clc_buffer_read(c.handle, kbuf.handle, 0, 4 * n, C.c_void_p(ko.data_ptr())))
-        gbc._raise_for(gbc.lib.clc_buffer_read(c.handle, vbuf.handle, 0, 4 * n, C.c_void_p(vo.data_ptr())))
+        with d2h_turn:
+            gbc._raise_for(gbc.lib.clc_buffer_read(c.handle, kbuf.handle, 0, 4 * n, C.c_void_p(ko.data_ptr())))
+            gbc._raise_for(gbc.lib.clc_buffer_read(c.handle, vbuf.handle, 0, 4 * n, C.c_void_p(vo.data_ptr())))
 
     def run_lanes(per_lane):
         errors = []
@@ -550,27 +571,32 @@ def main() -> None:
         if errors:
             raise errors[0]
 
-    run_lanes(2)  # warm-up: both contexts' pools and both lanes' first steps
-    per_lane = max(2, e2e_steps // 2)
+    run_lanes(1)  # warm-up: every context's arena and first step
+    per_lane = max(2, e2e_steps // len(lanes))
     barrier()
     t0 = time.perf_counter()
     run_lanes(per_lane)
-    pipe_s = max_over_ranks(time.perf_counter() - t0) / (2 * per_lane)
+    pipe_s = max_over_ranks(time.perf_counter() - t0) / (len(lanes) * per_lane)
     pipe_ok = all(bool(torch.equal(ko, keys_out.cpu())) and bool(torch.equal(vo, vals_out.cpu()))
                   for _, _, _, ko, vo in lanes)
     e2e = {"value": n * world / pipe_s / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": 8 * n,
            "d2h_bytes_per_step": 8 * n, "ms_per_step": pipe_s * 1e3, "bitexact": pipe_ok and e2e_ok,
-           "steps": 2 * per_lane,
-           "path": "per step: clc_buffer_write x2 (pinned host) -> clc_sort -> clc_buffer_read x2; two contexts "
-                   "on the device, two host threads taking alternate steps",
+           "steps": len(lanes) * per_lane,
+           "path": "per step: clc_buffer_write x2 (pinned host) -> clc_sort -> clc_buffer_read x2; three contexts "
+                   "on the device, three host threads taking alternate steps, one lane at a time per copy "
+                   "direction",
            "serial": {"value": n * world / e2e_s / 1e9, "ms_per_step": e2e_s * 1e3, "steps": e2e_steps,
+                      "phases": serial_phases,
                       "path": "the same calls, one context, one step at a time"}}
-    del h_keys, h_vals, h_keys_out, h_vals_out, h_keys_out2, h_vals_out2, lanes
+    del h_keys, h_vals, h_keys_out, h_vals_out
+    for _, kbuf, vbuf, _, _ in lanes[1:]:
+        kbuf.release()
+        vbuf.release()
+    del lanes
     kb.release()
     vb.release()
-    kb2.release()
-    vb2.release()
-    ctx2.close()
+    for c in extra:
+        c.close()
 
     workloads = {}
     if not args.no_extras:

@@ -689,6 +689,20 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     """The other configuration workloads, each timed the same way."""
     out = {}
 
+    def library_ms(fn, reps: int = 10) -> float:
+        """A library (torch/CUB) call's time, CUDA events around `reps` calls on
+        torch's current stream after warm-up: the comparator beside a kernel."""
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
     def entry(name, count, unit_name, ms, bytes_moved, ok, prof, extra=None):
         e = {"value": count / (ms * 1e-3) / 1e9, "unit": unit_name, "ms": ms,
              "hbm_frac": bytes_moved / (ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": bytes_moved,
@@ -749,13 +763,20 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     cs = torch.cumsum(x.to(torch.int64), 0)
     ok = int(total.item()) == int(cs[-1].item())
     ok = ok and bool(torch.equal(y[1:], cs[:-1].to(torch.int32))) and int(y[0].item()) == 0
-    entry("exclusive_scan_i32_n2^30", m, "Gelem/s", ms, 8 * m, ok, prof)
+    cub_ms = library_ms(lambda: torch.cumsum(x, 0, dtype=torch.int32, out=y))
+    entry("exclusive_scan_i32_n2^30", m, "Gelem/s", ms, 8 * m, ok, prof,
+          {"library_comparator": {"what": "torch.cumsum int32 -> int32 (CUB inclusive scan, no int64 total)",
+                                  "ms": cub_ms, "speedup": cub_ms / ms}})
     del cs
 
     # reduce (plus) of the same data
     xb = gbc.DeviceBuffer.wrap(ctx, x.data_ptr(), m, np.int32)
     ms, prof = timed(lambda: gbc.reduce(ctx, xb), steps, warmup, ("reduce.",))
-    entry("reduce_i32_n2^30", m, "Gelem/s", ms, 4 * m, True, prof, {"note": "includes the blocking result read"})
+    lib_ms = library_ms(lambda: torch.sum(x, dtype=torch.int64))
+    entry("reduce_i32_n2^30", m, "Gelem/s", ms, 4 * m, True, prof,
+          {"note": "includes the blocking result read",
+           "library_comparator": {"what": "torch.sum int32 -> int64 (no result read)", "ms": lib_ms,
+                                  "speedup": lib_ms / ms}})
 
     # copy_if ("x > 0") of the same data: stable compaction, count read back
     yb = gbc.DeviceBuffer.wrap(ctx, y.data_ptr(), m, np.int32)
@@ -763,8 +784,11 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ms, prof = timed(lambda: kept.append(gbc.copy_if(ctx, xb, yb, "x > 0")), steps, warmup, ("select.",))
     want = x[x > 0]
     ok = kept[-1] == want.numel() and bool(torch.equal(y[: kept[-1]], want))
+    lib_ms = library_ms(lambda: x[x > 0])
     entry("copy_if_i32_n2^30", m, "Gelem/s", ms, 4 * m + 4 * kept[-1], ok, prof,
-          {"predicate": "x > 0", "kept": int(kept[-1]), "note": "includes the blocking count read"})
+          {"predicate": "x > 0", "kept": int(kept[-1]), "note": "includes the blocking count read",
+           "library_comparator": {"what": "torch x[x > 0] (mask, then CUB select; blocking size read)", "ms": lib_ms,
+                                  "speedup": lib_ms / ms}})
     del want
 
     # transform: the Fahrenheit conversion of the reference's compute-pipeline
@@ -1057,7 +1081,9 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     ms, prof = timed(lambda: gbc.histogram_even_raw(ctx, u8.data_ptr(), m, np.uint8, hist.data_ptr(), 256, 0.0, 256.0),
                      steps, warmup, ("histogram.",))
     ok = bool(torch.equal(torch.bincount(u8.to(torch.int64), minlength=256).to(torch.int32), hist))
-    entry("histogram256_u8_n2^30", m, "Gelem/s", ms, m, ok, prof)
+    lib_ms = library_ms(lambda: torch.bincount(u8, minlength=256))
+    entry("histogram256_u8_n2^30", m, "Gelem/s", ms, m, ok, prof,
+          {"library_comparator": {"what": "torch.bincount on the uint8 tensor", "ms": lib_ms, "speedup": lib_ms / ms}})
     del u8
     torch.cuda.empty_cache()
 

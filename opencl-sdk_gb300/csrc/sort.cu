@@ -443,9 +443,14 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     contiguous run of the tile, so ranks stay in input order.
 // ---------------------------------------------------------------------------
 template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH, int BR,
-          bool HALF, int PAD>
+          bool HALF, int PAD, bool PACK = false>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
+    // PACK (32-bit keys with values): the locally sorted tile holds each key
+    // and its value side by side, placed with one 64-bit store instead of
+    // two 32-bit ones (2^28 pairs: 6.25 -> 6.07 ms with PAD 1, 6.07 -> 6.04
+    // with PAD 0; keys the AND of 4 words: 6.75 -> 6.52 ms).
+    static_assert(!PACK || (HAS_V && sizeof(K) == 4), "packed tiles hold 32-bit key-value pairs");
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
     constexpr int GROUPS = HALF ? 2 * WARPS : WARPS;  // ranking groups: warps or half-warps
@@ -685,8 +690,12 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t pos = warp_hist[grp * GSTRIDE + (rd[i] & 0xFFu)] + (rd[i] >> 8);
-            s_keys[pos] = key[i];
-            if (HAS_V) s_vals[pos] = val[i];
+            if constexpr (PACK) {
+                reinterpret_cast<uint2*>(s_keys)[pos] = make_uint2((uint32_t)key[i], val[i]);
+            } else {
+                s_keys[pos] = key[i];
+                if (HAS_V) s_vals[pos] = val[i];
+            }
         }
 
         // Decoupled look-back, one thread per digit, LBW status words per
@@ -745,10 +754,20 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         if (limit == (uint32_t)TILE) {
             uint32_t o[ITEMS];
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[tid + i * THREADS];
-            if (HAS_V) {
+            if constexpr (PACK) {
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[tid + i * THREADS];
+                for (int i = 0; i < ITEMS; ++i) {
+                    const uint2 kv = reinterpret_cast<const uint2*>(s_keys)[tid + i * THREADS];
+                    key[i] = (K)kv.x;
+                    val[i] = kv.y;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) key[i] = s_keys[tid + i * THREADS];
+                if (HAS_V) {
+#pragma unroll
+                    for (int i = 0; i < ITEMS; ++i) val[i] = s_vals[tid + i * THREADS];
+                }
             }
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) o[i] = s_bin_off[digit(key[i])] + tid + i * THREADS;
@@ -761,11 +780,11 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             }
         } else {
             for (uint32_t j = tid; j < limit; j += THREADS) {
-                const K kk = s_keys[j];
+                const K kk = PACK ? (K)reinterpret_cast<const uint2*>(s_keys)[j].x : s_keys[j];
                 const uint32_t o = s_bin_off[digit(kk)] + j;
                 if (o < n) {
                     dst_k[o] = kk;
-                    if (HAS_V) dst_v[o] = s_vals[j];
+                    if (HAS_V) dst_v[o] = PACK ? reinterpret_cast<const uint2*>(s_keys)[j].y : s_vals[j];
                 }
             }
         }
@@ -782,10 +801,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 }
 
 template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF, int BR,
-          bool HALF, int PAD>
+          bool HALF, int PAD, bool PACK = false>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR, HALF, PAD>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR, HALF, PAD, PACK>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -810,16 +829,18 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_P2(K, HV, T, I, B, W, S, PF) GBC_P2XP(K, HV, T, I, B, W, S, PF, 0, false, 0)
 #define GBC_P2R(K, HV, T, I, B, W, S, PF, BR) GBC_P2XP(K, HV, T, I, B, W, S, PF, BR, false, 0)
 #define GBC_P2H(K, HV, T, I, B, W, S, PF, PD) GBC_P2XP(K, HV, T, I, B, W, S, PF, 0, true, PD)
-#define GBC_P2XP(K, HV, T, I, B, W, S, PF, BR, HF, PD)                                                  \
-    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR, HF, PD>,              \
-                   &k_pass2<K, HV, T, I, true, B, W, S, PF, BR, HF, PD>}
+#define GBC_P2XP(K, HV, T, I, B, W, S, PF, BR, HF, PD) GBC_P2XPK(K, HV, T, I, B, W, S, PF, BR, HF, PD, false)
+#define GBC_P2XPK(K, HV, T, I, B, W, S, PF, BR, HF, PD, PK)                                                  \
+    PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR, HF, PD, PK>,              \
+                   &k_pass2<K, HV, T, I, true, B, W, S, PF, BR, HF, PD, PK>}
 template <bool HV> struct Variants<uint32_t, HV> {
     static constexpr int count = 11;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
-            GBC_P2H(uint32_t, HV, 256, 24, 2, 4, false, true, 1),
-            GBC_P2H(uint32_t, HV, 256, 24, 2, 4, false, true, 0),
+            // half-warp ranking, PAD 1 / PAD 0; key-value: the sorted tile as packed pairs
+            GBC_P2XPK(uint32_t, HV, 256, 24, 2, 4, false, true, 0, true, 1, HV),
+            GBC_P2XPK(uint32_t, HV, 256, 24, 2, 4, false, true, 0, true, 0, HV),
             GBC_P2H(uint32_t, HV, 256, 24, 2, 4, true, true, 1),
             HV ? GBC_P2(uint32_t, HV, 256, 24, 2, 4, false, true) : GBC_P2(uint32_t, HV, 256, 24, 2, 4, true, true),
             HV ? GBC_P2R(uint32_t, HV, 256, 24, 2, 4, false, true, 1) : GBC_P2R(uint32_t, HV, 256, 24, 2, 4, true, true, 1),
@@ -857,6 +878,7 @@ template <bool HV> struct Variants<uint64_t, HV> {
 #undef GBC_P2R
 #undef GBC_P2H
 #undef GBC_P2XP
+#undef GBC_P2XPK
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {

@@ -112,3 +112,30 @@ def test_rejections(gbc, ctx, orc):
     assert comp.num_elements == 0 and comp.compressed_bytes() == 0
     back = gbc.CompressedBuffer.deserialize(ctx, comp.serialize())
     assert back.num_elements == 0
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_both_decoders_every_width(gbc, ctx, orc, form):
+    # The one-pass decoder (lane-private whole words, the delta prefix sum
+    # by look-back) and the two-pass one (4-element groups, then a scan), each
+    # forced through the tuning table: chunks of every width 0..32, sizes that
+    # end inside a chunk and inside a lane's 32 elements, both modes.
+    rng = np.random.default_rng(40 + form)
+    ctx.tuning_set("bitpack:unpack", form)
+    try:
+        for chunk in (256, 2048, 65536):
+            for n in (5, 1000, 8192 * 3 + 33, 3 * chunk + 1237):
+                x = np.zeros(n, dtype=np.uint64)
+                for c in range((n + chunk - 1) // chunk):
+                    wbits = (5 * c + 1) % 33
+                    sl = slice(c * chunk, min(n, (c + 1) * chunk))
+                    hi = (1 << wbits) if wbits else 1
+                    x[sl] = 77 + rng.integers(0, hi, size=sl.stop - sl.start, dtype=np.uint64)
+                x = (x & 0xFFFFFFFF).astype(np.uint32)
+                steps = rng.integers(0, 50, n).astype(np.uint64)
+                ts = ((1700000000 + np.cumsum(steps)) & 0xFFFFFFFF).astype(np.uint32)
+                for data in (x, ts):
+                    for delta in (False, True):
+                        _roundtrip(gbc, ctx, orc, data, chunk, delta)
+    finally:
+        ctx.tuning_set("bitpack:unpack", -1)

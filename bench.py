@@ -519,12 +519,20 @@ def main() -> None:
     e2e_steps = max(3, min(args.steps, 10))
     for v in phases.values():
         v.clear()
+    arena_e2e = [ctx.arena_info()]
+    step_ms = []
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
         e2e_step()
+        step_ms.append((time.perf_counter() - ts) * 1e3)
     e2e_s = max_over_ranks(time.perf_counter() - t0) / e2e_steps
+    arena_e2e.append(ctx.arena_info())
     serial_phases = {k: round(statistics.median(v), 3) for k, v in phases.items()}
+    serial_phases["step_ms_min_median_max"] = [round(min(step_ms), 3), round(statistics.median(step_ms), 3),
+                                               round(max(step_ms), 3)]
+    serial_phases["arena_before_after"] = arena_e2e
     e2e_ok = bool(torch.equal(h_keys_out, keys_out.cpu())) and bool(torch.equal(h_vals_out, vals_out.cpu()))
 
     # The same steps pipelined over three lanes: three contexts on the device
@@ -573,19 +581,28 @@ def main() -> None:
 
     run_lanes(1)  # warm-up: every context's arena and first step
     per_lane = max(2, e2e_steps // len(lanes))
-    barrier()
-    t0 = time.perf_counter()
-    run_lanes(per_lane)
-    pipe_s = max_over_ranks(time.perf_counter() - t0) / (len(lanes) * per_lane)
+    # Three timed runs, the median reported (as the reference arm reports the
+    # median of its steps): a host-side stall of 40-100 ms, seen now and then
+    # on these machines in a single blocking copy, would otherwise decide the
+    # figure of a ~130 ms run.
+    runs_s = []
+    for _ in range(3):
+        barrier()
+        t0 = time.perf_counter()
+        run_lanes(per_lane)
+        runs_s.append(max_over_ranks(time.perf_counter() - t0) / (len(lanes) * per_lane))
+    pipe_s = statistics.median(runs_s)
     pipe_ok = all(bool(torch.equal(ko, keys_out.cpu())) and bool(torch.equal(vo, vals_out.cpu()))
                   for _, _, _, ko, vo in lanes)
     e2e = {"value": n * world / pipe_s / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": 8 * n,
            "d2h_bytes_per_step": 8 * n, "ms_per_step": pipe_s * 1e3, "bitexact": pipe_ok and e2e_ok,
-           "steps": len(lanes) * per_lane,
+           "steps": len(lanes) * per_lane, "runs_ms_per_step": [round(r * 1e3, 3) for r in runs_s],
+           "reported": "the median of three timed runs",
            "path": "per step: clc_buffer_write x2 (pinned host) -> clc_sort -> clc_buffer_read x2; three contexts "
                    "on the device, three host threads taking alternate steps, one lane at a time per copy "
                    "direction",
            "serial": {"value": n * world / e2e_s / 1e9, "ms_per_step": e2e_s * 1e3, "steps": e2e_steps,
+                      "median_step_value": n * world / (statistics.median(step_ms) * 1e-3) / 1e9,
                       "phases": serial_phases,
                       "path": "the same calls, one context, one step at a time"}}
     del h_keys, h_vals, h_keys_out, h_vals_out

@@ -173,6 +173,75 @@ __global__ void __launch_bounds__(THREADS) k_sel_count(SelArgs a, const __grid_c
     if (lane == 0) a.tiles[wi] = count;
 }
 
+// Pass 1 for the commonest predicates, `x OP literal` on 4-byte elements
+// (OP a comparison, the literal in x's own type: the program is a load of x
+// and one comparison with an immediate), with the comparison inlined instead
+// of interpreted: the interpreter's dispatch made the pass issue-bound (0.73
+// warp instructions per element for "x > 0"). Same masks and counts.
+template <typename T, int CMP> __device__ __forceinline__ bool compare(T x, T c)
+{
+    if constexpr (CMP == K_LT) return x < c;
+    else if constexpr (CMP == K_LE) return x <= c;
+    else if constexpr (CMP == K_GT) return x > c;
+    else if constexpr (CMP == K_GE) return x >= c;
+    else if constexpr (CMP == K_EQ) return x == c;
+    else return x != c;
+}
+
+template <typename T, int CMP>
+__global__ void __launch_bounds__(THREADS) k_sel_count_cmp(SelArgs a, T imm)
+{
+    using S = SelShape<4>;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t t = blockIdx.x;
+    const uint32_t wbase = t * S::TILE + warp * S::WARP_ELEMS;
+    uint32_t w[S::WORDS];
+    load_raw<4>(a, wbase, lane, w);
+    const bool whole = wbase + S::WARP_ELEMS <= a.n;
+    uint32_t count = 0, mine = 0;
+#pragma unroll
+    for (int j = 0; j < S::ITEMS; ++j) {
+        T x;
+        memcpy(&x, &w[j], 4);
+        const bool keep = compare<T, CMP>(x, imm) && (whole || wbase + ((j / S::V) * 32 + lane) * S::V + j % S::V < a.n);
+        const uint32_t m = __ballot_sync(FULL_MASK, keep);
+        count += __popc(m);
+        if (lane == j) mine = m;
+    }
+    const std::size_t wi = (std::size_t)t * WARPS + warp;
+    if (lane < S::ITEMS) a.masks[wi * S::ITEMS + lane] = mine;
+    if (lane == 0) a.tiles[wi] = count;
+}
+
+// The comparison kind when the program is `load x; compare with an immediate
+// of x's type` over a 4-byte element type, else -1.
+int simple_compare(const program& p)
+{
+    if (p.nops != 2) return -1;
+    const op& l = p.ops[0];
+    const op& c = p.ops[1];
+    if (l.kind != K_LOAD || l.src != S_X || l.t != p.x_ty) return -1;
+    if (c.kind < K_LT || c.kind > K_NE || c.src != S_IMM || c.t != p.x_ty) return -1;
+    if (p.x_ty != I32 && p.x_ty != U32 && p.x_ty != F32) return -1;
+    return c.kind;
+}
+
+template <typename T>
+void launch_count_cmp(device_context& ctx, const SelArgs& a, uint32_t num_tiles, int kind, uint64_t imm_bits)
+{
+    T imm;
+    const uint32_t b = (uint32_t)imm_bits;
+    memcpy(&imm, &b, 4);
+    switch (kind) {
+    case K_LT: k_sel_count_cmp<T, K_LT><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    case K_LE: k_sel_count_cmp<T, K_LE><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    case K_GT: k_sel_count_cmp<T, K_GT><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    case K_GE: k_sel_count_cmp<T, K_GE><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    case K_EQ: k_sel_count_cmp<T, K_EQ><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    default: k_sel_count_cmp<T, K_NE><<<num_tiles, THREADS, 0, ctx.stream>>>(a, imm); break;
+    }
+}
+
 // Pass 3 (after the exclusive scan of the warp counts), per warp: an
 // element's place among the warp's kept ones is the kept elements of earlier
 // rows, of lower lanes in its row (sum over the slots of popc(mask & lower
@@ -246,7 +315,15 @@ void run_select(device_context& ctx, const SelArgs& a0, const program& p, unsign
     a.masks = masks.as<uint32_t>();
     {
         kernel_timer kt(ctx, "select.count");
-        k_sel_count<SZ, W, STK><<<num_tiles, THREADS, slot_bytes, ctx.stream>>>(a, p);
+        const int cmp = SZ == 4 ? simple_compare(p) : -1;
+        if (cmp < 0)
+            k_sel_count<SZ, W, STK><<<num_tiles, THREADS, slot_bytes, ctx.stream>>>(a, p);
+        else if (p.x_ty == I32)
+            launch_count_cmp<int32_t>(ctx, a, num_tiles, cmp, p.ops[1].imm);
+        else if (p.x_ty == U32)
+            launch_count_cmp<uint32_t>(ctx, a, num_tiles, cmp, p.ops[1].imm);
+        else
+            launch_count_cmp<float>(ctx, a, num_tiles, cmp, p.ops[1].imm);
         check_cuda(cudaGetLastError(), "copy_if count launch");
     }
     const uint32_t zero = 0;

@@ -90,6 +90,18 @@ PREDICATES = [
     (np.uint8, "x - 100"),                      # int arithmetic after promotion
     (np.int16, "(x ^ 0x5555) < 0"),
     (np.int32, "(x+1) * ((x+2) * (x+3)) > 0"),  # uses the temporaries
+    # `x OP literal` on 4-byte elements: the inlined-comparison count pass
+    (np.int32, "x < -5"),
+    (np.int32, "x <= 7"),
+    (np.int32, "x >= -2147483647 - 1"),
+    (np.int32, "x == 0"),
+    (np.int32, "x != 3"),
+    (np.uint32, "x > 4000000000u"),
+    (np.uint32, "x == 5u"),
+    (np.float32, "x < 0.0f"),                   # NaN and -0.0 not kept
+    (np.float32, "x >= -0.0f"),
+    (np.float32, "x != 1.5f"),                  # NaN kept
+    (np.float32, "x == 0.0f"),                  # -0.0 kept
 ]
 
 
@@ -99,6 +111,8 @@ def sample(dtype, n, rng):
         v = (rng.standard_normal(n) * 2).astype(dt)
         v[::37] = np.nan
         v[::41] = 0.0
+        v[::43] = -0.0
+        v[::47] = 1.5
         return v
     info = np.iinfo(dt)
     v = rng.integers(info.min, info.max, size=n, dtype=dt, endpoint=True)

@@ -1,5 +1,5 @@
 // reduce_by_key over sorted keys, fused with a histogram of the low 16 key
-// bits: one single-pass decoupled look-back kernel.
+// bits.
 //
 // No reference counterpart (the reference has no reduce_by_key and no 64-bit
 // keys; the pipeline sort -> reduce_by_key -> histogram is the benchmark's).
@@ -8,34 +8,42 @@
 // the histogram bin (key & 0xFFFF) of every key gets +1, added once per run as
 // the run length.
 //
-// Each element contributes a state (h, s, c, p): h = it starts a run, s = the
-// sum since the latest run start, c = the number of run starts, p = the
-// position of the latest start. States combine in sequence order:
-//   A (+) B = (A.h | B.h, B.h ? B.s : A.s + B.s, A.c + B.c, B.h ? B.p : A.p),
-// which is associative; tiles publish their aggregate and inclusive states and
-// look back like the scan. The tile holding a run's last element knows the
-// run's index (c - 1), sum, start and hence length, and writes the run.
+// Each element contributes a state (s, c, p): s = the sum since the latest
+// run start, c = the number of run starts, p = the position of the latest
+// start. States combine in sequence order:
+//   A (+) B = (B.c ? B.s : A.s + B.s, A.c + B.c, B.c ? B.p : A.p),
+// which is associative. The element holding a run's last key knows the run's
+// index (c - 1), sum, start and hence length, and writes the run.
+//
+// Three passes over chunks of CHUNK keys (reduce, scan, reduce again), with
+// no look-back. A single-pass form with a decoupled look-back kept DRAM at
+// 18% of peak: its warps waited at the CTA barrier while the first warp
+// walked back (4.3 ms for 2^29 64-bit keys with 13M runs; these passes take
+// 0.79 + 0.05 + 1.28 ms there).
+//   1. k_rbk_chunk_states: a chunk's state from its keys (the number of run
+//      starts and the latest one) and the sum of the values from that start
+//      on (all of the chunk's values only when no run starts in it);
+//   2. k_rbk_scan_chunks: one CTA turns the chunk states into exclusive
+//      prefixes in place; the total's c is the number of runs;
+//   3. k_rbk_runs: each chunk, from its prefix, walks its elements in order
+//      and writes the runs that end in it, with their histogram bins.
 #include <cstring>
 #include <string>
 #include <type_traits>
 
 #include "device_common.cuh"
 #include "runtime.hpp"
-#include "sort_internal.hpp"
 
 namespace gbc {
 namespace {
 
 using dev::FULL_MASK;
-constexpr int ITEMS = 16;
-constexpr int LB_PER_LANE = 4;  // look-back window: 32 x 4 tiles per round trip
-constexpr uint64_t FLAG_AGG = 1, FLAG_PRE = 2;
-constexpr uint64_t TAG_MASK = (1ull << 29) - 1;
-constexpr uint64_t HEAD_BIT = 1ull << 61;
-constexpr uint64_t SLOTS = onesweep::RING_BYTES / 64;  // 8 words per tile
+constexpr int ITEMS = 16;           // consecutive keys per thread
+constexpr uint32_t CHUNK = 32768;   // keys per chunk: whole tiles of every CTA size
+constexpr int SCAN_THREADS = 1024;  // the chunk scan's one CTA
 
+// h is stored as c > 0 (a part holds a run start exactly when it counts one).
 struct State {
-    uint32_t h;  // 0/1
     uint64_t s;
     uint32_t c;
     uint32_t p;
@@ -44,17 +52,15 @@ struct State {
 __device__ __forceinline__ State combine(const State& a, const State& b)
 {
     State r;
-    r.h = a.h | b.h;
-    r.s = b.h ? b.s : a.s + b.s;
+    r.s = b.c ? b.s : a.s + b.s;
     r.c = a.c + b.c;
-    r.p = b.h ? b.p : a.p;
+    r.p = b.c ? b.p : a.p;
     return r;
 }
 
 __device__ __forceinline__ State shfl_up(const State& x, int d)
 {
     State y;
-    y.h = __shfl_up_sync(FULL_MASK, x.h, d);
     y.s = __shfl_up_sync(FULL_MASK, x.s, d);
     y.c = __shfl_up_sync(FULL_MASK, x.c, d);
     y.p = __shfl_up_sync(FULL_MASK, x.p, d);
@@ -63,7 +69,6 @@ __device__ __forceinline__ State shfl_up(const State& x, int d)
 __device__ __forceinline__ State shfl(const State& x, int src)
 {
     State y;
-    y.h = __shfl_sync(FULL_MASK, x.h, src);
     y.s = __shfl_sync(FULL_MASK, x.s, src);
     y.c = __shfl_sync(FULL_MASK, x.c, src);
     y.p = __shfl_sync(FULL_MASK, x.p, src);
@@ -81,28 +86,18 @@ __device__ __forceinline__ State warp_incl(State x)
     return x;
 }
 
-__device__ void publish(uint64_t* ring, uint64_t seq, uint64_t flag, const State& v)
+// A chunk's state in 16 bytes.
+__device__ __forceinline__ uint4 pack(const State& v)
 {
-    uint64_t* s = ring + (seq & (SLOTS - 1)) * 8;
-    const int o = flag == FLAG_PRE ? 2 : 0;
-    dev::st_relaxed(&s[o], v.s);
-    dev::st_relaxed(&s[o + 1], (uint64_t)v.c | ((uint64_t)v.p << 32));
-    dev::st_release(&s[4], (flag << 62) | (v.h ? HEAD_BIT : 0) | ((seq & TAG_MASK) << 32));
+    return make_uint4((uint32_t)v.s, (uint32_t)(v.s >> 32), v.c, v.p);
 }
-
-__device__ bool read(const uint64_t* ring, uint64_t seq, uint64_t& flag, State& v)
+__device__ __forceinline__ State unpack(const uint4 w)
 {
-    const uint64_t* s = ring + (seq & (SLOTS - 1)) * 8;
-    const uint64_t w = dev::ld_acquire(&s[4]);
-    flag = w >> 62;
-    if (flag == 0 || ((w >> 32) & TAG_MASK) != (seq & TAG_MASK)) return false;
-    const int o = flag == FLAG_PRE ? 2 : 0;
-    v.h = (w & HEAD_BIT) ? 1u : 0u;
-    v.s = dev::ld_relaxed(&s[o]);
-    const uint64_t cp = dev::ld_relaxed(&s[o + 1]);
-    v.c = (uint32_t)cp;
-    v.p = (uint32_t)(cp >> 32);
-    return true;
+    State v;
+    v.s = ((uint64_t)w.y << 32) | w.x;
+    v.c = w.z;
+    v.p = w.w;
+    return v;
 }
 
 template <typename K> struct RbkArgs {
@@ -111,199 +106,322 @@ template <typename K> struct RbkArgs {
     uint32_t n;
     K* keys_out;
     unsigned long long* sums_out;
-    uint32_t* counts_out;   // may be null
-    uint32_t* hist;         // 65536 bins or null
-    uint32_t* num_runs;     // device, written by the last tile
-    uint32_t num_tiles;
-    uint64_t* ring;
-    uint64_t seq0;
-    uint32_t* tile_ctr;
-    int* err;
+    uint32_t* counts_out;  // may be null
+    uint32_t* hist;        // 65536 bins or null
+    uint32_t* num_runs;    // device, or null
+    uint4* chunks;         // per chunk: its state (pass 1), then its exclusive prefix (pass 2)
+    uint32_t num_chunks;
 };
 
-// THREADS: 256, 128 or 64 per CTA. Every CTA's warps wait at a barrier while
-// its first warp looks back, so smaller CTAs (more of them per SM, each with
-// its own look-back in flight) keep more warps busy; registers cap any shape
-// at 16 warps per SM.
-template <typename K, int THREADS> __global__ void __launch_bounds__(THREADS) k_reduce_by_key(RbkArgs<K> a)
+// The thread's ITEMS consecutive keys from `first` (128-bit loads when whole
+// and aligned); valid: bit i set when first + i < n. Keys past n are 0.
+template <typename K>
+__device__ __forceinline__ void load_keys(const K* keys, uint32_t n, uint32_t first, bool aligned, K (&key)[ITEMS],
+                                          uint32_t& valid)
+{
+    if (aligned && first + ITEMS <= n) {
+        const uint4* kp = reinterpret_cast<const uint4*>(keys + first);
+#pragma unroll
+        for (int j = 0; j < ITEMS * (int)sizeof(K) / 16; ++j) {
+            const uint4 w = kp[j];
+            memcpy(reinterpret_cast<unsigned char*>(key) + 16 * j, &w, 16);
+        }
+        valid = (1u << ITEMS) - 1;
+        return;
+    }
+    valid = 0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t idx = first + i;
+        key[i] = idx < n ? keys[idx] : K(0);
+        if (idx < n) valid |= 1u << i;
+    }
+}
+
+// Bit i: element first + i starts a run (it is element 0 or differs from its
+// predecessor). The predecessor of the thread's first key is the previous
+// lane's last key; lane 0 reads it. Every lane of the warp calls this.
+template <typename K>
+__device__ __forceinline__ uint32_t run_starts(const K* keys, uint32_t first, const K (&key)[ITEMS], uint32_t valid,
+                                               int lane)
+{
+    K before = __shfl_up_sync(FULL_MASK, key[ITEMS - 1], 1);
+    if (lane == 0 && first > 0 && valid) before = keys[first - 1];
+    uint32_t head = 0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const K prev = i == 0 ? before : key[i - 1];
+        if (((valid >> i) & 1) && (first + i == 0 || key[i] != prev)) head |= 1u << i;
+    }
+    return head;
+}
+
+// The thread's part of the sum of v[from, end) over the CTA.
+template <int THREADS>
+__device__ __forceinline__ uint64_t range_sum(const uint32_t* v, uint32_t from, uint32_t end, int tid)
+{
+    uint64_t s = 0;
+    if (from >= end) return 0;
+    const bool al = (reinterpret_cast<uintptr_t>(v) & 15) == 0;
+    const uint32_t b0 = al ? min((from + 3u) & ~3u, end) : end;  // 128-bit loads from b0
+    for (uint32_t i = from + tid; i < b0; i += THREADS) s += v[i];
+    if (al) {
+        const uint32_t nq = (end - b0) >> 2;
+        const uint4* q = reinterpret_cast<const uint4*>(v + b0);
+#pragma unroll 4
+        for (uint32_t j = tid; j < nq; j += THREADS) {
+            const uint4 w = q[j];
+            s += (uint64_t)w.x + w.y + w.z + w.w;
+        }
+        for (uint32_t i = b0 + 4 * nq + tid; i < end; i += THREADS) s += v[i];
+    }
+    return s;
+}
+
+// Pass 1: a chunk's state. Its c and p come from the keys alone, read in
+// rows of 16 bytes per thread (consecutive threads, consecutive bytes; BATCH
+// rows in flight); its s is the sum of the values from its latest run start
+// to its end.
+template <typename K, int THREADS> __global__ void __launch_bounds__(THREADS) k_rbk_chunk_states(RbkArgs<K> a)
+{
+    constexpr int VEC = 16 / (int)sizeof(K);
+    constexpr uint32_t ROW = THREADS * VEC;  // keys per row of the CTA
+    constexpr int BATCH = 8;
+    constexpr int WARPS = THREADS / 32;
+    static_assert(CHUNK % (BATCH * ROW) == 0, "whole batches per chunk");
+    __shared__ uint32_t s_c[WARPS];
+    __shared__ int s_p[WARPS];
+    __shared__ unsigned long long s_s[WARPS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t c0 = blockIdx.x * CHUNK;
+    const uint32_t end = min(c0 + CHUNK, a.n);
+    const bool aligned = (reinterpret_cast<uintptr_t>(a.keys) & 15) == 0;
+    uint32_t cnt = 0;
+    int last = -1;  // the thread's latest run start
+    for (uint32_t rb = c0; rb < end; rb += BATCH * ROW) {  // the same for the whole CTA
+        K k[BATCH][VEC];
+#pragma unroll
+        for (int b = 0; b < BATCH; ++b) {
+            const uint32_t i0 = rb + b * ROW + tid * VEC;
+            if (aligned && i0 + VEC <= end) {
+                const uint4 w = *reinterpret_cast<const uint4*>(a.keys + i0);
+                memcpy(k[b], &w, 16);
+            } else {
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) k[b][v] = i0 + v < end ? a.keys[i0 + v] : K(0);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < BATCH; ++b) {
+            const uint32_t i0 = rb + b * ROW + tid * VEC;
+            K prev = __shfl_up_sync(FULL_MASK, k[b][VEC - 1], 1);
+            if (lane == 0 && i0 > 0 && i0 < end) prev = a.keys[i0 - 1];
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                const uint32_t idx = i0 + v;
+                const bool start = idx < end && (idx == 0 || k[b][v] != (v == 0 ? prev : k[b][v - 1]));
+                cnt += start ? 1u : 0u;
+                if (start) last = (int)idx;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
+        last = max(last, __shfl_xor_sync(FULL_MASK, last, o));
+    }
+    if (lane == 0) {
+        s_c[warp] = cnt;
+        s_p[warp] = last;
+    }
+    __syncthreads();
+    uint32_t C = 0;
+    int P = -1;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) {
+        C += s_c[w];
+        P = max(P, s_p[w]);
+    }
+    uint64_t sum = range_sum<THREADS>(a.vals, P >= 0 ? (uint32_t)P : c0, end, tid);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL_MASK, sum, o);
+    if (lane == 0) s_s[warp] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t S = 0;
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) S += s_s[w];
+        State v;
+        v.s = S;
+        v.c = C;
+        v.p = P >= 0 ? (uint32_t)P : 0u;
+        a.chunks[blockIdx.x] = pack(v);
+    }
+}
+
+// Pass 2, one CTA: the chunk states become their exclusive prefixes (the
+// empty state before chunk 0); the total's c, the number of runs, goes to
+// num_runs. Each thread takes a contiguous range of chunks.
+__global__ void __launch_bounds__(SCAN_THREADS) k_rbk_scan_chunks(uint4* chunks, uint32_t num, uint32_t* num_runs)
+{
+    static_assert(SCAN_THREADS == 32 * 32, "one lane of warp 0 per warp");
+    __shared__ State s_w[SCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t m = (num + SCAN_THREADS - 1) / SCAN_THREADS;
+    const uint32_t lo = min((uint32_t)tid * m, num), hi = min(lo + m, num);
+    State agg{0, 0, 0};
+#pragma unroll 8
+    for (uint32_t i = lo; i < hi; ++i) agg = combine(agg, unpack(chunks[i]));
+    const State incl = warp_incl(agg);
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const State wi = warp_incl(s_w[lane]);
+        const State wx = shfl_up(wi, 1);
+        s_w[lane] = lane == 0 ? State{0, 0, 0} : wx;
+        if (lane == 31 && num_runs != nullptr) *num_runs = wi.c;
+    }
+    __syncthreads();
+    State x = s_w[warp];
+    const State lx = shfl_up(incl, 1);
+    if (lane > 0) x = combine(x, lx);
+    for (uint32_t i = lo; i < hi; ++i) {
+        const State v = unpack(chunks[i]);
+        chunks[i] = pack(x);
+        x = combine(x, v);
+    }
+}
+
+// Where 16-byte chunk q of lane t's Q chunks sits in the warp's staging
+// area: the chunk index is XORed with bits of t so that 8 consecutive lanes
+// reading the same q (one shared-memory phase of 16-byte accesses) meet 8
+// different 16-byte bank groups, and so do 8 consecutive chunks stored by 8
+// consecutive lanes.
+template <int Q> __device__ __forceinline__ int staged(int t, int q)
+{
+    static_assert(Q == 4 || Q == 8, "4 or 8 chunks per lane");
+    return t * Q + (q ^ (Q == 8 ? (t & 7) : ((t >> 1) & 3)));
+}
+
+// Pass 3: from the chunk's prefix, each tile of the chunk in turn: the
+// threads' states, their exclusive prefixes (warp scans, then warp 0 over
+// the warp totals and the carried prefix), and the walk that writes every
+// run ending in the thread's elements. A whole, aligned tile is read by each
+// warp as rows of consecutive 16-byte chunks and handed to its lanes'
+// consecutive elements through shared memory (a lane reading its 16 keys
+// directly spreads each load over 32 lines: 2^29 64-bit keys, 1.79 ms).
+template <typename K, int THREADS> __global__ void __launch_bounds__(THREADS) k_rbk_runs(RbkArgs<K> a)
 {
     constexpr int TILE = THREADS * ITEMS;
-    __shared__ State s_warp[THREADS / 32];
-    __shared__ State s_prefix;
-    __shared__ uint32_t s_tile;
+    constexpr int SUB = CHUNK / TILE;
+    constexpr int WARPS = THREADS / 32;
+    constexpr int QK = ITEMS * (int)sizeof(K) / 16, QV = ITEMS * 4 / 16;  // 16-byte chunks per lane
+    // Two sets of warp prefixes, alternating by tile: a set is rewritten two
+    // tiles later, after every warp has passed a barrier that follows its read.
+    __shared__ State s_warp[2][WARPS];
+    __shared__ State s_carry;  // the prefix of the current tile
+    __shared__ uint4 s_stage[WARPS][32 * QK];  // a warp's keys, then its values
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t c0 = blockIdx.x * CHUNK;
     const bool aligned = ((reinterpret_cast<uintptr_t>(a.keys) | reinterpret_cast<uintptr_t>(a.vals)) & 15) == 0;
+    if (tid == 0) s_carry = unpack(a.chunks[blockIdx.x]);  // read by warp 0 after the first barrier
 
-    for (;;) {
-        // The tile index is taken only when the CTA can start on it; the
-        // tile a grid further on is prefetched into L2 (cf. the scan).
-        if (tid == 0) {
-            s_tile = atomicAdd(a.tile_ctr, 1u);
-            const uint64_t ahead = (uint64_t)s_tile + gridDim.x;
-            if (aligned && (ahead + 1) * TILE <= a.n) {
-                dev::prefetch_l2(a.keys + ahead * TILE, TILE * sizeof(K));
-                dev::prefetch_l2(a.vals + ahead * TILE, TILE * 4);
-            }
-        }
-        __syncthreads();
-        const uint32_t t = s_tile;
-        if (t >= a.num_tiles) break;
-        const uint32_t first = t * TILE + tid * ITEMS;  // blocked: this thread's items in order
-
+    for (int sub = 0; sub < SUB; ++sub) {
+        const uint32_t base = c0 + (uint32_t)sub * TILE;
+        if (base >= a.n) break;  // the same for the whole CTA
+        const uint32_t first = base + tid * ITEMS;
         K key[ITEMS];
         uint32_t val[ITEMS];
-        uint32_t head = 0, valid_mask = 0;
-        if (aligned && first + ITEMS <= a.n) {
-            // 128-bit loads of the thread's consecutive items
-            const uint4* kp = reinterpret_cast<const uint4*>(a.keys + first);
+        uint32_t valid;
+        if (aligned && base + TILE <= a.n) {
+            const uint32_t wfirst = base + warp * 32 * ITEMS;
+            const uint4* gk = reinterpret_cast<const uint4*>(a.keys + wfirst);
+            const uint4* gv = reinterpret_cast<const uint4*>(a.vals + wfirst);
+            uint4* st = s_stage[warp];
+            uint4 rk[QK], rv[QV];
 #pragma unroll
-            for (int j = 0; j < ITEMS * (int)sizeof(K) / 16; ++j) {
-                const uint4 w = kp[j];
-                memcpy(reinterpret_cast<unsigned char*>(key) + 16 * j, &w, 16);
-            }
-            const uint4* vp = reinterpret_cast<const uint4*>(a.vals + first);
+            for (int j = 0; j < QK; ++j) rk[j] = gk[j * 32 + lane];
 #pragma unroll
-            for (int j = 0; j < ITEMS / 4; ++j) {
-                const uint4 w = vp[j];
-                memcpy(&val[4 * j], &w, 16);
+            for (int j = 0; j < QV; ++j) rv[j] = gv[j * 32 + lane];
+#pragma unroll
+            for (int j = 0; j < QK; ++j) {
+                const int g = j * 32 + lane;
+                st[staged<QK>(g / QK, g % QK)] = rk[j];
             }
-            valid_mask = (ITEMS == 32) ? 0xFFFFFFFFu : ((1u << ITEMS) - 1);
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < QK; ++q) {
+                const uint4 w = st[staged<QK>(lane, q)];
+                memcpy(reinterpret_cast<unsigned char*>(key) + 16 * q, &w, 16);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int j = 0; j < QV; ++j) {
+                const int g = j * 32 + lane;
+                st[staged<QV>(g / QV, g % QV)] = rv[j];
+            }
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < QV; ++q) {
+                const uint4 w = st[staged<QV>(lane, q)];
+                memcpy(&val[4 * q], &w, 16);
+            }
+            valid = (1u << ITEMS) - 1;
         } else {
+            load_keys<K>(a.keys, a.n, first, false, key, valid);
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t idx = first + i;
-                if (idx < a.n) {
-                    key[i] = a.keys[idx];
-                    val[i] = a.vals[idx];
-                    valid_mask |= 1u << i;
-                } else {
-                    key[i] = 0;
-                    val[i] = 0;
-                }
-            }
+            for (int i = 0; i < ITEMS; ++i) val[i] = first + i < a.n ? a.vals[first + i] : 0u;
         }
-        const K before = (first > 0 && first - 1 < a.n) ? a.keys[first - 1] : K(0);
+        const uint32_t head = run_starts<K>(a.keys, first, key, valid, lane);
+        // Bit i of ends: element i is the last of its run, that is element i
+        // + 1 starts one, or i is the last element. The next lane's first
+        // element is the one after this lane's last; lane 31 compares keys.
+        uint32_t next_starts = __shfl_down_sync(FULL_MASK, head, 1) & 1u;
+        if (lane == 31) next_starts = first + ITEMS < a.n && a.keys[first + ITEMS] != key[ITEMS - 1];
+        uint32_t ends = ((head >> 1) | (next_starts << (ITEMS - 1))) & valid;
+        if (a.n - 1 - first < (uint32_t)ITEMS) ends |= 1u << (a.n - 1 - first);
+
+        // The thread's state: values past n are 0 and never start a run.
+        State st;
+        st.c = __popc(head);
+        st.p = head ? first + 31 - __clz(head) : 0u;
+        st.s = 0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t idx = first + i;
-            const K prev = i == 0 ? before : key[i - 1];
-            if (((valid_mask >> i) & 1) && (idx == 0 || key[i] != prev)) head |= 1u << i;
-        }
-        // thread state
-        State st{0, 0, 0, 0};
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            if (!((valid_mask >> i) & 1)) continue;
-            if ((head >> i) & 1) {
-                st.h = 1;
-                st.s = val[i];
-                st.c += 1;
-                st.p = first + i;
-            } else {
-                st.s += val[i];
-            }
-        }
+        for (int i = 0; i < ITEMS; ++i) st.s = ((head >> i) & 1) ? (uint64_t)val[i] : st.s + val[i];
         const State incl = warp_incl(st);
-        if (lane == 31) s_warp[warp] = incl;
+        State* sw = s_warp[sub & 1];
+        if (lane == 31) sw[warp] = incl;
         __syncthreads();
-
         if (warp == 0) {
-            // scan of the warp totals
-            State w = lane < THREADS / 32 ? s_warp[lane] : State{0, 0, 0, 0};
-            const State wi = warp_incl(w);
+            const State carry = s_carry;
+            const State wi = warp_incl(lane < WARPS ? sw[lane] : State{0, 0, 0});
             const State wx = shfl_up(wi, 1);
-            if (lane < THREADS / 32) s_warp[lane] = lane == 0 ? State{0, 0, 0, 0} : wx;
-            const State agg = shfl(wi, THREADS / 32 - 1);
-            const uint64_t my_seq = a.seq0 + t;
-            if (lane == 0) publish(a.ring, my_seq, t == 0 ? FLAG_PRE : FLAG_AGG, agg);
-            State excl{0, 0, 0, 0};
-            if (t > 0) {
-                // Look back over windows of 32 x LB_PER_LANE tiles (lane l
-                // inspects LB_PER_LANE consecutive ones); the nearest tile with
-                // an inclusive state ends the walk.
-                bool have = false, gave_up = false;
-                int64_t w_end = t;
-                for (;;) {
-                    uint64_t flag[LB_PER_LANE];
-                    State v[LB_PER_LANE];
-#pragma unroll
-                    for (int q = 0; q < LB_PER_LANE; ++q) {
-                        const int64_t k = w_end - 32 * LB_PER_LANE + lane * LB_PER_LANE + q;
-                        flag[q] = FLAG_PRE;  // before tile 0: the empty state
-                        v[q] = State{0, 0, 0, 0};
-                        if (k >= 0 && !read(a.ring, a.seq0 + (uint64_t)k, flag[q], v[q])) {
-                            const unsigned long long start = dev::globaltimer();
-                            for (uint32_t spin = 1;; ++spin) {
-                                if (read(a.ring, a.seq0 + (uint64_t)k, flag[q], v[q])) break;
-                                if ((spin & 255) == 0 && dev::globaltimer() - start > dev::SPIN_LIMIT_NS) {
-                                    gave_up = true;
-                                    flag[q] = FLAG_PRE;
-                                    v[q] = State{0, 0, 0, 0};
-                                    break;
-                                }
-                                if (spin > 32) __nanosleep(64);
-                            }
-                        }
-                    }
-                    int hi = -1;
-#pragma unroll
-                    for (int q = 0; q < LB_PER_LANE; ++q)
-                        if (flag[q] == FLAG_PRE) hi = q;
-                    const uint32_t pre = __ballot_sync(FULL_MASK, hi >= 0);
-                    const int L = pre ? 31 - __clz(pre) : -1;
-                    State contrib{0, 0, 0, 0};
-                    if (lane >= L) {
-                        const int q0 = lane == L ? hi : 0;
-#pragma unroll
-                        for (int q = 0; q < LB_PER_LANE; ++q)
-                            if (q >= q0) contrib = combine(contrib, v[q]);
-                    }
-                    const State ws = shfl(warp_incl(contrib), 31);
-                    excl = have ? combine(ws, excl) : ws;
-                    have = true;
-                    if (pre) break;
-                    w_end -= 32 * LB_PER_LANE;
-                }
-                if (__any_sync(FULL_MASK, gave_up) && lane == 0) dev::raise_error(a.err, dev::ERR_LOOKBACK_TIMEOUT);
-                if (lane == 0) publish(a.ring, my_seq, FLAG_PRE, combine(excl, agg));
-            }
-            if (lane == 0) {
-                s_prefix = excl;
-                if (t == a.num_tiles - 1 && a.num_runs != nullptr) *a.num_runs = combine(excl, agg).c;
-            }
+            const State agg = shfl(wi, WARPS - 1);
+            if (lane < WARPS) sw[lane] = lane == 0 ? carry : combine(carry, wx);
+            if (lane == 0) s_carry = combine(carry, agg);
         }
         __syncthreads();
 
-        // Walk this thread's items with the running state; close runs.
-        State run = combine(s_prefix, s_warp[warp]);
+        // The walk: the open run's sum element by element; at a run's end its
+        // index and start come from the run starts up to there (or, with none
+        // in this thread, from the incoming state).
+        State in = sw[warp];
         const State lx = shfl_up(incl, 1);
-        if (lane > 0) run = combine(run, lx);
-        const K after = (first + ITEMS < a.n) ? a.keys[first + ITEMS] : K(0);
+        if (lane > 0) in = combine(in, lx);
+        uint64_t sum = in.s;
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            if (!((valid_mask >> i) & 1)) continue;
-            const uint32_t idx = first + i;
-            if ((head >> i) & 1) {
-                run.h = 1;
-                run.s = val[i];
-                run.c += 1;
-                run.p = idx;
-            } else {
-                run.s += val[i];
-            }
-            const K next = i + 1 < ITEMS ? key[i + 1] : after;
-            const bool last = idx + 1 == a.n || ((i + 1 < ITEMS) ? ((valid_mask >> (i + 1)) & 1) == 0 || next != key[i]
-                                                                   : next != key[i]);
-            if (last && run.c > 0) {
-                const uint32_t r = run.c - 1;
-                const uint32_t len = idx - run.p + 1;
+            sum = ((head >> i) & 1) ? (uint64_t)val[i] : sum + val[i];
+            if ((ends >> i) & 1) {
+                const uint32_t upto = head & ((2u << i) - 1u);
+                const uint32_t r = in.c + __popc(upto) - 1u;  // element 0 starts a run: at least one start
+                const uint32_t len = first + i + 1u - (upto ? first + 31 - __clz(upto) : in.p);
                 a.keys_out[r] = key[i];
-                a.sums_out[r] = run.s;
+                a.sums_out[r] = sum;
                 if (a.counts_out) a.counts_out[r] = len;
                 if (a.hist) atomicAdd(&a.hist[(uint32_t)key[i] & 0xFFFFu], len);
             }
         }
-        __syncthreads();
     }
 }
 
@@ -323,14 +441,15 @@ void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const u
     }
     if (keys == nullptr || vals == nullptr || keys_out == nullptr || sums_out == nullptr)
         throw std::invalid_argument("reduce_by_key: null argument");
-    // CTA size from the tuning table (variant 0: 256 threads, 1: 128, 2: 64)
+    // CTA size from the tuning table: variant 0 (the default) 128 threads,
+    // 1: 64, 2: 256. Measured at 2^29 64-bit keys (13M runs), all three
+    // passes: 128 threads 2.16 ms, 64 2.32 ms, 256 2.37 ms.
     launch_shape shape;
     const std::string key = std::string("reduce_by_key:") + (key_bytes == 4 ? "u32" : "u64");
-    const int threads = ctx.tuning.lookup(key, shape) ? (shape.variant == 1 ? 128 : shape.variant == 2 ? 64 : 256)
-                                                      : 128;
-    const uint32_t num_tiles = (uint32_t)((n + (std::size_t)threads * ITEMS - 1) / ((std::size_t)threads * ITEMS));
-    unsigned char* ctl = ctx.d_small + 512;
-    check_cuda(cudaMemsetAsync(ctl, 0, 64, ctx.stream), "cudaMemsetAsync");
+    const int variant = ctx.tuning.lookup(key, shape) ? shape.variant : 0;
+    const int threads = variant == 1 ? 64 : variant == 2 ? 256 : 128;
+    const uint32_t num_chunks = (uint32_t)((n + CHUNK - 1) / CHUNK);
+    temp_buffer chunks(ctx.resource, (std::size_t)num_chunks * sizeof(uint4));
     auto launch = [&](auto tag, auto threads_tag) {
         using K = decltype(tag);
         constexpr int THREADS = decltype(threads_tag)::value;
@@ -343,18 +462,23 @@ void reduce_by_key(device_context& ctx, const void* keys, int key_bytes, const u
         a.counts_out = counts_out;
         a.hist = hist;
         a.num_runs = num_runs_device;
-        a.num_tiles = num_tiles;
-        a.ring = ctx.lookback_ring;
-        a.seq0 = ctx.reserve_seq(num_tiles);
-        a.tile_ctr = reinterpret_cast<uint32_t*>(ctl);
-        a.err = ctx.d_error;
-        int per_sm = 0;
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, &k_reduce_by_key<K, THREADS>, THREADS, 0),
-                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-        const int grid = (int)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * std::max(per_sm, 1));
-        kernel_timer kt(ctx, "reduce_by_key.lookback");
-        k_reduce_by_key<K, THREADS><<<grid, THREADS, 0, ctx.stream>>>(a);
-        check_cuda(cudaGetLastError(), "reduce_by_key launch");
+        a.chunks = chunks.as<uint4>();
+        a.num_chunks = num_chunks;
+        {
+            kernel_timer kt(ctx, "reduce_by_key.chunk_states");
+            k_rbk_chunk_states<K, THREADS><<<num_chunks, THREADS, 0, ctx.stream>>>(a);
+            check_cuda(cudaGetLastError(), "reduce_by_key chunk-state launch");
+        }
+        {
+            kernel_timer kt(ctx, "reduce_by_key.scan");
+            k_rbk_scan_chunks<<<1, SCAN_THREADS, 0, ctx.stream>>>(a.chunks, num_chunks, num_runs_device);
+            check_cuda(cudaGetLastError(), "reduce_by_key scan launch");
+        }
+        {
+            kernel_timer kt(ctx, "reduce_by_key.runs");
+            k_rbk_runs<K, THREADS><<<num_chunks, THREADS, 0, ctx.stream>>>(a);
+            check_cuda(cudaGetLastError(), "reduce_by_key runs launch");
+        }
     };
     auto by_threads = [&](auto tag) {
         if (threads == 64) launch(tag, std::integral_constant<int, 64>{});

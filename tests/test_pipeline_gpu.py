@@ -47,6 +47,51 @@ def test_reduce_by_key_long_runs_and_u32(ctx, gbc, orc):
         assert np.array_equal(co.to_host()[:runs], eco) and np.array_equal(hist.to_host(), eh)
 
 
+def _rbk_device(gbc, ctx, keys, vals, offset):
+    """reduce_by_key from device copies that start `offset` elements into
+    their buffers (offset 1: keys and values not 16-byte aligned)."""
+    n = keys.size
+    kb = gbc.DeviceBuffer.from_host(ctx, np.concatenate([np.zeros(offset, keys.dtype), keys]))
+    vb = gbc.DeviceBuffer.from_host(ctx, np.concatenate([np.zeros(offset, np.uint32), vals]))
+    ko, so = gbc.DeviceBuffer(ctx, n, keys.dtype), gbc.DeviceBuffer(ctx, n, np.uint64)
+    co, hist = gbc.DeviceBuffer(ctx, n, np.uint32), gbc.DeviceBuffer(ctx, 65536, np.uint32)
+    runs = gbc.reduce_by_key_raw(ctx, kb.device_pointer + offset * keys.itemsize, keys.dtype,
+                                 vb.device_pointer + offset * 4, n, ko.device_pointer, so.device_pointer,
+                                 co.device_pointer, hist.device_pointer)
+    return ko.to_host()[:runs], so.to_host()[:runs], co.to_host()[:runs], hist.to_host()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])  # 128, 64 and 256 threads per CTA
+@pytest.mark.parametrize("dtype", [np.uint32, np.uint64])
+def test_reduce_by_key_chunk_edges(ctx, gbc, orc, variant, dtype):
+    # The kernels work on chunks of 32,768 keys: runs that start exactly at a
+    # chunk's first key, end at its last, span whole chunks (no run start in
+    # them), single keys on both sides of a boundary, sizes one off a chunk,
+    # and unaligned keys and values.
+    c = 32768
+    rng = np.random.default_rng(variant * 10 + np.dtype(dtype).itemsize)
+    cases = [
+        np.repeat(np.arange(4, dtype=dtype), [c, c, 1, c - 1]),
+        np.repeat(np.arange(5, dtype=dtype), [c - 1, 1, 3 * c, 1, 5]),
+        np.repeat(np.arange(3, dtype=dtype), [1, 2 * c - 2, 1]),
+        np.arange(c + 1, dtype=dtype),
+        np.zeros(c - 1, dtype=dtype),
+        np.sort(rng.integers(0, 2000, size=5 * c + 123).astype(dtype)),
+    ]
+    key = "reduce_by_key:" + ("u32" if dtype == np.uint32 else "u64")
+    ctx.tuning_set(key, variant)
+    try:
+        for keys in cases:
+            vals = rng.integers(0, 2**32, size=keys.size, dtype=np.uint64).astype(np.uint32)
+            want = orc.std_reduce_by_key(keys, vals)
+            for offset in (0, 1):
+                got = _rbk_device(gbc, ctx, keys, vals, offset)
+                for g, w in zip(got, want):
+                    assert np.array_equal(g, w)
+    finally:
+        ctx.tuning_set(key, 0)
+
+
 def test_compute_pipeline_sample_flow(ctx, gbc, orc):
     # samples/core/compute-pipeline/main.cpp:94-183 with its default 1,000,000
     # readings, minus the file I/O, bitpack and static_map stages (outside the

@@ -508,9 +508,10 @@ GBC_EXPORT clc_status clc_tuning_save(clc_context ctx, const char* path);
  * caller's device data, stores the fastest in the context's tuning table
  * under the workload's key (element type and size class) and returns it with
  * its time per call. The entry applies to every key distribution of that
- * class, so the default variant 0 (the shape that holds up on skewed keys)
- * is kept unless another is more than 2% faster. keys_in must differ from
- * keys_out, which receives the sorted keys. Blocks. */
+ * class, so the default variant (the one used without an entry, a shape
+ * that holds up on skewed keys) is kept unless another is more than 2%
+ * faster. keys_in must differ from keys_out, which receives the sorted keys.
+ * Blocks. */
 GBC_EXPORT clc_status clc_autotune_sort(clc_context ctx, const void* keys_in, void* keys_out, clc_type key_type,
                                         const uint32_t* vals_in, uint32_t* vals_out, size_t n, int repetitions,
                                         int* best_variant, double* best_ms);

@@ -50,16 +50,16 @@ void check_args(const void* in, const void* out, int reps)
     if (reps < 1 || reps > 1000) throw std::invalid_argument("autotune: repetitions must be in [1, 1000]");
 }
 
-// The fastest candidate; with keep_first > 0, the first candidate (the
-// built-in default) unless the fastest beats it by more than that fraction.
-void pick(autotune_result& r, device_context& ctx, double keep_first = 0.0)
+// The fastest candidate; with margin > 0, candidate keep (the built-in
+// default) unless the fastest beats it by more than that fraction.
+void pick(autotune_result& r, device_context& ctx, double margin = 0.0, std::size_t keep = 0)
 {
     const auto it = std::min_element(r.ms.begin(), r.ms.end());
     r.best = r.candidates[it - r.ms.begin()];
     r.best_ms = *it;
-    if (keep_first > 0.0 && !r.ms.empty() && *it >= r.ms[0] * (1.0 - keep_first)) {
-        r.best = r.candidates[0];
-        r.best_ms = r.ms[0];
+    if (margin > 0.0 && keep < r.ms.size() && *it >= r.ms[keep] * (1.0 - margin)) {
+        r.best = r.candidates[keep];
+        r.best_ms = r.ms[keep];
     }
     launch_shape s;
     s.variant = r.best;
@@ -95,12 +95,12 @@ autotune_result autotune_sort(device_context& ctx, const void* keys_in, void* ke
         throw;
     }
     // The entry serves every key distribution of this size class, and the
-    // caller's keys are one of them. Variant 0 is the shape that holds up on
-    // skewed keys (half-warp count arrays one bank apart); PAD 0 is 0.5-1.3%
-    // faster on uniform 2^28 keys but 25-28% slower when the keys are the AND
-    // of 4 uniform words. So a variant replaces the default only when it is
-    // more than 2% faster on the caller's keys.
-    pick(r, ctx, 0.02);
+    // caller's keys are one of them. The defaults hold up on skewed keys
+    // (half-warp count arrays one bank apart); PAD 0 is 0.5-1.3% faster on
+    // uniform 2^28 keys but 25-28% slower when the keys are the AND of 4
+    // uniform words. So a variant replaces the default only when it is more
+    // than 2% faster on the caller's keys.
+    pick(r, ctx, 0.02, (std::size_t)sort_default_variant(key_bytes, kv, n));
     return r;
 }
 

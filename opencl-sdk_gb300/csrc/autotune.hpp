@@ -22,8 +22,8 @@ struct autotune_result {
 
 //! Plain radix sort: every compiled digit-pass variant (tile shape, CTAs per
 //! SM, look-back window, staging); keys_in must differ from keys_out. The
-//! default (variant 0) is kept unless another variant is more than 2% faster
-//! on the caller's keys.
+//! default (the variant used without a table entry) is kept unless another
+//! variant is more than 2% faster on the caller's keys.
 autotune_result autotune_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
                               const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, int repetitions);
 

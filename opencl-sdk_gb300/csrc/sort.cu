@@ -70,6 +70,12 @@ template <typename K> struct SortArgs {
     uint64_t seq0;
     uint32_t num_tiles;
     int* err;
+    // tile-offset form: per tile and digit, the tile's count, then its first
+    // output position; per chunk of tiles and digit, the same for the chunk
+    uint32_t* tile_off;
+    uint32_t* chunk_off;
+    uint32_t chunks;
+    uint32_t tiles_per_chunk;
 };
 
 // ---------------------------------------------------------------------------
@@ -417,6 +423,148 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 }
 
 // ---------------------------------------------------------------------------
+// Tile-offset form of the digit pass: every tile's output offsets are
+// computed before the pass (reduce, then scan), so the pass reads them
+// instead of looking back over its predecessors. Before each pass:
+//   k_tile_hist     each CTA counts the digits of every tile of a quarter of
+//                   a chunk (contiguous tiles) and adds them to the chunk's
+//                   totals;
+//   k_chunk_scan    the chunks' totals become their first output positions;
+//   k_tile_offsets  each chunk turns its tiles' counts into their first
+//                   output positions, in place.
+// The pass itself still takes its tiles in input order from the atomic
+// counter, so each digit's output is written in one advancing window. (With
+// each CTA sorting one chunk of tiles in order instead, 2^28 pairs took
+// 7.2 ms against 6.05: every (chunk, digit) is its own write stream.)
+// ---------------------------------------------------------------------------
+template <typename K>
+__device__ __forceinline__ const K* pass_src_keys(const SortArgs<K>& a, int slot, uint32_t act)
+{
+    if (slot == 0) return (a.in_place && (act & 1)) ? a.alt_keys : a.in_keys;
+    return ((act - slot) & 1) == 0 ? a.out_keys : a.alt_keys;
+}
+
+constexpr int TH_THREADS = 256;  // = RADIX: thread d owns digit d's counts
+constexpr int TH_SPLIT = 4;      // k_tile_hist CTAs per chunk
+
+template <typename K, bool IDENT, int TILE>
+__global__ void __launch_bounds__(TH_THREADS) k_tile_hist(SortArgs<K> a, int slot)
+{
+    constexpr int WARPS = TH_THREADS / 32;
+    constexpr int VEC = 16 / (int)sizeof(K);
+    constexpr int NV = (TILE / VEC + TH_THREADS - 1) / TH_THREADS;  // 16-byte loads per thread per tile
+    static_assert(TH_THREADS == RADIX && TILE % VEC == 0, "one thread per digit; whole vectors per tile");
+    __shared__ uint32_t h[WARPS][RADIX];  // per warp
+    const uint32_t act = a.ctl->plan.num_active;
+    if (slot >= (int)act) return;
+    const uint32_t shift = a.ctl->plan.shift[slot];
+    const K* src = pass_src_keys(a, slot, act);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int w = 0; w < WARPS; ++w) h[w][tid] = 0;
+    __syncthreads();
+    uint32_t* my = h[warp];
+    auto count = [&](K k) { atomicAdd(&my[(uint32_t)((IDENT ? k : a.xf(k)) >> shift) & 0xFFu], 1u); };
+    const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    const uint32_t chunk = blockIdx.x / TH_SPLIT, part = blockIdx.x % TH_SPLIT;
+    const uint32_t per = (a.tiles_per_chunk + TH_SPLIT - 1) / TH_SPLIT;
+    const uint32_t cend = min((chunk + 1) * a.tiles_per_chunk, a.num_tiles);
+    const uint32_t t0 = min(chunk * a.tiles_per_chunk + part * per, cend), t1 = min(t0 + per, cend);
+    uint32_t total = 0;
+    for (uint32_t t = t0; t < t1; ++t) {
+        const uint64_t b = (uint64_t)t * TILE;
+        if (aligned && b + TILE <= a.n) {
+            const uint4* v4 = reinterpret_cast<const uint4*>(src + b);
+            uint4 w[NV];
+#pragma unroll
+            for (int j = 0; j < NV; ++j)
+                if (j * TH_THREADS + tid < TILE / VEC) w[j] = dev::ld_stream(v4 + j * TH_THREADS + tid);
+#pragma unroll
+            for (int j = 0; j < NV; ++j)
+                if (j * TH_THREADS + tid < TILE / VEC) {
+                    K ks[VEC];
+                    memcpy(ks, &w[j], 16);
+#pragma unroll
+                    for (int q = 0; q < VEC; ++q) count(ks[q]);
+                }
+        } else {
+            const uint64_t e = min(b + TILE, (uint64_t)a.n);
+            for (uint64_t i = b + tid; i < e; i += TH_THREADS) count(src[i]);
+        }
+        __syncthreads();
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) {
+            c += h[w][tid];
+            h[w][tid] = 0;
+        }
+        a.tile_off[(size_t)t * RADIX + tid] = c;
+        total += c;
+        __syncthreads();
+    }
+    if (total != 0) atomicAdd(&a.chunk_off[(size_t)chunk * RADIX + tid], total);
+}
+
+// The chunks' counts of each digit become their first output positions
+// (the digit's start plus the counts of every earlier chunk), in place. One
+// warp per digit, 32 digits per CTA; lane l scans a contiguous run of chunks.
+template <typename K> __global__ void __launch_bounds__(1024) k_chunk_scan(SortArgs<K> a, int slot)
+{
+    const uint32_t act = a.ctl->plan.num_active;
+    if (slot >= (int)act) return;
+    const int lane = threadIdx.x & 31, d = blockIdx.x * 32 + (threadIdx.x >> 5);
+    uint32_t* col = a.chunk_off + d;
+    const uint32_t per = (a.chunks + 31) / 32;
+    const uint32_t c0 = min(lane * per, a.chunks), c1 = min(c0 + per, a.chunks);
+    uint32_t sum = 0;
+    for (uint32_t c = c0; c < c1; c += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = c + j < c1 ? col[(size_t)(c + j) * RADIX] : 0u;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sum += v[j];
+    }
+    const uint32_t incl = dev::warp_inclusive_scan(sum, [](uint32_t x, uint32_t y) { return x + y; });
+    uint32_t run = a.ctl->plan.bin_start[slot][d] + incl - sum;
+    for (uint32_t c = c0; c < c1; c += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = c + j < c1 ? col[(size_t)(c + j) * RADIX] : 0u;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (c + j < c1) {
+                col[(size_t)(c + j) * RADIX] = run;
+                run += v[j];
+            }
+    }
+}
+
+// Each chunk's tiles: counts become first output positions, in place
+// (thread d, digit d; the counts of 16 tiles in flight). The chunk's totals
+// are cleared for the next pass's k_tile_hist.
+template <typename K> __global__ void __launch_bounds__(RADIX) k_tile_offsets(SortArgs<K> a, int slot)
+{
+    constexpr int B = 16;
+    const uint32_t act = a.ctl->plan.num_active;
+    if (slot >= (int)act) return;
+    const int d = threadIdx.x;
+    uint32_t run = a.chunk_off[(size_t)blockIdx.x * RADIX + d];
+    a.chunk_off[(size_t)blockIdx.x * RADIX + d] = 0;
+    const uint32_t t0 = blockIdx.x * a.tiles_per_chunk, t1 = min(t0 + a.tiles_per_chunk, a.num_tiles);
+    uint32_t* col = a.tile_off + d;
+    for (uint32_t t = t0; t < t1; t += B) {
+        uint32_t v[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) v[j] = t + j < t1 ? col[(size_t)(t + j) * RADIX] : 0u;
+#pragma unroll
+        for (int j = 0; j < B; ++j)
+            if (t + j < t1) {
+                col[(size_t)(t + j) * RADIX] = run;
+                run += v[j];
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // K2, second form. The first form executes about 4.3 warp instructions per
 // key and keeps the ALU pipe ~64% busy while DRAM runs at ~15%: it is bound
 // by instruction issue (8 ballots per row of keys) and by its look-back,
@@ -443,9 +591,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_pass_mb(SortArgs<K> a, int sl
 //     contiguous run of the tile, so ranks stay in input order.
 // ---------------------------------------------------------------------------
 template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int LBW, bool STAGED, bool PREFETCH, int BR,
-          bool HALF, int PAD, bool PACK = false>
+          bool HALF, int PAD, bool PACK = false, bool TOFF = false>
 __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 {
+    // TOFF: the tile's output offsets come from tile_off (computed before the
+    // pass) instead of a look-back.
     // PACK (32-bit keys with values): the locally sorted tile holds each key
     // and its value side by side, placed with one 64-bit store instead of
     // two 32-bit ones (2^28 pairs: 6.25 -> 6.07 ms with PAD 1, 6.07 -> 6.04
@@ -514,6 +664,7 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
     if (tid < RADIX) s_bin_start[tid] = a.ctl->plan.bin_start[slot][tid];
     const uint64_t seq0 = a.seq0 + (uint64_t)slot * a.num_tiles;
     uint32_t* ctr = &a.ctl->tile_ctr[slot];
+    auto take = [&]() -> uint32_t { return atomicAdd(ctr, 1u); };  // thread 0: the next tile
     const uint32_t n = a.n;
     // Bulk copies need 16-byte aligned sources; a partial last tile is loaded
     // by plain loads.
@@ -539,13 +690,13 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             dev::mbar_init(&s_bar[1], 1);
             dev::fence_mbar_init();
         }
-        issue(0, atomicAdd(ctr, 1u));
+        issue(0, take());
     }
     int st = 0;
     uint32_t parity = 0;  // bit s: phase parity of stage s's barrier
 
     for (;;) {
-        if (STAGED && tid == 0) issue(st ^ 1, atomicAdd(ctr, 1u));  // the next tile's copy
+        if (STAGED && tid == 0) issue(st ^ 1, take());  // the next tile's copy
         if (PREFETCH && tid == 0) {
             // The tile a grid further on, which some CTA takes about one
             // tile-time from now, is prefetched into L2.
@@ -561,6 +712,8 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         if (t >= a.num_tiles) break;
         const uint32_t tile_base = t * TILE;
         const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+        // TOFF: digit tid's first output position for this tile, used after ranking
+        const uint32_t toff = TOFF && tid < RADIX ? a.tile_off[(size_t)t * RADIX + tid] : 0u;
         K* s_keys = reinterpret_cast<K*>(tiles + (STAGED ? st : 0) * STAGE_BYTES);
         uint32_t* s_vals = reinterpret_cast<uint32_t*>(tiles + (STAGED ? st : 0) * STAGE_BYTES + KEY_BYTES);
         const bool staged = s_inflight[st] != 0;
@@ -676,7 +829,7 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         uint32_t agg = count;
         if (tid == RADIX - 1) agg -= (uint32_t)TILE - valid;  // padding sits in bin 255
         uint64_t* my_status = a.ring + ((seq0 + t) & (RING_TILES - 1)) * RADIX;
-        if (tid < RADIX)
+        if (!TOFF && tid < RADIX)
             dev::st_relaxed(&my_status[tid], pack_status(t == 0 ? FLAG_PRE : FLAG_AGG, seq0 + t, agg));
         const uint32_t local = dev::bins_exclusive_sum(count, s_scratch);
         if (tid < RADIX) {
@@ -698,9 +851,11 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
             }
         }
 
-        // Decoupled look-back, one thread per digit, LBW status words per
-        // round trip.
-        if (tid < RADIX) {
+        // The tile's offsets: read (TOFF) or from a decoupled look-back, one
+        // thread per digit, LBW status words per round trip.
+        if (TOFF) {
+            if (tid < RADIX) s_bin_off[tid] = toff - s_local[tid];
+        } else if (tid < RADIX) {
             uint32_t excl = 0;
             if (t > 0) {
                 int64_t k = (int64_t)t - 1;
@@ -749,11 +904,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
         // consecutive addresses); unstaged, the next tile's index is fetched
         // meanwhile. After a timed-out wait the offsets are unknown: nothing
         // is written.
-        if (!STAGED && tid == 0) s_stage_tile[0] = atomicAdd(ctr, 1u);
+        if (!STAGED && tid == 0) s_stage_tile[0] = take();
         const uint32_t limit = s_abort ? 0u : valid;
         if (limit == (uint32_t)TILE) {
             uint32_t o[ITEMS];
-#pragma unroll
             if constexpr (PACK) {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
@@ -801,10 +955,10 @@ __device__ __forceinline__ void pass2_body(const SortArgs<K>& a, int slot)
 }
 
 template <typename K, bool HAS_V, int THREADS, int ITEMS, bool IDENT, int MINB, int LBW, bool STAGED, bool PF, int BR,
-          bool HALF, int PAD, bool PACK = false>
+          bool HALF, int PAD, bool PACK = false, bool TOFF = false>
 __global__ void __launch_bounds__(THREADS, MINB) k_pass2(SortArgs<K> a, int slot)
 {
-    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR, HALF, PAD, PACK>(a, slot);
+    pass2_body<K, HAS_V, THREADS, ITEMS, IDENT, LBW, STAGED, PF, BR, HALF, PAD, PACK, TOFF>(a, slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -816,6 +970,10 @@ template <typename K> struct PassVariant {
     bool staged;                             // second form: next tile bulk-copied into a second stage
     void (*kernel)(SortArgs<K>, int);        // any key transform
     void (*kernel_ident)(SortArgs<K>, int);  // identity transform (unsigned ascending)
+    // tile-offset form (second form): the per-tile digit counts pass run
+    // before each digit pass (null otherwise)
+    void (*hist)(SortArgs<K>, int) = nullptr;
+    void (*hist_ident)(SortArgs<K>, int) = nullptr;
 };
 
 template <typename K, bool HAS_V> struct Variants;
@@ -833,8 +991,17 @@ template <typename K, bool HAS_V> struct Variants;
 #define GBC_P2XPK(K, HV, T, I, B, W, S, PF, BR, HF, PD, PK)                                                  \
     PassVariant<K>{T, I, true, S, &k_pass2<K, HV, T, I, false, B, W, S, PF, BR, HF, PD, PK>,              \
                    &k_pass2<K, HV, T, I, true, B, W, S, PF, BR, HF, PD, PK>}
+#define GBC_P2T(K, HV, T, I, B, PF, HF, PD, PK)                                                           \
+    PassVariant<K>{T, I, true, false, &k_pass2<K, HV, T, I, false, B, 4, false, PF, 0, HF, PD, PK, true>, \
+                   &k_pass2<K, HV, T, I, true, B, 4, false, PF, 0, HF, PD, PK, true>,                      \
+                   &k_tile_hist<K, false, T * I>, &k_tile_hist<K, true, T * I>}
 template <bool HV> struct Variants<uint32_t, HV> {
-    static constexpr int count = 11;
+    static constexpr int count = 13;
+    // The tile-offset form (PAD 1), the default for keys without values from
+    // 2^27 keys when the tuning table has no entry (2^28 uniform: 4.77 ms
+    // against 5.04; 2^27: 2.45 against 2.53; smaller sizes and key-value
+    // sorts are faster with the look-back).
+    static constexpr int TILE_OFFSETS = 11;
     static PassVariant<uint32_t> get(int i)
     {
         static const PassVariant<uint32_t> v[count] = {
@@ -850,6 +1017,8 @@ template <bool HV> struct Variants<uint32_t, HV> {
             GBC_P2(uint32_t, HV, 384, 16, 2, 4, false, true),
             GBC_P1(uint32_t, HV, 256, 16, false),
             GBC_P1B(uint32_t, HV, 256, 16, 3),
+            GBC_P2T(uint32_t, HV, 256, 24, 2, true, true, 1, HV),
+            GBC_P2T(uint32_t, HV, 256, 24, 2, true, true, 0, HV),
         };
         return v[std::min(std::max(i, 0), count - 1)];
     }
@@ -879,6 +1048,7 @@ template <bool HV> struct Variants<uint64_t, HV> {
 #undef GBC_P2H
 #undef GBC_P2XP
 #undef GBC_P2XPK
+#undef GBC_P2T
 
 template <typename K> std::size_t pass_smem(const PassVariant<K>& pv, bool has_v)
 {
@@ -955,6 +1125,10 @@ static void run_sort(device_context& ctx, const K* in_k, K* out_k, const uint32_
     a.seq0 = ctx.reserve_seq((uint64_t)P * num_tiles);
     a.num_tiles = num_tiles;
     a.err = ctx.d_error;
+    a.tile_off = nullptr;
+    a.chunk_off = nullptr;
+    a.chunks = 0;
+    a.tiles_per_chunk = 0;
 
     // K1
     constexpr int HT = 256, NSUB = 2;
@@ -981,10 +1155,44 @@ static void run_sort(device_context& ctx, const K* in_k, K* out_k, const uint32_
     auto* pk = ident ? pv.kernel_ident : pv.kernel;
     const int pblocks = prepare_kernel(pk, pv.threads, psmem, g_occupancy, g_occupancy_mutex);
     const int pgrid = (int)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * pblocks);
+    if (pv.hist == nullptr) {
+        for (int s = 0; s < P; ++s) {
+            kernel_timer kt(ctx, "sort.digit_pass");
+            pk<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
+            check_cuda(cudaGetLastError(), "radix sort pass launch");
+        }
+        return;
+    }
+    // Tile offsets: chunks of contiguous tiles, 2 per SM (fewer when the
+    // tiles do not fill them), each counted by TH_SPLIT CTAs.
+    const uint32_t want_chunks = (uint32_t)std::min<std::size_t>(num_tiles, (std::size_t)ctx.sm_count * 2);
+    a.tiles_per_chunk = (num_tiles + want_chunks - 1) / want_chunks;
+    a.chunks = (num_tiles + a.tiles_per_chunk - 1) / a.tiles_per_chunk;
+    temp_buffer tile_off(ctx.resource, (std::size_t)num_tiles * RADIX * sizeof(uint32_t));
+    temp_buffer chunk_off(ctx.resource, (std::size_t)a.chunks * RADIX * sizeof(uint32_t));
+    a.tile_off = tile_off.as<uint32_t>();
+    a.chunk_off = chunk_off.as<uint32_t>();
+    check_cuda(cudaMemsetAsync(a.chunk_off, 0, (std::size_t)a.chunks * RADIX * sizeof(uint32_t), ctx.stream),
+               "cudaMemsetAsync");
+    auto* hk = ident ? pv.hist_ident : pv.hist;
     for (int s = 0; s < P; ++s) {
-        kernel_timer kt(ctx, "sort.digit_pass");
-        pk<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
-        check_cuda(cudaGetLastError(), "radix sort pass launch");
+        {
+            kernel_timer kt(ctx, "sort.tile_histogram");
+            hk<<<a.chunks * TH_SPLIT, TH_THREADS, 0, ctx.stream>>>(a, s);
+            check_cuda(cudaGetLastError(), "radix sort tile histogram launch");
+        }
+        {
+            kernel_timer kt(ctx, "sort.tile_offsets");
+            k_chunk_scan<K><<<RADIX / 32, 1024, 0, ctx.stream>>>(a, s);
+            check_cuda(cudaGetLastError(), "radix sort chunk scan launch");
+            k_tile_offsets<K><<<a.chunks, RADIX, 0, ctx.stream>>>(a, s);
+            check_cuda(cudaGetLastError(), "radix sort tile offsets launch");
+        }
+        {
+            kernel_timer kt(ctx, "sort.digit_pass");
+            pk<<<pgrid, pv.threads, psmem, ctx.stream>>>(a, s);
+            check_cuda(cudaGetLastError(), "radix sort pass launch");
+        }
     }
 }
 
@@ -995,6 +1203,12 @@ int sort_variant_count(int key_bytes, bool has_values)
     using namespace onesweep;
     if (key_bytes == 4) return has_values ? Variants<uint32_t, true>::count : Variants<uint32_t, false>::count;
     return has_values ? Variants<uint64_t, true>::count : Variants<uint64_t, false>::count;
+}
+
+int sort_default_variant(int key_bytes, bool has_values, std::size_t n)
+{
+    using namespace onesweep;
+    return key_bytes == 4 && !has_values && n >= (std::size_t(1) << 27) ? Variants<uint32_t, false>::TILE_OFFSETS : 0;
 }
 
 std::string sort_tuning_key(int key_bytes, bool has_values, std::size_t n)
@@ -1031,7 +1245,7 @@ void radix_sort(device_context& ctx, const void* keys_in, void* keys_out, int ke
     check_size(n);
     const bool kv = vals_in != nullptr;
     launch_shape shape;
-    ctx.tuning.lookup(sort_tuning_key(key_bytes, kv, n), shape);
+    if (!ctx.tuning.lookup(sort_tuning_key(key_bytes, kv, n), shape)) shape.variant = sort_default_variant(key_bytes, kv, n);
     if (key_bytes == 4) {
         const auto xf = dev::make_xform<uint32_t>(key_kind, descending);
         const auto* in = static_cast<const uint32_t*>(keys_in);

@@ -40,6 +40,8 @@ struct SortControl {
 }  // namespace onesweep
 
 int sort_variant_count(int key_bytes, bool has_values);
+//! The variant used when the tuning table has no entry for the workload.
+int sort_default_variant(int key_bytes, bool has_values, std::size_t n);
 std::string sort_tuning_key(int key_bytes, bool has_values, std::size_t n);
 
 }  // namespace gbc

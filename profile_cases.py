@@ -1,9 +1,10 @@
 """Profiling harness: runs one named workload a fixed number of times so that
 an ncu capture has a short, deterministic launch sequence.
 
-  python profile_cases.py CASE [--n N] [--iters K]
+  python profile_cases.py CASE [--n N] [--iters K] [--variant V]
 
-Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys), sort-kv64
+Cases: sort-kv (u32 keys + u32 values), sort-keys (u32 keys; both take
+--variant V to run digit-pass variant V), sort-kv64
 (u64 keys + u32 values), scan-i32 (exclusive, int64 total), reduce-i32,
 hist-u8 (256 bins), segsort-u64kv (lognormal segments, median 256, sigma 2,
 n = total keys), rbk-u64 (reduce_by_key over sorted keys with runs, fused
@@ -33,6 +34,8 @@ def main() -> None:
     ap.add_argument("case")
     ap.add_argument("--n", type=int, default=1 << 25)
     ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="sort cases: the digit-pass variant to use (tuning-table entry for this size)")
     args = ap.parse_args()
 
     import numpy as np
@@ -52,6 +55,9 @@ def main() -> None:
         k, ko = u32(n), torch.empty(n, dtype=torch.int32, device="cuda")
         v, vo = torch.arange(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")
         kv = args.case == "sort-kv"
+
+        if args.variant >= 0:
+            ctx.tuning_set(gbc.tuning_sort_key(4, kv, n), args.variant)
 
         def step():
             gbc.sort_raw(ctx, k.data_ptr(), ko.data_ptr(), np.uint32, n, v.data_ptr() if kv else 0,

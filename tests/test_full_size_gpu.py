@@ -1,11 +1,11 @@
 """The configurations at their full sizes, through the library's public calls,
 checked bit for bit against the oracle (the restated reference algorithms on
-every host thread): the 2^28 uniform key-value sort and its lowest-entropy
-form (keys the AND of 4 uniform words), 2^27 64-bit key-value pairs, the
-exclusive scan of 2^30 int32 with its exact int64 total, the 256-bin
-histogram of 2^30 bytes, the learned-CDF sort of 2^26 mixture floats, and
-bitpack compression of 2^28 timestamps (words equal to the oracle's, and the
-round trip). Inputs are seeded."""
+every host thread): the 2^28 uniform key-value and keys-only sorts, the
+key-value sort of keys that are the AND of 4 uniform words (its lowest
+entropy), 2^27 64-bit key-value pairs, the exclusive scan of 2^30 int32 with
+its exact int64 total, the 256-bin histogram of 2^30 bytes, the learned-CDF
+sort of 2^26 mixture floats, and bitpack compression of 2^28 timestamps
+(words equal to the oracle's, and the round trip). Inputs are seeded."""
 import numpy as np
 import pytest
 from helpers import learned_mixture
@@ -28,6 +28,15 @@ def _kv_sort_against_oracle(gbc, ctx, orc, keys):
 def test_kv_sort_2e28_uniform(gbc, ctx, orc):
     keys = np.random.default_rng(1).integers(0, 2**32, size=1 << 28, dtype=np.uint32)
     _kv_sort_against_oracle(gbc, ctx, orc, keys)
+
+
+def test_keys_sort_2e28_uniform(gbc, ctx, orc):
+    # keys only: the tile-offset form of the digit pass, the default at this size
+    keys = np.random.default_rng(4).integers(0, 2**32, size=1 << 28, dtype=np.uint32)
+    kb = gbc.DeviceBuffer.from_host(ctx, keys)
+    gbc.sort(ctx, kb)
+    orc.ref_radix_sort_inplace(keys)
+    assert np.array_equal(kb.to_host(), keys)
 
 
 def test_kv_sort_2e28_and_of_4_words(gbc, ctx, orc):

@@ -179,6 +179,38 @@ def test_repeated_calls_and_memory_reuse(ctx, gbc, orc):
     assert s.total_allocations > before
 
 
+# The tile-offset variants of the 32-bit keys-only list (PAD 1, PAD 0): every
+# tile's output offsets are counted before the pass instead of looked back.
+TILE_OFFSET_VARIANTS = (11, 12)
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float32])
+@pytest.mark.parametrize("descending", [False, True])
+def test_tile_offset_form_multi_tile_chunks(ctx, gbc, orc, dtype, descending):
+    # The tile-offset form (the default for keys without values from 2^27
+    # keys) forced at 5,000,003 keys: 814 tiles in chunks of 3, so the chunk
+    # scan carries offsets across chunks, the last chunk holds one tile and
+    # the last tile is partial; every 32-bit key transform, both directions,
+    # and one case whose constant top byte leaves an odd number of passes.
+    assert gbc.tuning_sort_variants(4, False) == 13
+    n = 5_000_003
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    cases = [bits, (bits & np.uint32(0x00FFFFFF)) | np.uint32(0x3F000000)]
+    key = gbc.tuning_sort_key(4, False, n)
+    try:
+        for var in TILE_OFFSET_VARIANTS:
+            ctx.tuning_set(key, var)
+            for raw in cases:
+                keys = raw.view(dtype)
+                exp = orc.ref_radix_sort(keys, None, descending)[0]
+                kb = gbc.DeviceBuffer.from_host(ctx, keys)
+                gbc.sort(ctx, kb, descending)
+                assert np.array_equal(kb.to_host().view(np.uint32), exp.view(np.uint32)), (var, dtype, descending)
+    finally:
+        ctx.tuning_set(key, 0)
+
+
 @pytest.mark.parametrize("key_dtype", [np.uint32, np.uint64])
 @pytest.mark.parametrize("with_values", [False, True])
 def test_every_compiled_variant(ctx, gbc, orc, key_dtype, with_values):

@@ -1416,6 +1416,10 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
     }
     seg_options so;
     so.skip = skip.as<uint8_t>();
+    // Buckets are mostly near the one-CTA capacity: twice the warps per CTA
+    // (one CTA per SM either way) finish them faster (2^28 mixture keys:
+    // 2.50 -> 1.92 ms for the one-CTA sorts, 7.72 -> 7.22 ms for the sort).
+    so.cta_threads = 512;
     segmented_sort(ctx, out, out, 4, key_kind, nullptr, nullptr, n, boff.as<uint32_t>(), buckets, false, so);
     {
         kernel_timer kt(ctx, "learned.check");

@@ -191,7 +191,7 @@ template <typename K, int TILE> __global__ void __launch_bounds__(1024) k_seg_pl
 
 // ---------------------------------------------------------------------------
 // Shared-memory LSD sort of one segment by a group of GW warps (GW = 1: a
-// warp on its own; GW = SMALL_WARPS: the whole CTA). Stable: items are ranked
+// warp on its own; GW = the CTA's warps: the whole CTA). Stable: items are ranked
 // in index order (warp chunk, row, lane) and scattered by digit.
 // ---------------------------------------------------------------------------
 template <int GW> __device__ __forceinline__ void group_sync()
@@ -366,8 +366,13 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_warp(SegArgs<K> a)
     seg_small_warp<K, HAS_V, SUB>(a);
 }
 
-template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_small_cta(const SegArgs<K>& a)
+// THREADS: 256, or 512 where the shared memory allows (twice the warps in
+// flight on the SM for the same shared-memory tile).
+template <typename K, bool HAS_V, bool SUB, int THREADS = SMALL_THREADS>
+__device__ __forceinline__ void seg_small_cta(const SegArgs<K>& a)
 {
+    constexpr int WARPS = THREADS / 32;
+    static_assert(THREADS % 32 == 0 && THREADS >= RADIX && WARPS <= 32, "one thread per bin; scratch holds 32 warps");
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t cap = SUB ? a.sub_cap : a.cta_cap;
     K* k0 = reinterpret_cast<K*>(smem);
@@ -376,8 +381,8 @@ template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_
     uint32_t* v1 = v0 + (HAS_V ? cap : 0);
     uint32_t* rd = v1 + (HAS_V ? cap : 0);
     uint32_t* hist = rd + cap;
-    uint32_t* masks = hist + SMALL_WARPS * RADIX;
-    for (int i = threadIdx.x; i < SMALL_WARPS * RADIX; i += SMALL_THREADS) masks[i] = 0;
+    uint32_t* masks = hist + WARPS * RADIX;
+    for (int i = threadIdx.x; i < WARPS * RADIX; i += THREADS) masks[i] = 0;
     __shared__ uint32_t scratch[64 + 8];
     __shared__ uint32_t s_work;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -398,16 +403,16 @@ template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_
             b = a.off[s];
             len = a.off[s + 1] - b;
         }
-        for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
+        for (uint32_t i = threadIdx.x; i < len; i += THREADS) {
             k0[i] = src_k[b + i];
             if (HAS_V) v0[i] = src_v[b + i];
         }
         __syncthreads();
         bool flipped = false;
-        group_sort<K, HAS_V, SMALL_WARPS>(k0, k1, v0, v1, rd, hist, masks, scratch, len, a.xf, warp, lane, flipped);
+        group_sort<K, HAS_V, WARPS>(k0, k1, v0, v1, rd, hist, masks, scratch, len, a.xf, warp, lane, flipped);
         const K* rk = flipped ? k1 : k0;
         const uint32_t* rv = flipped ? v1 : v0;
-        for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
+        for (uint32_t i = threadIdx.x; i < len; i += THREADS) {
             a.out_k[b + i] = rk[i];
             if (HAS_V) a.out_v[b + i] = rv[i];
         }
@@ -415,10 +420,17 @@ template <typename K, bool HAS_V, bool SUB> __device__ __forceinline__ void seg_
     }
 }
 
-template <typename K, bool HAS_V, bool SUB>
-__global__ void __launch_bounds__(SMALL_THREADS) k_seg_small_cta(SegArgs<K> a)
+template <typename K, bool HAS_V, bool SUB, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_seg_small_cta(SegArgs<K> a)
 {
-    seg_small_cta<K, HAS_V, SUB>(a);
+    seg_small_cta<K, HAS_V, SUB, THREADS>(a);
+}
+
+//! Shared memory of the one-CTA sort: two copies of keys (and values) and a
+//! packed rank per element, then a histogram and a peer-mask array per warp.
+template <typename K, bool HAS_V> constexpr std::size_t cta_sort_smem(uint32_t cap, int threads)
+{
+    return (std::size_t)cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * (std::size_t)(threads / 32) * RADIX * 4;
 }
 
 // ---------------------------------------------------------------------------
@@ -933,6 +945,29 @@ template <typename F> static int occupancy(F* kernel, int threads, std::size_t s
     return std::max(b, 1);
 }
 
+// The one-CTA sorts of the segments (SUB: sub-buckets) of at most cap keys:
+// 512 threads when threads == 512 and their shared memory fits the opt-in,
+// else 256. (Keys-only u32 at the largest capacity: 16,384 keys in 224 KiB
+// with 512 threads, one CTA per SM either way, so twice the warps hide the
+// shared-memory round trips.)
+template <typename K, bool HAS_V, bool SUB>
+static void launch_cta_sort(device_context& ctx, const SegArgs<K>& a, uint32_t cap, int threads, cudaStream_t st)
+{
+    auto wide = &k_seg_small_cta<K, HAS_V, SUB, 512>;
+    const std::size_t wsmem = cta_sort_smem<K, HAS_V>(cap, 512);
+    cudaFuncAttributes fa{};
+    check_cuda(cudaFuncGetAttributes(&fa, wide), "cudaFuncGetAttributes");
+    if (threads == 512 && wsmem + fa.sharedSizeBytes <= ctx.smem_optin) {
+        set_smem(wide, wsmem);
+        wide<<<ctx.sm_count * occupancy(wide, 512, wsmem), 512, wsmem, st>>>(a);
+    } else {
+        auto kern = &k_seg_small_cta<K, HAS_V, SUB, SMALL_THREADS>;
+        const std::size_t smem = cta_sort_smem<K, HAS_V>(cap, SMALL_THREADS);
+        set_smem(kern, smem);
+        kern<<<ctx.sm_count * occupancy(kern, SMALL_THREADS, smem), SMALL_THREADS, smem, st>>>(a);
+    }
+}
+
 template <typename K, bool HAS_V>
 void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uint32_t* out_v, std::size_t n,
          const uint32_t* off, std::size_t nseg, dev::KeyXform<K> xf, const seg_options& opt)
@@ -942,8 +977,9 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     constexpr int TILE = LS::THREADS * LS::ITEMS;
     // Largest segment one CTA sorts in shared memory: two copies of keys (and
     // values) plus a packed rank per element, and 16 KiB of warp histograms
-    // and peer masks, must fit the 227 KiB opt-in (u32: 12 B/elem keys-only,
-    // 20 B/elem with values; u64: 20 and 28 B/elem).
+    // and peer masks (256 threads; 32 KiB with 512), must fit the 227 KiB
+    // opt-in (u32: 12 B/elem keys-only, 20 B/elem with values; u64: 20 and
+    // 28 B/elem).
     constexpr int MAX_CAP = sizeof(K) == 4 ? (HAS_V ? 10240 : 16384) : (HAS_V ? 7168 : 10240);
     const uint32_t cta_cap =
         (uint32_t)std::max<int>(WARP_CAP + 1, std::min<int>(opt.cta_cap > 0 ? opt.cta_cap : MAX_CAP, MAX_CAP));
@@ -1001,9 +1037,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
 
     constexpr std::size_t per_warp_smem =
         2 * WARP_CAP * sizeof(K) + (HAS_V ? 2 * WARP_CAP * 4 : 0) + WARP_CAP * 4 + 2 * RADIX * 4;
-    auto cta_smem = [](uint32_t cap) {
-        return (std::size_t)cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * SMALL_WARPS * RADIX * 4;
-    };
+    auto cta_smem = [](uint32_t cap) { return cta_sort_smem<K, HAS_V>(cap, SMALL_THREADS); };
     // the large pass: two half-warp count arrays of RADIX + LARGE_PAD words per warp, and a tile
     constexpr std::size_t large_pass_smem = (std::size_t)(LS::THREADS / 32) * (RADIX + LARGE_PAD) * 8 +
                                             (std::size_t)TILE * sizeof(K) + (HAS_V ? (std::size_t)TILE * 4 : 0);
@@ -1065,11 +1099,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
     }
     {
         kernel_timer kt(ctx, "segsort.small_cta");
-        const std::size_t smem = (std::size_t)cta_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) + 2 * SMALL_WARPS * RADIX * 4;
-        auto kern = &k_seg_small_cta<K, HAS_V, false>;
-        set_smem(kern, smem);
-        const int grid = ctx.sm_count * occupancy(kern, SMALL_THREADS, smem);
-        kern<<<grid, SMALL_THREADS, smem, ctx.stream>>>(a);
+        launch_cta_sort<K, HAS_V, false>(ctx, a, cta_cap, opt.cta_threads, ctx.stream);
         check_cuda(cudaGetLastError(), "segmented sort cta launch");
     }
     if (maybe_large) {
@@ -1104,11 +1134,7 @@ void run(device_context& ctx, const K* in_k, K* out_k, const uint32_t* in_v, uin
             set_smem(wk, per_warp * SMALL_WARPS);
             wk<<<ctx.sm_count * occupancy(wk, SMALL_THREADS, per_warp * SMALL_WARPS), SMALL_THREADS,
                  per_warp * SMALL_WARPS, aux>>>(a);
-            const std::size_t csmem = (std::size_t)msd_cap * (2 * sizeof(K) + (HAS_V ? 8 : 0) + 4) +
-                                      2 * SMALL_WARPS * RADIX * 4;
-            auto ck = &k_seg_small_cta<K, HAS_V, true>;
-            set_smem(ck, csmem);
-            ck<<<ctx.sm_count * occupancy(ck, SMALL_THREADS, csmem), SMALL_THREADS, csmem, aux>>>(a);
+            launch_cta_sort<K, HAS_V, true>(ctx, a, msd_cap, opt.cta_threads, aux);
             check_cuda(cudaGetLastError(), "segmented sort sub-bucket launch");
         }
     }
@@ -1128,6 +1154,8 @@ std::string segsort_batch_tuning_key(int key_bytes, bool has_values, std::size_t
 {
     return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":batch";
 }
+
+std::string segsort_cta_threads_tuning_key() { return "segsort:cta_threads"; }
 
 std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
 {
@@ -1164,6 +1192,10 @@ void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, in
         o.msd_cap = ctx.tuning.lookup(segsort_msd_tuning_key(key_bytes, vals_in != nullptr, n, num_segments), shape)
                         ? shape.variant
                         : 0;
+    }
+    if (o.cta_threads == 0) {
+        launch_shape shape;
+        if (ctx.tuning.lookup(segsort_cta_threads_tuning_key(), shape)) o.cta_threads = shape.variant;
     }
     if (o.persistent < 0) {
         launch_shape shape;

@@ -47,6 +47,37 @@ def test_segmented_sort(ctx, gbc, orc, layout, key_dtype, with_values):
         assert np.array_equal(vb.to_host(), ev)
 
 
+@pytest.mark.parametrize("threads", [256, 512])
+@pytest.mark.parametrize("key_dtype,with_values", [(np.uint64, True), (np.uint32, False), (np.uint32, True)])
+def test_one_cta_sort_thread_counts(ctx, gbc, orc, threads, key_dtype, with_values):
+    # The one-CTA segment sorts at 256 threads and at 512 (taken wherever the
+    # capacity's shared memory fits, else 256), at two capacities: the
+    # type's largest and 2,048 keys.
+    off = offsets_from_lengths([256, 257, 700, 2047, 2048, 2049, 5000, 8191, 8192, 10240, 16384, 3, 1])
+    n = int(off[-1])
+    rng = np.random.default_rng(threads)
+    keys = rng.integers(0, 2**63, size=n, dtype=np.uint64).astype(key_dtype)
+    keys[::5] = keys[0]
+    vals = np.arange(n, dtype=np.uint32)
+    ek, ev = orc.std_segmented_sort(keys, off, vals if with_values else None)
+    ob = gbc.DeviceBuffer.from_host(ctx, off)
+    tag = "u64" if np.dtype(key_dtype).itemsize == 8 else "u32"
+    key = f"segsort:{tag}{'kv' if with_values else 'k'}:{_size_class(n)}:avg{_size_class(n // (off.size - 1))}"
+    try:
+        ctx.tuning_set("segsort:cta_threads", threads)
+        for cap in (0, 2048):  # 0: the type's largest capacity
+            ctx.tuning_set(key, cap)
+            kb = gbc.DeviceBuffer.from_host(ctx, keys)
+            vb = gbc.DeviceBuffer.from_host(ctx, vals) if with_values else None
+            gbc.segmented_sort(ctx, kb, ob, vb)
+            assert np.array_equal(kb.to_host(), ek), (threads, cap)
+            if with_values:
+                assert np.array_equal(vb.to_host(), ev), (threads, cap)
+    finally:
+        ctx.tuning_set("segsort:cta_threads", 0)
+        ctx.tuning_set(key, 0)
+
+
 def test_segmented_sort_out_of_place_descending(ctx, gbc, orc):
     off = orc.lognormal_segments(2000, 128, 2.0, 1, 1 << 16, seed=8)
     n = int(off[-1])

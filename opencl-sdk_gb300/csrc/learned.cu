@@ -46,6 +46,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "device_common.cuh"
@@ -69,7 +70,6 @@ constexpr int NCELLS = 1 << LUT_BITS;
 constexpr int PART_THREADS = 1024;
 constexpr int PART_ITEMS = 8;               // keys in flight per thread in the partition passes
 constexpr uint32_t PART_GROUP = 128;        // buckets per group of the first partition level
-constexpr uint32_t PART_RANGE = 2 * PART_THREADS;  // widest bucket range a second-level chunk stages
 
 __host__ __device__ __forceinline__ bool is_weight(int i)
 {
@@ -588,19 +588,19 @@ __host__ __device__ constexpr std::size_t part_smem_bytes(uint32_t buckets)
     return (std::size_t)buckets * 4 + (std::size_t)(buckets - 1) * 4 + (std::size_t)(NCELLS + 1) * 2;
 }
 
-// k_partition_buckets: 2 x PART_RANGE words, the staged chunk's keys and
-// buckets.
-__host__ __device__ constexpr std::size_t bucket_smem_bytes()
+// k_partition_buckets with T threads: 2 x (2T) words (the staged bucket
+// range), the staged chunk's keys and buckets.
+__host__ __device__ constexpr std::size_t bucket_smem_bytes(int T)
 {
-    return ((std::size_t)2 * PART_RANGE + (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
-           (std::size_t)PART_ITEMS * PART_THREADS * 2;
+    return ((std::size_t)2 * (2 * T) + (std::size_t)PART_ITEMS * T) * 4 + (std::size_t)PART_ITEMS * T * 2;
 }
 
-// k_partition_groups: 2 x groups words, the staged chunk's keys and buckets.
-__host__ __device__ constexpr std::size_t group_smem_bytes(uint32_t buckets)
+// k_partition_groups with T threads: 2 x groups words, the staged chunk's
+// keys and buckets.
+__host__ __device__ constexpr std::size_t group_smem_bytes(uint32_t buckets, int T)
 {
-    return ((std::size_t)2 * ((buckets + PART_GROUP - 1) / PART_GROUP) + (std::size_t)PART_ITEMS * PART_THREADS) * 4 +
-           (std::size_t)PART_ITEMS * PART_THREADS * 2;
+    return ((std::size_t)2 * ((buckets + PART_GROUP - 1) / PART_GROUP) + (std::size_t)PART_ITEMS * T) * 4 +
+           (std::size_t)PART_ITEMS * T * 2;
 }
 
 // Loads the splitters and the table into shared memory after a buckets-word
@@ -701,20 +701,21 @@ __global__ void k_cursors(const uint32_t* __restrict__ bucket_off, uint32_t buck
 // a chunk) takes one global cursor increment per key instead. The buckets
 // come with the keys (src_ids), so there is no search. Shared memory:
 // 2 x PART_RANGE words, the staged keys and their buckets relative to L (u16).
-__global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs a, const uint32_t* __restrict__ src,
-                                                                    const uint16_t* __restrict__ src_ids,
-                                                                    uint32_t* __restrict__ dst,
-                                                                    uint32_t* __restrict__ cursor)
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_partition_buckets(PartArgs a, const uint32_t* __restrict__ src,
+                                                                const uint16_t* __restrict__ src_ids,
+                                                                uint32_t* __restrict__ dst,
+                                                                uint32_t* __restrict__ cursor)
 {
     extern __shared__ uint32_t sh[];
-    constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
+    constexpr uint32_t PER = PART_ITEMS * T;
     constexpr uint32_t NONE = 0xFFFFFFFFu;
-    static_assert(PART_RANGE == 2 * PART_THREADS, "two range entries per thread");
+    constexpr uint32_t PART_RANGE = 2 * T;  // two range entries per thread
     uint32_t* hist = sh;                                       // [PART_RANGE]: counts, then chunk offsets
     uint32_t* delta = hist + PART_RANGE;                       // [PART_RANGE]: global start - chunk offset
     uint32_t* stage = delta + PART_RANGE;                      // [PER]
     uint16_t* sbkt = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
-    __shared__ uint32_t s_warp[PART_THREADS / 32], s_lo, s_hi;
+    __shared__ uint32_t s_warp[T / 32], s_lo, s_hi;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         s_lo = NONE;
@@ -727,7 +728,7 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
         uint32_t k[PART_ITEMS], b[PART_ITEMS], r[PART_ITEMS];
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) {
-            const uint32_t i = j * PART_THREADS + tid;
+            const uint32_t i = j * T + tid;
             k[j] = i < count ? src[first + i] : 0u;
             b[j] = i < count ? (uint32_t)src_ids[first + i] : NONE;
         }
@@ -750,7 +751,7 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
         const uint32_t L = s_lo, span = s_hi - s_lo + 1;  // every chunk holds at least one key
         const bool wide = span > PART_RANGE;
         if (!wide)
-            for (uint32_t e = tid; e < span; e += PART_THREADS) hist[e] = 0;
+            for (uint32_t e = tid; e < span; e += T) hist[e] = 0;
         __syncthreads();
         if (tid == 0) {  // for the next chunk: every thread has read L and span
             s_lo = NONE;
@@ -796,7 +797,7 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
                 sbkt[slot] = (uint16_t)(b[j] - L);
             }
         __syncthreads();
-        for (uint32_t i = tid; i < count; i += PART_THREADS) {
+        for (uint32_t i = tid; i < count; i += T) {
             const uint32_t pos = delta[sbkt[i]] + i;
             if (pos < a.n) dst[pos] = stage[i];
         }
@@ -811,19 +812,20 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_buckets(PartArgs 
 // reservation per group present, then written out run by run with
 // consecutive threads on consecutive addresses. Shared memory: 2 x groups
 // words, the staged keys and their buckets (u16).
-__global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a, uint32_t groups,
-                                                                   uint32_t* __restrict__ dst,
-                                                                   uint16_t* __restrict__ dst_ids,
-                                                                   uint32_t* __restrict__ cursor)
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_partition_groups(PartArgs a, uint32_t groups,
+                                                               uint32_t* __restrict__ dst,
+                                                               uint16_t* __restrict__ dst_ids,
+                                                               uint32_t* __restrict__ cursor)
 {
     extern __shared__ uint32_t sh[];
-    constexpr uint32_t PER = PART_ITEMS * PART_THREADS;
+    constexpr uint32_t PER = PART_ITEMS * T;
     constexpr uint32_t NONE = 0xFFFFFFFFu;
     uint32_t* hist = sh;                                       // [groups]: counts, then chunk offsets
     uint32_t* delta = hist + groups;                           // [groups]: global start - chunk offset
     uint32_t* stage = delta + groups;                          // [PER]
     uint16_t* sbkt = reinterpret_cast<uint16_t*>(stage + PER); // [PER]
-    __shared__ uint32_t s_warp[PART_THREADS / 32];
+    __shared__ uint32_t s_warp[T / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t chunks = (a.n + PER - 1) / PER;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
@@ -832,19 +834,19 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a
         uint32_t k[PART_ITEMS], bb[PART_ITEMS], g[PART_ITEMS], r[PART_ITEMS];
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) {
-            const uint32_t i = j * PART_THREADS + tid;
+            const uint32_t i = j * T + tid;
             k[j] = i < count ? a.keys[first + i] : 0u;
             bb[j] = i < count ? (uint32_t)a.ids[first + i] : 0u;
         }
         __syncthreads();  // the previous chunk's write-out is done
 #pragma unroll
-        for (int j = 0; j < PART_ITEMS; ++j) g[j] = j * PART_THREADS + tid < count ? bb[j] / PART_GROUP : NONE;
-        for (uint32_t i = tid; i < groups; i += PART_THREADS) hist[i] = 0;
+        for (int j = 0; j < PART_ITEMS; ++j) g[j] = j * T + tid < count ? bb[j] / PART_GROUP : NONE;
+        for (uint32_t i = tid; i < groups; i += T) hist[i] = 0;
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < PART_ITEMS; ++j) r[j] = g[j] != NONE ? atomicAdd(&hist[g[j]], 1u) : 0u;
         __syncthreads();
-        // chunk offsets (exclusive scan over groups <= PART_THREADS) and reservations
+        // chunk offsets (exclusive scan over groups <= T) and reservations
         const uint32_t v = tid < groups ? hist[tid] : 0u;
         const uint32_t incl = dev::warp_inclusive_scan(v, [](uint32_t p, uint32_t q) { return p + q; });
         if (lane == 31) s_warp[warp] = incl;
@@ -866,7 +868,7 @@ __global__ void __launch_bounds__(PART_THREADS, 1) k_partition_groups(PartArgs a
                 sbkt[slot] = (uint16_t)bb[j];
             }
         __syncthreads();
-        for (uint32_t i = tid; i < count; i += PART_THREADS) {
+        for (uint32_t i = tid; i < count; i += T) {
             const uint32_t b = sbkt[i];
             const uint32_t pos = delta[b / PART_GROUP] + i;
             if (pos < a.n) {
@@ -1384,25 +1386,49 @@ void learned_sort(device_context& ctx, const void* keys_in, void* keys_out, int 
         uint32_t* bucket_cur = cur.as<uint32_t>();
         uint32_t* group_cur = bucket_cur + buckets;
         k_cursors<<<(buckets + 255) / 256, 256, 0, ctx.stream>>>(boff.as<uint32_t>(), buckets, group_cur, bucket_cur);
-        {
+        // Threads per partition CTA, per level: 1024 (one CTA per SM), 512
+        // or 256 (two or four per SM, each CTA's barriers and reservation
+        // round trips overlapping the others' work; a chunk is 8 keys per
+        // thread). The first level needs groups <= threads. Measured at 2^28
+        // mixture keys (1024 / 512 / 256 threads): group level 1.36 / 1.11 /
+        // 1.53 ms (at 256, chunks of 2,048 keys leave ~10 keys per group and
+        // chunk), bucket level 1.12 / 0.98 / 0.91 ms. Defaults 512 and 256;
+        // the tuning table's "learned:group_threads" and
+        // "learned:bucket_threads" entries override them.
+        auto threads_of = [&](const char* key, int dflt, uint32_t need) {
+            launch_shape sh;
+            int t = ctx.tuning.lookup(key, sh) ? sh.variant : dflt;
+            if (t != 256 && t != 512) t = PART_THREADS;
+            return (uint32_t)t < need ? PART_THREADS : t;
+        };
+        const int gt = threads_of("learned:group_threads", 512, groups);
+        const int bt = threads_of("learned:bucket_threads", 256, 0);
+        auto group_level = [&](auto tc) {
+            constexpr int T = decltype(tc)::value;
             kernel_timer kt(ctx, "learned.partition_groups");
-            const std::size_t gsmem = group_smem_bytes(buckets);
-            check_cuda(cudaFuncSetAttribute(k_partition_groups, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            const std::size_t gsmem = group_smem_bytes(buckets, T);
+            check_cuda(cudaFuncSetAttribute(k_partition_groups<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)gsmem),
                        "cudaFuncSetAttribute");
-            k_partition_groups<<<(int)rows, PART_THREADS, gsmem, ctx.stream>>>(pa, groups, tmp.as<uint32_t>(),
-                                                                               tmp_ids.as<uint16_t>(), group_cur);
-        }
-        {
+            k_partition_groups<T><<<(int)rows * (PART_THREADS / T), T, gsmem, ctx.stream>>>(
+                pa, groups, tmp.as<uint32_t>(), tmp_ids.as<uint16_t>(), group_cur);
+        };
+        auto bucket_level = [&](auto tc) {
+            constexpr int T = decltype(tc)::value;
             kernel_timer kt(ctx, "learned.partition_buckets");
-            const std::size_t bsmem = bucket_smem_bytes();
-            check_cuda(cudaFuncSetAttribute(k_partition_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            const std::size_t bsmem = bucket_smem_bytes(T);
+            check_cuda(cudaFuncSetAttribute(k_partition_buckets<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)bsmem),
                        "cudaFuncSetAttribute");
-            k_partition_buckets<<<(int)rows, PART_THREADS, bsmem, ctx.stream>>>(pa, tmp.as<uint32_t>(),
-                                                                                tmp_ids.as<uint16_t>(), out,
-                                                                                bucket_cur);
-        }
+            k_partition_buckets<T><<<(int)rows * (PART_THREADS / T), T, bsmem, ctx.stream>>>(
+                pa, tmp.as<uint32_t>(), tmp_ids.as<uint16_t>(), out, bucket_cur);
+        };
+        if (gt == 256) group_level(std::integral_constant<int, 256>());
+        else if (gt == 512) group_level(std::integral_constant<int, 512>());
+        else group_level(std::integral_constant<int, PART_THREADS>());
+        if (bt == 256) bucket_level(std::integral_constant<int, 256>());
+        else if (bt == 512) bucket_level(std::integral_constant<int, 512>());
+        else bucket_level(std::integral_constant<int, PART_THREADS>());
         check_cuda(cudaGetLastError(), "learned partition launch");
     }
     // Finish every bucket that holds two different keys in place

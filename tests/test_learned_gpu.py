@@ -70,6 +70,23 @@ def test_learned_sort_is_bit_identical_to_plain(ctx, gbc, n):
     assert st.last_loss < st.first_loss
 
 
+@pytest.mark.parametrize("group_threads,bucket_threads", [(256, 1024), (512, 512), (1024, 256)])
+def test_partition_levels_at_every_cta_size(ctx, gbc, group_threads, bucket_threads):
+    # The two partition levels with 1, 2 or 4 CTAs per SM (1024, 512 or 256
+    # threads each, so 8,192, 4,096 or 2,048 keys per chunk): the same output.
+    keys = learned_mixture(3_000_001, seed=9)
+    ref = plain_sort(ctx, gbc, keys)
+    try:
+        ctx.tuning_set("learned:group_threads", group_threads)
+        ctx.tuning_set("learned:bucket_threads", bucket_threads)
+        out, st = learned(ctx, gbc, keys)
+    finally:
+        ctx.tuning_set("learned:group_threads", 512)
+        ctx.tuning_set("learned:bucket_threads", 256)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+    assert st.violation == 0 and st.fallback == 0
+
+
 def test_trained_network_beats_bucketing_without_it(ctx, gbc):
     # Without the network the keys are bucketed by equal-width ranges of the
     # key domain; the mixture's narrow clusters then fill a few buckets far

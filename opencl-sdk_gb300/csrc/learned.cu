@@ -528,25 +528,41 @@ __global__ void __launch_bounds__(REFINE_THREADS) k_refine_plan(uint32_t* __rest
     if (threadIdx.x == REFINE_THREADS - 1) *added = s_part[REFINE_THREADS - 1];
 }
 
-// The final splitters: root bucket b's granted splitters (offset off[b],
-// count off[b + 1] - off[b], or *added - off[b] for the last), then spm[b].
+// The final splitters, one thread per output position i. Root bucket b's
+// group (its granted splitters, then spm[b] unless b is the last) starts at
+// position b + off[b]; a thread finds its group by binary search, so a root
+// bucket granted thousands of splitters does not leave them to one thread.
+// Positions past the last group are 2^32 - 1 (empty buckets).
 __global__ void k_refine_write(const uint32_t* __restrict__ sorted, uint32_t s, const uint32_t* __restrict__ spm,
                                uint32_t bm, uint32_t buckets, const uint32_t* __restrict__ lo_in,
                                const uint32_t* __restrict__ off, const uint32_t* __restrict__ added,
                                uint32_t* __restrict__ sp)
 {
     const uint32_t total = *added;
+    const uint32_t used = bm - 1 + total;  // positions the groups fill
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < bm; b += stride) {
-        const uint32_t first = off[b], r = (b + 1 < bm ? off[b + 1] : total) - first;
-        const uint32_t lo = lo_in[b], hi = b + 1 < bm ? lo_in[b + 1] : s;
-        const uint32_t c = hi - lo;
-        const uint32_t base = b + first;  // b root splitters and `first` added ones come before
-        for (uint32_t j = 1; j <= r; ++j) sp[base + j - 1] = sorted[lo + (uint32_t)(((uint64_t)j * c) / (r + 1))];
-        if (b + 1 < bm) sp[base + r] = spm[b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i + 1 < buckets; i += stride) {
+        if (i >= used) {
+            sp[i] = 0xFFFFFFFFu;
+            continue;
+        }
+        // the last root bucket whose group starts at or before i (group 0 starts at 0)
+        uint32_t lo_b = 1, hi_b = bm;
+        while (lo_b < hi_b) {
+            const uint32_t m = (lo_b + hi_b) >> 1;
+            if (m + off[m] <= i) lo_b = m + 1;
+            else hi_b = m;
+        }
+        const uint32_t b = lo_b - 1;
+        const uint32_t j = i - (b + off[b]);
+        const uint32_t r = (b + 1 < bm ? off[b + 1] : total) - off[b];
+        if (j < r) {
+            const uint32_t l = lo_in[b], h = b + 1 < bm ? lo_in[b + 1] : s;
+            sp[i] = sorted[l + (uint32_t)(((uint64_t)(j + 1) * (h - l)) / (r + 1))];
+        } else {
+            sp[i] = spm[b];  // j == r: the root splitter closing group b (b + 1 < bm)
+        }
     }
-    for (uint32_t i = bm - 1 + total + blockIdx.x * blockDim.x + threadIdx.x; i + 1 < buckets; i += stride)
-        sp[i] = 0xFFFFFFFFu;
 }
 
 // ---- 5. partition ----------------------------------------------------------
@@ -1198,8 +1214,8 @@ uint32_t build_model(device_context& ctx, const uint32_t* sorted, uint32_t S, ui
             k_refine_want<<<(bm + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, spm, bm, n, cap, std::max(1u, cap / 2),
                                                                      lo, want);
             k_refine_plan<<<1, REFINE_THREADS, 0, ctx.stream>>>(want, bm, budget, m.est + 1);
-            k_refine_write<<<(bm + 255) / 256, 256, 0, ctx.stream>>>(sorted, S, spm, bm, buckets, lo, want, m.est + 1,
-                                                                      m.sp);
+            k_refine_write<<<std::max(1u, (buckets + 254) / 256), 256, 0, ctx.stream>>>(sorted, S, spm, bm, buckets, lo, want,
+                                                                           m.est + 1, m.sp);
         }
         k_lut<<<(NCELLS + 1 + 255) / 256, 256, 0, ctx.stream>>>(m.sp, buckets, m.frame, m.lut);
         check_cuda(cudaGetLastError(), "learned splitter launch");

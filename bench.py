@@ -581,12 +581,12 @@ def main() -> None:
 
     run_lanes(1)  # warm-up: every context's arena and first step
     per_lane = max(2, e2e_steps // len(lanes))
-    # Three timed runs, the median reported (as the reference arm reports the
+    # Seven timed runs, the median reported (as the reference arm reports the
     # median of its steps): a host-side stall of 40-100 ms, seen now and then
     # on these machines in a single blocking copy, would otherwise decide the
-    # figure of a ~130 ms run.
+    # figure of a ~130 ms run, and stalls have hit two runs of three.
     runs_s = []
-    for _ in range(3):
+    for _ in range(7):
         barrier()
         t0 = time.perf_counter()
         run_lanes(per_lane)
@@ -597,7 +597,7 @@ def main() -> None:
     e2e = {"value": n * world / pipe_s / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": 8 * n,
            "d2h_bytes_per_step": 8 * n, "ms_per_step": pipe_s * 1e3, "bitexact": pipe_ok and e2e_ok,
            "steps": len(lanes) * per_lane, "runs_ms_per_step": [round(r * 1e3, 3) for r in runs_s],
-           "reported": "the median of three timed runs",
+           "reported": "the median of seven timed runs",
            "path": "per step: clc_buffer_write x2 (pinned host) -> clc_sort -> clc_buffer_read x2; three contexts "
                    "on the device, three host threads taking alternate steps, one lane at a time per copy "
                    "direction",

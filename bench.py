@@ -906,6 +906,7 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
 
     seg_key = f"segsort:u64kv:{size_class(total)}:avg{size_class(total // lens.size)}"
     msd_cap = ctx.tuning_get(seg_key + ":msd")
+    seg_threads = ctx.tuning_get(seg_key + ":threads")
     seg_form = ctx.tuning_get(seg_key + ":batch")
     batch()
     ctx.finish()
@@ -988,7 +989,7 @@ def run_extras(ctx, gbc, torch, np, stream, timed, uniform_u32, n, peak, steps, 
     seg_bytes = 24 * (total - large_keys) + (8 + 8 * 24) * large_keys + 8 * total
     entry("segmented_sort_u64kv_200k_lognormal", total, "Gkeys/s", ms_seg, seg_bytes, ok, prof_s,
           {"segments": int(lens.size), "total_keys": total, "graph": True, "autotuned_cta_capacity": seg_cap,
-           "autotuned_msd_capacity": msd_cap,
+           "autotuned_msd_capacity": msd_cap, "autotuned_cta_threads": seg_threads,
            "autotuned_form": {0: "launch sequence on two streams", 1: "one persistent launch"}.get(
                seg_form, f"one persistent launch, {seg_form - 1}/8 of its CTAs on the small segments"),
            "one_launch": {"ms": ms_one, "gkeys": total / (ms_one * 1e-3) / 1e9, "bitexact": one_ok,

@@ -516,7 +516,10 @@ GBC_EXPORT clc_status clc_autotune_sort(clc_context ctx, const void* keys_in, vo
                                         const uint32_t* vals_in, uint32_t* vals_out, size_t n, int repetitions,
                                         int* best_variant, double* best_ms);
 /* The same for the segmented sort: the candidates are capacities of its
- * one-CTA size class; the key adds the class of the average segment length. */
+ * one-CTA size class; the key adds the class of the average segment length.
+ * The MSD route's capacity, the one-CTA sorts' thread count and the launch
+ * form are tuned after it and stored under the same key with ":msd",
+ * ":threads" and ":batch". */
 GBC_EXPORT clc_status clc_autotune_segmented_sort(clc_context ctx, const void* keys_in, void* keys_out,
                                                   clc_type key_type, const uint32_t* vals_in, uint32_t* vals_out,
                                                   size_t n, const uint32_t* offsets, size_t num_segments,

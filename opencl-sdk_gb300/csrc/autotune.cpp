@@ -126,6 +126,7 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         o.cta_cap = c;
         o.msd_cap = 0;
         o.persistent = 0;
+        o.cta_threads = 256;
         r.ms.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);
@@ -144,12 +145,31 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         o.cta_cap = r.best;
         o.msd_cap = c;
         o.persistent = 0;
+        o.cta_threads = 256;
         m.ms.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);
         }));
     }
     pick(m, ctx);
+    // Then the one-CTA sorts' thread count at those capacities: 256, or 512
+    // (twice the warps per CTA; it pays for segments near the capacity and
+    // costs for batches of mostly short ones), stored under its own key.
+    autotune_result t;
+    t.key = segsort_threads_tuning_key(key_bytes, kv, n, num_segments);
+    for (int threads : {256, 512}) {
+        seg_options o;
+        o.cta_cap = r.best;
+        o.msd_cap = m.best;
+        o.persistent = 0;
+        o.cta_threads = threads;
+        t.candidates.push_back(threads);
+        t.ms.push_back(ev.time(ctx, repetitions, [&] {
+            segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
+                           false, o);
+        }));
+    }
+    pick(t, ctx);
     // Last, the launch form: the launch sequence at that capacity against the
     // one persistent launch (every CTA on both paths, or 1/8 .. 3/8 of them
     // on the small and medium segments), at capacities whose shared memory
@@ -158,7 +178,7 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         int persistent, cap;
     };
     std::vector<form> forms{{0, r.best}};
-    std::vector<double> times{std::min(r.best_ms, m.best_ms)};
+    std::vector<double> times{std::min({r.best_ms, m.best_ms, t.best_ms})};
     for (int mode = 1; mode <= 4; ++mode)
         for (int c : {1024, 2048}) forms.push_back({mode, std::min(c, cap)});
     for (std::size_t f = 1; f < forms.size(); ++f) {
@@ -166,6 +186,7 @@ autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in
         o.cta_cap = forms[f].cap;
         o.msd_cap = m.best;
         o.persistent = forms[f].persistent;
+        o.cta_threads = 256;  // the persistent kernel's CTAs have 256 threads
         times.push_back(ev.time(ctx, repetitions, [&] {
             segmented_sort(ctx, keys_in, keys_out, key_bytes, key_kind, vals_in, vals_out, n, offsets, num_segments,
                            false, o);

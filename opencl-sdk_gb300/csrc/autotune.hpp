@@ -27,9 +27,12 @@ struct autotune_result {
 autotune_result autotune_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes, int key_kind,
                               const uint32_t* vals_in, uint32_t* vals_out, std::size_t n, int repetitions);
 
-//! Segmented sort: the capacity of the one-CTA size class (segments up to
-//! that length are sorted in one CTA's shared memory, longer ones by the
-//! batched onesweep); keys_in must differ from keys_out.
+//! Segmented sort, in four stages on the caller's batch: the capacity of the
+//! one-CTA size class (segments up to that length are sorted in one CTA's
+//! shared memory, longer ones by the batched onesweep), the MSD route's
+//! bucket capacity, the one-CTA sorts' thread count (256 or 512), and the
+//! launch form (the launch sequence or one persistent launch); each is
+//! stored under its own key. keys_in must differ from keys_out.
 autotune_result autotune_segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, int key_bytes,
                                         int key_kind, const uint32_t* vals_in, uint32_t* vals_out, std::size_t n,
                                         const uint32_t* offsets, std::size_t num_segments, int repetitions);

@@ -1157,6 +1157,11 @@ std::string segsort_batch_tuning_key(int key_bytes, bool has_values, std::size_t
 
 std::string segsort_cta_threads_tuning_key() { return "segsort:cta_threads"; }
 
+std::string segsort_threads_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
+{
+    return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":threads";
+}
+
 std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments)
 {
     return segsort_tuning_key(key_bytes, has_values, n, num_segments) + ":msd";
@@ -1195,7 +1200,9 @@ void segmented_sort(device_context& ctx, const void* keys_in, void* keys_out, in
     }
     if (o.cta_threads == 0) {
         launch_shape shape;
-        if (ctx.tuning.lookup(segsort_cta_threads_tuning_key(), shape)) o.cta_threads = shape.variant;
+        if (ctx.tuning.lookup(segsort_threads_tuning_key(key_bytes, vals_in != nullptr, n, num_segments), shape) ||
+            ctx.tuning.lookup(segsort_cta_threads_tuning_key(), shape))
+            o.cta_threads = shape.variant;
     }
     if (o.persistent < 0) {
         launch_shape shape;

@@ -27,7 +27,9 @@ struct seg_options {
     int persistent = -1;
     // threads of each one-CTA segment sort: 256, or 512 (where the shared
     // memory of the CTA's capacity fits, else 256), which doubles the warps
-    // in flight. 0: the tuning table's "segsort:cta_threads" entry, else 256.
+    // in flight. 0: the tuning table's entry for this workload (the
+    // segmented key with ":threads", stored by the autotuner), else its
+    // "segsort:cta_threads" entry, else 256.
     // 512 pays for segments near the capacity (the learned sort's buckets:
     // 2.50 -> 1.92 ms at 2^28 keys) and costs for batches of mostly short
     // ones (200,000 lognormal segments of median 256: 24.7 -> 25.7 ms).
@@ -54,6 +56,9 @@ std::string segsort_batch_tuning_key(int key_bytes, bool has_values, std::size_t
 //! The tuning-table key of the one-CTA sorts' thread count (256 or 512; one
 //! entry for every segmented sort of the context).
 std::string segsort_cta_threads_tuning_key();
+//! The tuning-table key of the one-CTA sorts' thread count for one workload
+//! class (the segmented key with ":threads").
+std::string segsort_threads_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
 //! The tuning-table key of the MSD route's bucket capacity (0: off).
 std::string segsort_msd_tuning_key(int key_bytes, bool has_values, std::size_t n, std::size_t num_segments);
 

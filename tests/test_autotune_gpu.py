@@ -40,6 +40,19 @@ def test_autotune_segmented_sort_stores_a_capacity(ctx, gbc, orc):
     assert 1024 <= cap and ms > 0
     rk, rv = orc.std_segmented_sort(keys, off, vals)
     assert np.array_equal(kout.to_host(), rk) and np.array_equal(vout.to_host(), rv)
+    # every stage stored its choice under the workload's key
+    k = 0
+    while (1 << k) < n:
+        k += 1
+    a = 0
+    while (1 << a) < n // (off.size - 1):
+        a += 1
+    key = f"segsort:u64kv:2^{k}:avg2^{a}"
+    assert ctx.tuning_get(key) == cap
+    assert ctx.tuning_get(key + ":threads") in (256, 512)
+    assert ctx.tuning_get(key + ":batch") in range(0, 5)
+    for suffix in ("", ":msd", ":threads", ":batch"):
+        ctx.tuning_set(key + suffix, 0)
 
 
 def test_autotune_rejects_in_place(ctx, gbc):

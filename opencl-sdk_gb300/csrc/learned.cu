@@ -708,15 +708,15 @@ __global__ void k_cursors(const uint32_t* __restrict__ bucket_off, uint32_t buck
 }
 
 // Second partition level, keys only (the order inside a bucket is free):
-// src holds the keys grouped by bucket group, so a chunk of PART_ITEMS x
-// PART_THREADS keys spans a narrow bucket range [L, R]. Per chunk: ranks
+// src holds the keys grouped by bucket group, so a chunk of PART_ITEMS x T
+// keys (T threads per CTA) spans a narrow bucket range [L, R]. Per chunk: ranks
 // within each bucket by shared atomics over that range, the chunk staged in
 // shared memory in bucket order, one global reservation per bucket present,
 // then written out run by run with consecutive threads on consecutive
-// addresses. A chunk wider than PART_RANGE buckets (groups much smaller than
-// a chunk) takes one global cursor increment per key instead. The buckets
-// come with the keys (src_ids), so there is no search. Shared memory:
-// 2 x PART_RANGE words, the staged keys and their buckets relative to L (u16).
+// addresses. A chunk wider than 2T buckets (groups much smaller than a
+// chunk) takes one global cursor increment per key instead. The buckets come
+// with the keys (src_ids), so there is no search. Shared memory: 2 x 2T
+// words, the staged keys and their buckets relative to L (u16).
 template <int T>
 __global__ void __launch_bounds__(T, 1024 / T) k_partition_buckets(PartArgs a, const uint32_t* __restrict__ src,
                                                                 const uint16_t* __restrict__ src_ids,
@@ -823,7 +823,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_partition_buckets(PartArgs a, c
 // First partition level, keys only: every key, with its bucket, to its
 // bucket group (bucket / PART_GROUP; the buckets are those the counting pass
 // stored, so the group regions hold exactly their counted keys). Per chunk
-// of PART_ITEMS x PART_THREADS keys: ranks within each group by shared
+// of PART_ITEMS x T keys (T threads per CTA, T >= groups): ranks within each group by shared
 // atomics, the chunk staged in shared memory in group order, one global
 // reservation per group present, then written out run by run with
 // consecutive threads on consecutive addresses. Shared memory: 2 x groups
